@@ -1,0 +1,254 @@
+"""Host-side mirror of the reference's builder interface.
+
+``BVHBuilder`` follows include/bvh_builder.h:10-37 (getName, build, getNodes, getIndices,
+getLastBuildTimeMS, getTimingBreakdown); ``TriangleMesh`` follows include/mesh.h:9-50 (nine
+float32 SoA arrays).  The concrete builders stand in for LBVHBuilderCUDA
+(src/cuda/lbvh_builder.cuh:16-64), LBVHPlusBuilderCUDA (src/cuda/lbvh_plus_builder.cuh:11-61)
+and PLOCBuilderCUDA (src/cuda/ploc_builder.cuh:10-67) and run every step on the GPU through
+the C ABI (include/bvh_gb300.h).  Errors raise ``BVHError`` (a RuntimeError), as the
+reference's callers expect std::exception.
+
+``Context.build_device`` is the device-resident path (inputs already in HBM, tree stays there).
+"""
+from __future__ import annotations
+
+import abc
+import ctypes
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _capi as C
+
+
+@dataclass
+class TriangleMesh:
+    """SoA triangle mesh (include/mesh.h:9-50): v0x..v2z, float32, one entry per triangle."""
+    v0x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v0y: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v0z: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v1x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v1y: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v1z: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v2x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v2y: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    v2z: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+
+    def __post_init__(self):
+        for f in C.MESH_FIELDS:
+            a = np.ascontiguousarray(getattr(self, f), dtype=np.float32)
+            setattr(self, f, a)
+        n = {getattr(self, f).shape[0] for f in C.MESH_FIELDS}
+        if len(n) != 1:
+            raise ValueError("all nine SoA arrays must have the same length")
+
+    @classmethod
+    def from_vertices(cls, v0: np.ndarray, v1: np.ndarray, v2: np.ndarray) -> "TriangleMesh":
+        """From three (n, 3) vertex arrays."""
+        return cls(v0[:, 0], v0[:, 1], v0[:, 2], v1[:, 0], v1[:, 1], v1[:, 2], v2[:, 0], v2[:, 1], v2[:, 2])
+
+    def arrays(self) -> Sequence[np.ndarray]:
+        return [getattr(self, f) for f in C.MESH_FIELDS]
+
+    def size(self) -> int:
+        return int(self.v0x.shape[0])
+
+    def __len__(self) -> int:
+        return self.size()
+
+    def getTriangleBounds(self, i: int):
+        """mesh.h:36-49: (min, max) of triangle i."""
+        v = np.array([[self.v0x[i], self.v0y[i], self.v0z[i]], [self.v1x[i], self.v1y[i], self.v1z[i]],
+                      [self.v2x[i], self.v2y[i], self.v2z[i]]], np.float32)
+        return v.min(0), v.max(0)
+
+
+class Context:
+    """A library context on one CUDA device (owns the workspace and the last tree)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = C.load_library()
+        h = ctypes.c_void_p()
+        C.check(self.lib.bvh_ctx_create(ctypes.byref(h), int(device)), "bvh_ctx_create")
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.bvh_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self, algo: int, morton_bits: Optional[int] = None, treelet_rounds: Optional[int] = None,
+               ploc_radius: Optional[int] = None, max_iterations: Optional[int] = None) -> C.Params:
+        p = self.lib.bvh_default_params(algo)
+        if morton_bits is not None:
+            p.morton_bits = morton_bits
+        if treelet_rounds is not None:
+            p.treelet_rounds = treelet_rounds
+        if ploc_radius is not None:
+            p.ploc_radius = ploc_radius
+        if max_iterations is not None:
+            p.max_iterations = max_iterations
+        return p
+
+    def reserve(self, n: int, algo: int = C.ALGO_LBVH):
+        C.check(self.lib.bvh_ctx_reserve(self.handle, n, algo), "bvh_ctx_reserve")
+
+    def build_device(self, ptrs: Sequence[int], n: int, params: C.Params, stream: int = 0) -> C.Tree:
+        """Build from nine device addresses; asynchronous on `stream` (a cudaStream_t value)."""
+        m = C.mesh_struct(ptrs, n)
+        t = C.Tree()
+        C.check(self.lib.bvh_build_device(self.handle, ctypes.byref(m), ctypes.byref(params),
+                                          ctypes.c_void_p(stream), ctypes.byref(t)), "bvh_build_device")
+        return t
+
+    def build_host(self, mesh: TriangleMesh, params: C.Params, stream: int = 0):
+        """Upload, build, download (BVHBuilder::build).  Returns (nodes, indices)."""
+        n = mesh.size()
+        arrs = mesh.arrays()
+        m = C.mesh_struct([a.ctypes.data for a in arrs], n)
+        nodes = np.zeros(max(2 * n - 1, 0), C.NODE_DTYPE)
+        idx = np.zeros(n, np.uint32)
+        nn = ctypes.c_uint32(0)
+        C.check(self.lib.bvh_build_host(self.handle, ctypes.byref(m), ctypes.byref(params), ctypes.c_void_p(stream),
+                                        nodes.ctypes.data if n else None, idx.ctypes.data if n else None,
+                                        ctypes.byref(nn)), "bvh_build_host")
+        return nodes[: nn.value], idx
+
+    def download(self, tree: C.Tree, stream: int = 0):
+        nodes = np.zeros(tree.n_nodes, C.NODE_DTYPE)
+        idx = np.zeros(tree.n_prims, np.uint32)
+        if tree.n_nodes:
+            C.check(self.lib.bvh_tree_download(self.handle, ctypes.byref(tree), ctypes.c_void_p(stream),
+                                               nodes.ctypes.data, idx.ctypes.data), "bvh_tree_download")
+        return nodes, idx
+
+    def sync(self):
+        C.check(self.lib.bvh_sync(self.handle), "bvh_sync")
+
+    def last_timing(self) -> C.Timing:
+        t = C.Timing()
+        C.check(self.lib.bvh_last_timing(self.handle, ctypes.byref(t)), "bvh_last_timing")
+        return t
+
+    def trace(self, nodes_ptr: int, n_nodes: int, mesh_ptrs: Sequence[int], n_tris: int, ray_ptrs: Sequence[int],
+              n_rays: int, hit_ptrs: Sequence[int], stream: int = 0):
+        m = C.mesh_struct(mesh_ptrs, n_tris)
+        r = C.Rays(*ray_ptrs, n_rays)
+        h = C.Hits(*hit_ptrs)
+        C.check(self.lib.bvh_trace(self.handle, ctypes.c_void_p(nodes_ptr), n_nodes, ctypes.byref(m), ctypes.byref(r),
+                                   ctypes.byref(h), ctypes.c_void_p(stream)), "bvh_trace")
+
+    def trace_pinhole(self, nodes_ptr: int, n_nodes: int, mesh_ptrs: Sequence[int], n_tris: int, cam: C.Camera,
+                      width: int, height: int, hit_ptrs: Sequence[int], stream: int = 0):
+        m = C.mesh_struct(mesh_ptrs, n_tris)
+        h = C.Hits(*hit_ptrs)
+        C.check(self.lib.bvh_trace_pinhole(self.handle, ctypes.c_void_p(nodes_ptr), n_nodes, ctypes.byref(m),
+                                           ctypes.byref(cam), width, height, ctypes.byref(h),
+                                           ctypes.c_void_p(stream)), "bvh_trace_pinhole")
+
+
+def auto_camera(root_node) -> C.Camera:
+    """autoCamera (src/render_engine.cu:601-637) from a host root node (NODE_DTYPE record) or None."""
+    lib = C.load_library()
+    cam = C.Camera()
+    if root_node is None:
+        C.check(lib.bvh_auto_camera(None, ctypes.byref(cam)))
+    else:
+        rec = np.array([root_node], C.NODE_DTYPE)
+        C.check(lib.bvh_auto_camera(ctypes.c_void_p(rec.ctypes.data), ctypes.byref(cam)))
+    return cam
+
+
+class BVHBuilder(abc.ABC):
+    """include/bvh_builder.h:10-37."""
+
+    @abc.abstractmethod
+    def getName(self) -> str: ...
+
+    @abc.abstractmethod
+    def build(self, mesh: TriangleMesh) -> None: ...
+
+    @abc.abstractmethod
+    def getNodes(self) -> np.ndarray: ...
+
+    @abc.abstractmethod
+    def getIndices(self) -> np.ndarray: ...
+
+    @abc.abstractmethod
+    def getLastBuildTimeMS(self) -> float: ...
+
+    def getTimingBreakdown(self) -> str:
+        return ""
+
+
+class _GpuBuilder(BVHBuilder):
+    _algo = C.ALGO_LBVH
+
+    def __init__(self, device: int = 0, **params):
+        self._ctx = Context(device)
+        self._params = self._ctx.params(self._algo, **params)
+        self._nodes = np.zeros(0, C.NODE_DTYPE)
+        self._indices = np.zeros(0, np.uint32)
+        self._timing = C.Timing()
+
+    def build(self, mesh: TriangleMesh) -> None:
+        self._nodes, self._indices = self._ctx.build_host(mesh, self._params)
+        self._timing = self._ctx.last_timing() if mesh.size() else C.Timing()
+
+    def getNodes(self) -> np.ndarray:
+        return self._nodes
+
+    def getIndices(self) -> np.ndarray:
+        return self._indices
+
+    def getLastBuildTimeMS(self) -> float:
+        """Device time of the build kernels (upload excluded), bvh_builder.h:29-31."""
+        return float(self._timing.total_ms)
+
+    def getTimingBreakdown(self) -> str:
+        t = self._timing
+        return (f"  Scene bounds:     {t.bounds_ms:.3f} ms\n"
+                f"  Morton + boxes:   {t.morton_ms:.3f} ms\n"
+                f"  Radix sort:       {t.sort_ms:.3f} ms\n"
+                f"  Hierarchy+refit:  {t.emit_ms:.3f} ms\n"
+                f"  Optimise/cluster: {t.optimize_ms:.3f} ms")
+
+
+class LBVHBuilder(_GpuBuilder):
+    """LBVHBuilderCUDA: 30-bit Morton by default (morton_bits=60 or 63 for longer keys)."""
+    _algo = C.ALGO_LBVH
+
+    def getName(self) -> str:
+        return "LBVH" if self._params.morton_bits == 30 else f"LBVH-{self._params.morton_bits}"
+
+
+class LBVHPlusBuilder(_GpuBuilder):
+    """LBVHPlusBuilderCUDA: 60-bit Morton, one treelet pass by default."""
+    _algo = C.ALGO_LBVH_PLUS
+
+    def getName(self) -> str:
+        return "LBVH+"
+
+
+class PLOCBuilder(_GpuBuilder):
+    """PLOCBuilderCUDA(r): radius-r nearest-neighbour clustering."""
+    _algo = C.ALGO_PLOC
+
+    def __init__(self, r: int = 25, device: int = 0, **params):
+        super().__init__(device, ploc_radius=r, **params)
+
+    def getName(self) -> str:
+        return f"PLOC CUDA (r={self._params.ploc_radius})"
+
+    def getTimingBreakdown(self) -> str:
+        t = self._timing
+        return (f"  Initialization:   {t.bounds_ms + t.morton_ms + t.sort_ms + t.emit_ms:.3f} ms\n"
+                f"  Clustering:       {t.optimize_ms:.3f} ms ({t.ploc_iterations} iterations)")

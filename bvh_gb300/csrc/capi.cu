@@ -1,0 +1,366 @@
+// capi.cu -- the C ABI (include/bvh_gb300.h): contexts, builds, timing, traversal.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/bvh_gb300.h"
+#include "lbvh.cuh"
+#include "trace.cuh"
+
+using namespace bvhgb;
+
+struct bvh_ctx {
+  int device = 0;
+  Workspace ws;
+  StageEvents evs;
+  bvh_timing last{};
+  int last_algo = -1;
+  bool have_timing = false;
+  uint32_t* h_status = nullptr;  // pinned copy of the device status word
+  cudaStream_t last_stream = nullptr;
+};
+
+static bvh_status from_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return BVH_OK;
+  if (e == cudaErrorMemoryAllocation) return BVH_ERR_OUT_OF_MEMORY;
+  return BVH_ERR_DEVICE;
+}
+
+extern "C" const char* bvh_status_string(bvh_status s) {
+  switch (s) {
+    case BVH_OK: return "ok";
+    case BVH_ERR_INVALID_ARG: return "invalid argument";
+    case BVH_ERR_OUT_OF_MEMORY: return "out of memory";
+    case BVH_ERR_NO_PROGRESS: return "no progress (PLOC found no mutual pair or hit its iteration cap)";
+    case BVH_ERR_DEVICE: return "CUDA device error";
+    case BVH_ERR_TIMEOUT: return "device-side wait timed out";
+    case BVH_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+extern "C" const char* bvh_version(void) { return "bvh_gb300 0.1 (sm_103a)"; }
+
+extern "C" bvh_params bvh_default_params(int32_t algo) {
+  bvh_params p;
+  memset(&p, 0, sizeof(p));
+  p.algo = algo;
+  p.morton_bits = algo == BVH_ALGO_LBVH_PLUS ? 60 : 30;
+  p.treelet_rounds = 1;
+  p.ploc_radius = 25;
+  p.max_iterations = 0;
+  return p;
+}
+
+extern "C" bvh_status bvh_ctx_create(bvh_ctx** out, int device) {
+  if (!out) return BVH_ERR_INVALID_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return BVH_ERR_INVALID_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return BVH_ERR_DEVICE;
+  bvh_ctx* c = new (std::nothrow) bvh_ctx();
+  if (!c) return BVH_ERR_OUT_OF_MEMORY;
+  c->device = device;
+  for (int k = 0; k < 8; ++k)
+    if (cudaEventCreate(&c->evs.ev[k]) != cudaSuccess) { delete c; return BVH_ERR_DEVICE; }
+  c->evs.use = true;
+  if (cudaMallocHost(&c->h_status, 64) != cudaSuccess) { delete c; return BVH_ERR_OUT_OF_MEMORY; }
+  *out = c;
+  return BVH_OK;
+}
+
+extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
+  if (!ctx) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  workspace_free(ctx->ws);
+  for (int k = 0; k < 8; ++k) cudaEventDestroy(ctx->evs.ev[k]);
+  cudaFreeHost(ctx->h_status);
+  delete ctx;
+  return BVH_OK;
+}
+
+extern "C" bvh_status bvh_ctx_reserve(bvh_ctx* ctx, uint32_t n, int32_t algo) {
+  if (!ctx) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = workspace_reserve(ctx->ws, n);
+  if (e == cudaSuccess && algo == BVH_ALGO_PLOC) e = workspace_reserve_ploc(ctx->ws, n);
+  return from_cuda(e);
+}
+
+extern "C" bvh_status bvh_ctx_device_bytes(const bvh_ctx* ctx, uint64_t* bytes) {
+  if (!ctx || !bytes) return BVH_ERR_INVALID_ARG;
+  const Workspace& w = ctx->ws;
+  uint64_t b = 0;
+  if (w.cap_n) b += (uint64_t)w.cap_n * (8 * 2 + 4 * 2 + sizeof(Box) + 2 * sizeof(Node) + 8) + w.scratch_words * 4;
+  if (w.ploc_cap) b += (uint64_t)w.ploc_cap * (2 * sizeof(Box) + 8 + 4) + (w.ploc_cap / 2048 + 8) * 8;
+  b += (uint64_t)w.mesh_cap * 36;
+  *bytes = b;
+  return BVH_OK;
+}
+
+static bool valid_params(const bvh_params* p) {
+  if (!p) return false;
+  switch (p->algo) {
+    case BVH_ALGO_LBVH:
+      return p->morton_bits == 30 || p->morton_bits == 60 || p->morton_bits == 63;
+    case BVH_ALGO_LBVH_PLUS:
+      return (p->morton_bits == 30 || p->morton_bits == 60 || p->morton_bits == 63) && p->treelet_rounds >= 0 &&
+             p->treelet_rounds <= 64;
+    case BVH_ALGO_PLOC:
+      return p->ploc_radius >= 1 && p->ploc_radius <= 512 && p->max_iterations >= 0;
+  }
+  return false;
+}
+
+static MeshPtrs mesh_ptrs(const bvh_mesh_soa* m) {
+  MeshPtrs p;
+  p.v[0] = m->v0x; p.v[1] = m->v0y; p.v[2] = m->v0z;
+  p.v[3] = m->v1x; p.v[4] = m->v1y; p.v[5] = m->v1z;
+  p.v[6] = m->v2x; p.v[7] = m->v2y; p.v[8] = m->v2z;
+  return p;
+}
+
+static bool mesh_ok(const bvh_mesh_soa* m) {
+  if (!m) return false;
+  if (m->n == 0) return true;
+  if (m->n > (1u << 30) - 1) return false;  // look-back descriptors hold 30-bit counts
+  const float* a[9] = {m->v0x, m->v0y, m->v0z, m->v1x, m->v1y, m->v1z, m->v2x, m->v2y, m->v2z};
+  for (int k = 0; k < 9; ++k)
+    if (!a[k]) return false;
+  return true;
+}
+
+static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, cudaStream_t st,
+                             bvh_tree* out) {
+  const uint32_t n = mesh->n;
+  ctx->have_timing = false;
+  ctx->last = bvh_timing{};
+  ctx->last_algo = params->algo;
+  ctx->last_stream = st;
+  out->nodes = nullptr;
+  out->indices = nullptr;
+  out->n_nodes = 0;
+  out->n_prims = n;
+  if (n == 0) return BVH_OK;  // empty mesh: empty tree
+  MeshPtrs m = mesh_ptrs(mesh);
+  uint32_t* idx = nullptr;
+  cudaError_t e;
+  if (params->algo == BVH_ALGO_PLOC) {
+    int it = 0, np = 0;
+    unsigned long long cs = 0;
+    e = ploc_build(ctx->ws, m, n, params->ploc_radius, params->max_iterations, st, &ctx->evs, &idx, &it, &cs, &np);
+    ctx->last.ploc_iterations = it;
+    ctx->last.ploc_cluster_sum = cs;
+    if (e != cudaSuccess) return from_cuda(e);
+    if (np) return BVH_ERR_NO_PROGRESS;
+  } else {
+    int rounds = params->algo == BVH_ALGO_LBVH_PLUS ? params->treelet_rounds : 0;
+    e = lbvh_build(ctx->ws, m, n, params->morton_bits, rounds, st, &ctx->evs, &idx);
+    if (e != cudaSuccess) return from_cuda(e);
+  }
+  ScratchLayout L = scratch_layout(ctx->ws.cap_n);
+  cudaMemcpyAsync(ctx->h_status, ctx->ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(ctx->evs.ev[6], st);
+  out->nodes = reinterpret_cast<const bvh_node*>(ctx->ws.nodes);
+  out->indices = idx;
+  out->n_nodes = 2 * n - 1;
+  ctx->have_timing = true;
+  return from_cuda(cudaGetLastError());
+}
+
+extern "C" bvh_status bvh_build_device(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
+                                       bvh_tree* out) {
+  if (!ctx || !out || !mesh_ok(mesh) || !valid_params(params)) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  return build_impl(ctx, mesh, params, reinterpret_cast<cudaStream_t>(stream), out);
+}
+
+static bvh_status check_status_word(bvh_ctx* ctx) {
+  uint32_t s = *ctx->h_status;
+  if (s & (kStatusSortTimeout | kStatusClimbTimeout)) return BVH_ERR_TIMEOUT;
+  if (s & kStatusNoProgress) return BVH_ERR_NO_PROGRESS;
+  return BVH_OK;
+}
+
+extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
+  if (!ctx) return BVH_ERR_INVALID_ARG;
+  if (!ctx->have_timing) return BVH_OK;
+  cudaError_t e = cudaEventSynchronize(ctx->evs.ev[6]);
+  if (e != cudaSuccess) return from_cuda(e);
+  return check_status_word(ctx);
+}
+
+extern "C" bvh_status bvh_last_timing(bvh_ctx* ctx, bvh_timing* out) {
+  if (!ctx || !out) return BVH_ERR_INVALID_ARG;
+  bvh_status s = bvh_sync(ctx);
+  bvh_timing t = ctx->last;
+  if (ctx->have_timing) {
+    cudaEvent_t* ev = ctx->evs.ev;
+    float a = 0;
+    if (cudaEventElapsedTime(&a, ev[0], ev[1]) == cudaSuccess) t.bounds_ms = a;
+    if (cudaEventElapsedTime(&a, ev[1], ev[2]) == cudaSuccess) t.morton_ms = a;
+    if (cudaEventElapsedTime(&a, ev[2], ev[3]) == cudaSuccess) t.sort_ms = a;
+    if (cudaEventElapsedTime(&a, ev[3], ev[4]) == cudaSuccess) t.emit_ms = a;
+    if (cudaEventElapsedTime(&a, ev[4], ev[5]) == cudaSuccess) t.optimize_ms = a;
+    if (cudaEventElapsedTime(&a, ev[0], ev[5]) == cudaSuccess) t.total_ms = a;
+  }
+  *out = t;
+  return s;
+}
+
+extern "C" bvh_status bvh_tree_download(bvh_ctx* ctx, const bvh_tree* tree, void* stream, bvh_node* host_nodes,
+                                        uint32_t* host_indices) {
+  if (!ctx || !tree) return BVH_ERR_INVALID_ARG;
+  if (tree->n_nodes == 0) return BVH_OK;
+  if (!host_nodes || !host_indices) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(host_nodes, tree->nodes, (size_t)tree->n_nodes * sizeof(bvh_node),
+                                  cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host_indices, tree->indices, (size_t)tree->n_prims * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return from_cuda(e);
+}
+
+extern "C" bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
+                                     bvh_node* host_nodes, uint32_t* host_indices, uint32_t* n_nodes) {
+  if (!ctx || !mesh_ok(mesh) || !valid_params(params)) return BVH_ERR_INVALID_ARG;
+  const uint32_t n = mesh->n;
+  if (n_nodes) *n_nodes = 0;
+  if (n == 0) return BVH_OK;
+  if (!host_nodes || !host_indices) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace& ws = ctx->ws;
+  if (ws.mesh_cap < n) {
+    cudaFree(ws.mesh_dev);
+    ws.mesh_dev = nullptr;
+    ws.mesh_cap = 0;
+    // nine arrays, each padded to a multiple of 4 floats so that all stay 16-byte aligned
+    size_t stride = ((size_t)n + 3) & ~size_t(3);
+    cudaError_t e = cudaMalloc(&ws.mesh_dev, stride * 9 * sizeof(float));
+    if (e != cudaSuccess) return from_cuda(e);
+    ws.mesh_cap = n;
+  }
+  const size_t stride = ((size_t)ws.mesh_cap + 3) & ~size_t(3);
+  const float* src[9] = {mesh->v0x, mesh->v0y, mesh->v0z, mesh->v1x, mesh->v1y, mesh->v1z,
+                         mesh->v2x, mesh->v2y, mesh->v2z};
+  bvh_mesh_soa dm;
+  float* dst[9];
+  for (int k = 0; k < 9; ++k) {
+    dst[k] = ws.mesh_dev + stride * k;
+    cudaError_t e = cudaMemcpyAsync(dst[k], src[k], (size_t)n * 4, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return from_cuda(e);
+  }
+  dm.v0x = dst[0]; dm.v0y = dst[1]; dm.v0z = dst[2];
+  dm.v1x = dst[3]; dm.v1y = dst[4]; dm.v1z = dst[5];
+  dm.v2x = dst[6]; dm.v2y = dst[7]; dm.v2z = dst[8];
+  dm.n = n;
+  bvh_tree tree;
+  bvh_status s = build_impl(ctx, &dm, params, st, &tree);
+  if (s != BVH_OK) return s;
+  s = bvh_tree_download(ctx, &tree, stream, host_nodes, host_indices);
+  if (s != BVH_OK) return s;
+  s = check_status_word(ctx);
+  if (s == BVH_OK && n_nodes) *n_nodes = tree.n_nodes;
+  return s;
+}
+
+// ---------------------------------------------------------------------------------------
+// traversal
+// ---------------------------------------------------------------------------------------
+extern "C" bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
+                                const bvh_rays* rays, const bvh_hits* hits, void* stream) {
+  if (!ctx || !mesh_ok(mesh) || !rays || !hits) return BVH_ERR_INVALID_ARG;
+  if (rays->n == 0) return BVH_OK;
+  if (n_nodes > 0 && !nodes) return BVH_ERR_INVALID_ARG;
+  if (!rays->ox || !rays->oy || !rays->oz || !rays->dx || !rays->dy || !rays->dz) return BVH_ERR_INVALID_ARG;
+  if (!hits->t || !hits->prim || !hits->nodes_visited || !hits->aabb_tests || !hits->tri_tests)
+    return BVH_ERR_INVALID_ARG;
+  if (n_nodes > 0x7fffffffu) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  RayPtrs rp;
+  rp.o[0] = rays->ox; rp.o[1] = rays->oy; rp.o[2] = rays->oz;
+  rp.d[0] = rays->dx; rp.d[1] = rays->dy; rp.d[2] = rays->dz;
+  HitOut ho{hits->t, hits->prim, hits->nodes_visited, hits->aabb_tests, hits->tri_tests};
+  return from_cuda(trace_rays(reinterpret_cast<const Node*>(nodes), (int)n_nodes, mesh_ptrs(mesh), mesh->n, rp,
+                              rays->n, ho, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+// Camera basis exactly as the CPU oracle computes it (orc_pinhole_rays): float arithmetic,
+// tan(fov/2) in double.  This file's host code is compiled with -ffp-contract=off.
+static void normalize3(float v[3]) {
+  float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  if (len < 1e-12f) { v[0] = v[1] = v[2] = 0.0f; return; }
+  float inv = 1.0f / len;
+  v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
+}
+
+static bool make_basis(const bvh_camera* cam, int32_t w, int32_t h, PinholeBasis* b) {
+  if (!cam || w <= 0 || h <= 0) return false;
+  if ((uint64_t)w * (uint64_t)h > 0xffffffffull) return false;
+  float f[3] = {cam->look_at[0] - cam->eye[0], cam->look_at[1] - cam->eye[1], cam->look_at[2] - cam->eye[2]};
+  normalize3(f);
+  const float* up = cam->up;
+  float r[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+  normalize3(r);
+  float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+  float half_h = (float)tan((double)(cam->fov_y_deg * 3.14159265358979f / 180.0f) * 0.5);
+  float half_w = half_h * ((float)w / (float)h);
+  for (int k = 0; k < 3; ++k) { b->eye[k] = cam->eye[k]; b->f[k] = f[k]; b->r[k] = r[k]; b->u[k] = u[k]; }
+  b->half_w = half_w;
+  b->half_h = half_h;
+  b->width = w;
+  b->height = h;
+  return true;
+}
+
+extern "C" bvh_status bvh_trace_pinhole(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
+                                        const bvh_camera* cam, int32_t width, int32_t height, const bvh_hits* hits,
+                                        void* stream) {
+  if (!ctx || !mesh_ok(mesh) || !hits) return BVH_ERR_INVALID_ARG;
+  if (!hits->t || !hits->prim || !hits->nodes_visited || !hits->aabb_tests || !hits->tri_tests)
+    return BVH_ERR_INVALID_ARG;
+  if (n_nodes > 0 && !nodes) return BVH_ERR_INVALID_ARG;
+  PinholeBasis b;
+  if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  HitOut ho{hits->t, hits->prim, hits->nodes_visited, hits->aabb_tests, hits->tri_tests};
+  return from_cuda(trace_pinhole(reinterpret_cast<const Node*>(nodes), (int)n_nodes, mesh_ptrs(mesh), mesh->n, b, ho,
+                                 reinterpret_cast<cudaStream_t>(stream)));
+}
+
+extern "C" bvh_status bvh_pinhole_rays(const bvh_camera* cam, int32_t width, int32_t height, float* ox, float* oy,
+                                       float* oz, float* dx, float* dy, float* dz, void* stream) {
+  PinholeBasis b;
+  if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
+  if (!ox || !oy || !oz || !dx || !dy || !dz) return BVH_ERR_INVALID_ARG;
+  return from_cuda(pinhole_rays(b, ox, oy, oz, dx, dy, dz, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+// autoCamera, src/render_engine.cu:601-637.
+extern "C" bvh_status bvh_auto_camera(const bvh_node* root, bvh_camera* cam) {
+  if (!cam) return BVH_ERR_INVALID_ARG;
+  cam->fov_y_deg = 60.0f;
+  cam->up[0] = 0.0f; cam->up[1] = 1.0f; cam->up[2] = 0.0f;
+  if (!root) {
+    cam->eye[0] = 0.0f; cam->eye[1] = 0.0f; cam->eye[2] = 5.0f;
+    cam->look_at[0] = cam->look_at[1] = cam->look_at[2] = 0.0f;
+    return BVH_OK;
+  }
+  float c[3] = {(root->min_x + root->max_x) * 0.5f, (root->min_y + root->max_y) * 0.5f,
+                (root->min_z + root->max_z) * 0.5f};
+  float e[3] = {root->max_x - root->min_x, root->max_y - root->min_y, root->max_z - root->min_z};
+  float diag = sqrtf((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2]);
+  if (diag < 1e-6f) diag = 2.0f;
+  float fov = cam->fov_y_deg * 3.14159265358979f / 180.0f;
+  float dist = (diag * 0.5f) / (float)tan((double)(fov * 0.5f)) * 1.2f;
+  cam->eye[0] = c[0] + dist * 0.6f;
+  cam->eye[1] = c[1] + dist * 0.3f;
+  cam->eye[2] = c[2] + dist * 0.7f;
+  for (int k = 0; k < 3; ++k) cam->look_at[k] = c[k];
+  return BVH_OK;
+}

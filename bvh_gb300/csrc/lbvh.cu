@@ -1,0 +1,657 @@
+// lbvh.cu -- LBVH construction on sm_103a.
+//
+// Pipeline (one stream, no host synchronisation):
+//   k_bounds      scene AABB of all triangles (reference: kComputeBoundsAndCentroids_nt +
+//                 kReduceBounds_Step1/2_nt, src/cuda/lbvh_builder.cu:47-165), also zeroes the
+//                 sort scratch for this build.
+//   k_morton      per-triangle AABB (kept for the leaves), centroid, Morton code
+//                 (kComputeMortonCodes_nt :167-181 / kComputeMortonCodes_P, lbvh_plus_builder.cu:276-290)
+//                 and the digit histograms of every radix pass.
+//   k_onesweep    one kernel per 8-bit digit: stable LSD radix sort with decoupled look-back
+//                 (replaces cub::DeviceRadixSort::SortPairs, lbvh_builder.cu:413-438, and
+//                 thrust::sort_by_key, lbvh_plus_builder.cu:465).
+//   k_emit        bottom-up construction of the Karras tree with boxes in one pass: every
+//                 node is completed by the second child to arrive, which also unions the
+//                 boxes (reference: kBuildInternalNodes_nt :183-229 + kInitLeafNodes_nt :231-241
+//                 + kRefitHierarchy_nt :243-274).  The node ids are exactly Karras's.
+#include <algorithm>
+#include <cstdio>
+
+#include "lbvh.cuh"
+
+namespace bvhgb {
+
+// ---------------------------------------------------------------------------------------
+// scratch
+// ---------------------------------------------------------------------------------------
+int sort_tile(int key_bytes) { return kSortThreads * (key_bytes == 4 ? kSortIpt32 : kSortIpt64); }
+
+ScratchLayout scratch_layout(uint32_t n) {
+  ScratchLayout L;
+  size_t o = 0;
+  L.status = o; o += 1;
+  L.ticket = o; o += 1;
+  o = (o + 3) & ~size_t(3);
+  L.scene = o; o += 8;
+  L.ploc = o; o += 16;
+  L.partials = o; o += (size_t)kBoundsBlocks * 8;
+  o = (o + 3) & ~size_t(3);
+  L.zero_begin = o;
+  L.counters = o; o += 16;
+  L.hist = o; o += (size_t)kMaxPasses * 256;
+  L.desc = o;
+  // the smaller tile (64-bit keys) gives the most tiles
+  size_t tiles = div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_tile(8));
+  o += (size_t)kMaxPasses * tiles * 256;
+  L.zero_end = o;
+  L.total = o;
+  return L;
+}
+
+// ---------------------------------------------------------------------------------------
+// k_bounds: scene AABB (+ zeroing of the per-build scratch)
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void warp_reduce_box(float& a, float& b, float& c, float& d, float& e, float& f) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fminf(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fminf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    c = fminf(c, __shfl_xor_sync(0xffffffffu, c, o));
+    d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+    e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    f = fmaxf(f, __shfl_xor_sync(0xffffffffu, f, o));
+  }
+}
+
+__device__ __forceinline__ void tri_box_acc(float a0, float a1, float a2, float& mn, float& mx) {
+  mn = fminf(mn, fminf(a0, fminf(a1, a2)));
+  mx = fmaxf(mx, fmaxf(a0, fmaxf(a1, a2)));
+}
+
+__global__ void __launch_bounds__(256) k_bounds(MeshPtrs m, uint32_t n, int vec4, uint32_t* __restrict__ scratch,
+                                                ScratchLayout L) {
+  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t gsz = gridDim.x * blockDim.x;
+  // zero this build's histograms, tile counters and look-back descriptors
+  {
+    uint4* z = reinterpret_cast<uint4*>(scratch + L.zero_begin);
+    size_t words4 = (L.zero_end - L.zero_begin) / 4;
+    for (size_t w = gtid; w < words4; w += gsz) z[w] = make_uint4(0, 0, 0, 0);
+    for (size_t w = L.zero_begin + words4 * 4 + gtid; w < L.zero_end; w += gsz) scratch[w] = 0;
+    if (gtid == 0) scratch[L.status] = 0;
+  }
+  float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
+  uint32_t done = 0;
+  if (vec4) {
+    const uint32_t n4 = n >> 2;
+    const float4* p[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) p[k] = reinterpret_cast<const float4*>(m.v[k]);
+    for (uint32_t q = gtid; q < n4; q += gsz) {
+      float4 x0 = __ldcs(p[0] + q), y0 = __ldcs(p[1] + q), z0 = __ldcs(p[2] + q);
+      float4 x1 = __ldcs(p[3] + q), y1 = __ldcs(p[4] + q), z1 = __ldcs(p[5] + q);
+      float4 x2 = __ldcs(p[6] + q), y2 = __ldcs(p[7] + q), z2 = __ldcs(p[8] + q);
+      tri_box_acc(x0.x, x1.x, x2.x, mnx, mxx); tri_box_acc(x0.y, x1.y, x2.y, mnx, mxx);
+      tri_box_acc(x0.z, x1.z, x2.z, mnx, mxx); tri_box_acc(x0.w, x1.w, x2.w, mnx, mxx);
+      tri_box_acc(y0.x, y1.x, y2.x, mny, mxy); tri_box_acc(y0.y, y1.y, y2.y, mny, mxy);
+      tri_box_acc(y0.z, y1.z, y2.z, mny, mxy); tri_box_acc(y0.w, y1.w, y2.w, mny, mxy);
+      tri_box_acc(z0.x, z1.x, z2.x, mnz, mxz); tri_box_acc(z0.y, z1.y, z2.y, mnz, mxz);
+      tri_box_acc(z0.z, z1.z, z2.z, mnz, mxz); tri_box_acc(z0.w, z1.w, z2.w, mnz, mxz);
+    }
+    done = n4 << 2;
+  }
+  for (uint32_t i = done + gtid; i < n; i += gsz) {
+    tri_box_acc(m.v[0][i], m.v[3][i], m.v[6][i], mnx, mxx);
+    tri_box_acc(m.v[1][i], m.v[4][i], m.v[7][i], mny, mxy);
+    tri_box_acc(m.v[2][i], m.v[5][i], m.v[8][i], mnz, mxz);
+  }
+  warp_reduce_box(mnx, mny, mnz, mxx, mxy, mxz);
+  __shared__ float s_red[8][6];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_red[w][0] = mnx; s_red[w][1] = mny; s_red[w][2] = mnz;
+    s_red[w][3] = mxx; s_red[w][4] = mxy; s_red[w][5] = mxz;
+  }
+  __syncthreads();
+  float* part = reinterpret_cast<float*>(scratch + L.partials);
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      mnx = fminf(mnx, s_red[k][0]); mny = fminf(mny, s_red[k][1]); mnz = fminf(mnz, s_red[k][2]);
+      mxx = fmaxf(mxx, s_red[k][3]); mxy = fmaxf(mxy, s_red[k][4]); mxz = fmaxf(mxz, s_red[k][5]);
+    }
+    float* pb = part + (size_t)blockIdx.x * 8;
+    pb[0] = mnx; pb[1] = mny; pb[2] = mnz; pb[3] = mxx; pb[4] = mxy; pb[5] = mxz;
+    __threadfence();
+    uint32_t t = atomicAdd(scratch + L.ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  // last block: reduce the partials
+  __threadfence();
+  mnx = mny = mnz = FLT_MAX;
+  mxx = mxy = mxz = -FLT_MAX;
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    const float* pb = part + (size_t)b * 8;
+    mnx = fminf(mnx, __ldcg(pb + 0)); mny = fminf(mny, __ldcg(pb + 1)); mnz = fminf(mnz, __ldcg(pb + 2));
+    mxx = fmaxf(mxx, __ldcg(pb + 3)); mxy = fmaxf(mxy, __ldcg(pb + 4)); mxz = fmaxf(mxz, __ldcg(pb + 5));
+  }
+  warp_reduce_box(mnx, mny, mnz, mxx, mxy, mxz);
+  __syncthreads();
+  if (lane == 0) {
+    s_red[w][0] = mnx; s_red[w][1] = mny; s_red[w][2] = mnz;
+    s_red[w][3] = mxx; s_red[w][4] = mxy; s_red[w][5] = mxz;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      mnx = fminf(mnx, s_red[k][0]); mny = fminf(mny, s_red[k][1]); mnz = fminf(mnz, s_red[k][2]);
+      mxx = fmaxf(mxx, s_red[k][3]); mxy = fmaxf(mxy, s_red[k][4]); mxz = fmaxf(mxz, s_red[k][5]);
+    }
+    SceneParams* sp = reinterpret_cast<SceneParams*>(scratch + L.scene);
+    float ex = mxx - mnx, ey = mxy - mny, ez = mxz - mnz;
+    sp->mn[0] = mnx; sp->mn[1] = mny; sp->mn[2] = mnz; sp->mn[3] = 0.f;
+    sp->ext[0] = (ex > 1e-6f) ? ex : 1.0f;
+    sp->ext[1] = (ey > 1e-6f) ? ey : 1.0f;
+    sp->ext[2] = (ez > 1e-6f) ? ez : 1.0f;
+    sp->ext[3] = 0.f;
+    scratch[L.ticket] = 0;  // ready for the next build
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// k_morton: AABB + centroid + Morton code + digit histograms of every pass
+// ---------------------------------------------------------------------------------------
+template <int BITS, typename K>
+__device__ __forceinline__ K tri_code(float x0, float y0, float z0, float x1, float y1, float z1, float x2,
+                                      float y2, float z2, const float* smn, const float* sext, Box& box) {
+  float lx = fminf(x0, fminf(x1, x2)), ly = fminf(y0, fminf(y1, y2)), lz = fminf(z0, fminf(z1, z2));
+  float hx = fmaxf(x0, fmaxf(x1, x2)), hy = fmaxf(y0, fmaxf(y1, y2)), hz = fmaxf(z0, fmaxf(z1, z2));
+  box.lo = make_float4(lx, ly, lz, 0.f);
+  box.hi = make_float4(hx, hy, hz, 0.f);
+  // centroid = (min + max) * 0.5 (lbvh_builder.cu:65), normalised with IEEE division (:175-177)
+  float cx = __fmul_rn(__fadd_rn(lx, hx), 0.5f), cy = __fmul_rn(__fadd_rn(ly, hy), 0.5f),
+        cz = __fmul_rn(__fadd_rn(lz, hz), 0.5f);
+  float nx = __fdiv_rn(__fsub_rn(cx, smn[0]), sext[0]);
+  float ny = __fdiv_rn(__fsub_rn(cy, smn[1]), sext[1]);
+  float nz = __fdiv_rn(__fsub_rn(cz, smn[2]), sext[2]);
+  return (K)morton_code<BITS>(nx, ny, nz);
+}
+
+template <int BITS, typename K>
+__global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4, K* __restrict__ keys,
+                                                Box* __restrict__ boxes, uint32_t* __restrict__ scratch,
+                                                ScratchLayout L) {
+  constexpr int P = (int)sizeof(K);  // 8-bit digit passes
+  __shared__ uint32_t s_hist[P][256];
+  for (int i = threadIdx.x; i < P * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+  __shared__ float s_scene[8];
+  if (threadIdx.x < 8) s_scene[threadIdx.x] = __ldcg(reinterpret_cast<const float*>(scratch + L.scene) + threadIdx.x);
+  __syncthreads();
+  const float* smn = s_scene;
+  const float* sext = s_scene + 4;
+  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t gsz = gridDim.x * blockDim.x;
+  uint32_t done = 0;
+  if (vec4) {
+    const uint32_t n4 = n >> 2;
+    const float4* p[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) p[k] = reinterpret_cast<const float4*>(m.v[k]);
+    for (uint32_t q = gtid; q < n4; q += gsz) {
+      float4 x0 = __ldcs(p[0] + q), y0 = __ldcs(p[1] + q), z0 = __ldcs(p[2] + q);
+      float4 x1 = __ldcs(p[3] + q), y1 = __ldcs(p[4] + q), z1 = __ldcs(p[5] + q);
+      float4 x2 = __ldcs(p[6] + q), y2 = __ldcs(p[7] + q), z2 = __ldcs(p[8] + q);
+      Box b[4];
+      K c[4];
+      c[0] = tri_code<BITS, K>(x0.x, y0.x, z0.x, x1.x, y1.x, z1.x, x2.x, y2.x, z2.x, smn, sext, b[0]);
+      c[1] = tri_code<BITS, K>(x0.y, y0.y, z0.y, x1.y, y1.y, z1.y, x2.y, y2.y, z2.y, smn, sext, b[1]);
+      c[2] = tri_code<BITS, K>(x0.z, y0.z, z0.z, x1.z, y1.z, z1.z, x2.z, y2.z, z2.z, smn, sext, b[2]);
+      c[3] = tri_code<BITS, K>(x0.w, y0.w, z0.w, x1.w, y1.w, z1.w, x2.w, y2.w, z2.w, smn, sext, b[3]);
+      if constexpr (sizeof(K) == 4) {
+        reinterpret_cast<uint4*>(keys)[q] = make_uint4(c[0], c[1], c[2], c[3]);
+      } else {
+        ulonglong2* kp = reinterpret_cast<ulonglong2*>(keys) + 2 * (size_t)q;
+        kp[0] = make_ulonglong2(c[0], c[1]);
+        kp[1] = make_ulonglong2(c[2], c[3]);
+      }
+      float4* bp = reinterpret_cast<float4*>(boxes + 4 * (size_t)q);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        bp[2 * e] = b[e].lo;
+        bp[2 * e + 1] = b[e].hi;
+#pragma unroll
+        for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c[e] >> (8 * p2)) & 255u], 1u);
+      }
+    }
+    done = n4 << 2;
+  }
+  for (uint32_t i = done + gtid; i < n; i += gsz) {
+    Box b;
+    K c = tri_code<BITS, K>(m.v[0][i], m.v[1][i], m.v[2][i], m.v[3][i], m.v[4][i], m.v[5][i], m.v[6][i],
+                            m.v[7][i], m.v[8][i], smn, sext, b);
+    keys[i] = c;
+    boxes[i] = b;
+#pragma unroll
+    for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c >> (8 * p2)) & 255u], 1u);
+  }
+  __syncthreads();
+  uint32_t* gh = scratch + L.hist;
+  for (int i = threadIdx.x; i < P * 256; i += blockDim.x) {
+    uint32_t c = (&s_hist[0][0])[i];
+    if (c) atomicAdd(gh + i, c);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// k_onesweep: one stable LSD pass over an 8-bit digit with decoupled look-back
+// ---------------------------------------------------------------------------------------
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kValMask = (1u << 30) - 1;
+
+template <int THREADS>
+__device__ __forceinline__ unsigned long long block_exclusive_scan_u64(unsigned long long v,
+                                                                      unsigned long long* s_warp) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long t = lane < THREADS / 32 ? s_warp[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < THREADS / 32) s_warp[lane] = t;  // inclusive warp totals
+  }
+  __syncthreads();
+  unsigned long long before = w ? s_warp[w - 1] : 0ull;
+  return before + x - v;
+}
+
+template <typename K, int THREADS, int IPT>
+__global__ void __launch_bounds__(THREADS) k_onesweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                      K* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                                      int pass, uint32_t* __restrict__ scratch, ScratchLayout L,
+                                                      uint32_t tiles) {
+  constexpr int BINS = 256, NW = THREADS / 32, TILE = THREADS * IPT;
+  static_assert(THREADS == BINS, "one thread per bin");
+  extern __shared__ __align__(16) unsigned char smem[];
+  K* s_keys = reinterpret_cast<K*>(smem);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+  uint32_t* s_whist = s_vals + TILE;          // NW x BINS
+  uint32_t* s_binstart = s_whist + NW * BINS; // BINS
+  uint32_t* s_gstart = s_binstart + BINS;     // BINS
+  unsigned long long* s_scan = reinterpret_cast<unsigned long long*>(s_gstart + BINS);  // 32
+  uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_scan + 32);
+
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int shift = 8 * pass;
+  if (tid == 0) *s_tile = atomicAdd(scratch + L.counters + pass, 1u);
+  for (int b = tid; b < NW * BINS; b += THREADS) s_whist[b] = 0;
+  __syncthreads();
+  const uint32_t tile = *s_tile;
+  const uint32_t base = tile * (uint32_t)TILE;
+
+  K key[IPT];
+  uint32_t val[IPT];
+  uint32_t rnk[IPT];
+  const uint32_t wbase = base + (uint32_t)w * 32u * IPT;
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    uint32_t idx = wbase + (uint32_t)k * 32u + lane;
+    bool ok = idx < n;
+    key[k] = ok ? kin[idx] : K(0);
+    val[k] = ok ? (vin ? vin[idx] : idx) : 0u;
+  }
+  // stable warp-local ranking: items in (k, lane) order == original order within the warp
+  uint32_t* wh = s_whist + w * BINS;
+  const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    uint32_t idx = wbase + (uint32_t)k * 32u + lane;
+    uint32_t d = idx < n ? (uint32_t)(key[k] >> shift) & 255u : 256u;
+    uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (lane == leader && d < 256u) {
+      old = wh[d];
+      wh[d] = old + __popc(peers);
+    }
+    old = __shfl_sync(0xffffffffu, old, leader);
+    rnk[k] = old + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+  // per bin: exclusive prefix over warps, tile count
+  const int b = tid;
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int ww = 0; ww < NW; ++ww) {
+    uint32_t c = s_whist[ww * BINS + b];
+    s_whist[ww * BINS + b] = cnt;
+    cnt += c;
+  }
+  const uint32_t ghist = __ldcg(scratch + L.hist + pass * BINS + b);
+  unsigned long long packed = ((unsigned long long)ghist << 32) | cnt;
+  unsigned long long ex = block_exclusive_scan_u64<THREADS>(packed, s_scan);
+  s_binstart[b] = (uint32_t)ex;                 // tile-local start of bin b
+  const uint32_t binbase = (uint32_t)(ex >> 32);  // global start of bin b
+  // decoupled look-back on bin b
+  uint32_t* desc = scratch + L.desc + ((size_t)pass * tiles) * BINS;
+  uint32_t excl = 0;
+  if (tile == 0) {
+    st_release(desc + b, kFlagInc | cnt);
+  } else {
+    st_release(desc + (size_t)tile * BINS + b, kFlagAgg | cnt);
+    int64_t j = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+      uint32_t v = ld_acquire(desc + (size_t)j * BINS + b);
+      uint32_t fl = v & ~kValMask;
+      if (fl == 0) {
+        if (++spins > kSpinLimit) {
+          atomicOr(scratch + L.status, kStatusSortTimeout);
+          break;
+        }
+        continue;
+      }
+      excl += v & kValMask;
+      if (fl == kFlagInc) break;
+      --j;
+    }
+    st_release(desc + (size_t)tile * BINS + b, kFlagInc | (excl + cnt));
+  }
+  s_gstart[b] = binbase + excl;
+  __syncthreads();
+  // local scatter into tile order
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    uint32_t idx = wbase + (uint32_t)k * 32u + lane;
+    if (idx < n) {
+      uint32_t d = (uint32_t)(key[k] >> shift) & 255u;
+      uint32_t pos = s_binstart[d] + s_whist[w * BINS + d] + rnk[k];
+      s_keys[pos] = key[k];
+      s_vals[pos] = val[k];
+    }
+  }
+  __syncthreads();
+  const uint32_t len = min((uint32_t)TILE, n - base);
+  for (uint32_t i = tid; i < len; i += THREADS) {
+    K kk = s_keys[i];
+    uint32_t d = (uint32_t)(kk >> shift) & 255u;
+    uint32_t dst = s_gstart[d] + (i - s_binstart[d]);
+    if (dst < n) {  // always true unless a look-back wait gave up (status already set)
+      kout[dst] = kk;
+      vout[dst] = s_vals[i];
+    }
+  }
+}
+
+template <typename K>
+size_t onesweep_smem() {
+  constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
+  constexpr int TILE = kSortThreads * IPT;
+  return (size_t)TILE * sizeof(K) + (size_t)TILE * 4 + (size_t)(kSortThreads / 32) * 256 * 4 + 2 * 256 * 4 +
+         32 * 8 + 16;
+}
+
+template <typename K>
+cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L, int* final_buf) {
+  constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
+  constexpr int TILE = kSortThreads * IPT;
+  const uint32_t tiles = div_up(n, TILE);
+  const size_t smem = onesweep_smem<K>();
+  auto kern = k_onesweep<K, kSortThreads, IPT>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  int cur = 0;
+  for (int p = 0; p < passes; ++p) {
+    const K* kin = reinterpret_cast<const K*>(ws.keys[cur]);
+    const uint32_t* vin = p == 0 ? nullptr : ws.vals[cur];
+    kern<<<tiles, kSortThreads, smem, st>>>(kin, vin, reinterpret_cast<K*>(ws.keys[cur ^ 1]), ws.vals[cur ^ 1], n, p,
+                                            ws.scratch, L, tiles);
+    cur ^= 1;
+  }
+  *final_buf = cur;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// k_emit: bottom-up Karras hierarchy + refit in one pass
+// ---------------------------------------------------------------------------------------
+// delta_nt (lbvh_builder.cu:33-43) / delta_P (lbvh_plus_builder.cu:41-47): common-prefix length of
+// the (code, original index) keys; -1 outside [0, n).
+template <typename K>
+__device__ __forceinline__ int karras_delta(const K* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
+                                            int64_t i, int64_t j) {
+  if (j < 0 || j >= (int64_t)n) return -1;
+  K a = __ldg(keys + i), b = __ldg(keys + j);
+  if (a == b) {
+    uint32_t x = __ldg(vals + i) ^ __ldg(vals + j);
+    if constexpr (sizeof(K) == 4) return 32 + __clz(x);
+    else return 64 + __clzll((unsigned long long)x);
+  }
+  if constexpr (sizeof(K) == 4) return __clz((uint32_t)(a ^ b));
+  else return __clzll((unsigned long long)(a ^ b));
+}
+
+__device__ __forceinline__ void store_node(Node* nodes, int32_t idx, const Box& b, int32_t l, int32_t r, int32_t aux0) {
+  float4* p = reinterpret_cast<float4*>(nodes + idx);
+  __stcg(p, b.lo);
+  __stcg(p + 1, b.hi);
+  __stcg(reinterpret_cast<int4*>(p + 2), make_int4(l, r, aux0, 0));
+}
+__device__ __forceinline__ Box load_node_box(const Node* nodes, int32_t idx) {
+  const float4* p = reinterpret_cast<const float4*>(nodes + idx);
+  Box b;
+  b.lo = __ldcg(p);
+  b.hi = __ldcg(p + 1);
+  return b;
+}
+
+// One thread per sorted position i.  A thread owns the range [f, l] of the node it is building;
+// it finds the parent's split gamma from the neighbouring prefixes (the side with the longer
+// common prefix is the parent's, Apetrei 2014), publishes its far endpoint in slot[gamma] and the
+// second arrival continues with the union.  Internal node ids follow Karras: a left child's id is
+// its last index, a right child's id its first index, the root is 0, leaf i is n-1+i.
+template <typename K, bool PARENTS>
+__global__ void __launch_bounds__(256) k_emit(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                              const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
+                                              unsigned long long* __restrict__ slots, uint32_t epoch, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t prim = __ldg(vals + i);
+  Box box;
+  {
+    const float4* bp = reinterpret_cast<const float4*>(tri_boxes + prim);
+    box.lo = __ldg(bp);
+    box.hi = __ldg(bp + 1);
+  }
+  int32_t my = (int32_t)(n - 1 + i);
+  store_node(nodes, my, box, (int32_t)(prim | kLeafBit), -1, -1);
+  if (n == 1) return;
+  int64_t f = i, l = i;
+  int32_t lc = -1, rc = -1;
+  bool internal = false;
+  const unsigned long long tag = (unsigned long long)epoch << 32;
+  while (true) {
+    if (internal && f == 0 && l == (int64_t)n - 1) {
+      store_node(nodes, 0, box, lc, rc, -1);
+      if (PARENTS) {
+        __stcg(&nodes[lc].aux0, 0);
+        __stcg(&nodes[rc].aux0, 0);
+      }
+      return;
+    }
+    const int dl = karras_delta(keys, vals, n, f - 1, f);
+    const int dr = karras_delta(keys, vals, n, l, l + 1);
+    const bool is_left = dr > dl;
+    const uint32_t gamma = is_left ? (uint32_t)l : (uint32_t)(f - 1);
+    if (internal) {
+      my = (int32_t)(is_left ? l : f);
+      store_node(nodes, my, box, lc, rc, -1);
+      if (PARENTS) {
+        __stcg(&nodes[lc].aux0, my);
+        __stcg(&nodes[rc].aux0, my);
+      }
+    }
+    const uint32_t far = is_left ? (uint32_t)f : (uint32_t)l;
+    __threadfence();
+    const unsigned long long old = atomicExch(slots + gamma, tag | far);
+    if ((old & 0xffffffff00000000ull) != tag) return;  // first child to arrive
+    __threadfence();
+    const uint32_t other = (uint32_t)old;
+    int32_t sib;
+    if (is_left) {
+      sib = (other == gamma + 1) ? (int32_t)(n + gamma) : (int32_t)(gamma + 1);
+      lc = my;
+      rc = sib;
+      l = other;
+      box = box_union(box, load_node_box(nodes, sib));
+    } else {
+      sib = (other == gamma) ? (int32_t)(n - 1 + gamma) : (int32_t)gamma;
+      lc = sib;
+      rc = my;
+      f = other;
+      box = box_union(load_node_box(nodes, sib), box);
+    }
+    internal = true;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------------------
+void workspace_free(Workspace& ws) {
+  cudaFree(ws.keys[0]); cudaFree(ws.keys[1]);
+  cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
+  cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch);
+  cudaFree(ws.cbox[0]); cudaFree(ws.cbox[1]); cudaFree(ws.cid[0]); cudaFree(ws.cid[1]); cudaFree(ws.nbr);
+  cudaFree(ws.mesh_dev);
+  ws = Workspace();
+}
+
+cudaError_t workspace_reserve(Workspace& ws, uint32_t n) {
+  if (n <= ws.cap_n && ws.scratch) return cudaSuccess;
+  uint32_t cap = std::max<uint32_t>(n, 1024);
+  cudaFree(ws.keys[0]); cudaFree(ws.keys[1]); cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
+  cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch);
+  ws.keys[0] = ws.keys[1] = nullptr; ws.vals[0] = ws.vals[1] = nullptr;
+  ws.boxes = nullptr; ws.nodes = nullptr; ws.slots = nullptr; ws.scratch = nullptr; ws.cap_n = 0;
+  cudaError_t e;
+  if ((e = cudaMalloc(&ws.keys[0], (size_t)cap * 8)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.keys[1], (size_t)cap * 8)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.vals[0], (size_t)cap * 4)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.vals[1], (size_t)cap * 4)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.boxes, (size_t)cap * sizeof(Box))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.nodes, (2 * (size_t)cap) * sizeof(Node))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.slots, (size_t)cap * 8)) != cudaSuccess) return e;
+  ScratchLayout L = scratch_layout(cap);
+  if ((e = cudaMalloc(&ws.scratch, L.total * 4)) != cudaSuccess) return e;
+  if ((e = cudaMemset(ws.slots, 0, (size_t)cap * 8)) != cudaSuccess) return e;
+  if ((e = cudaMemset(ws.scratch, 0, L.total * 4)) != cudaSuccess) return e;
+  ws.scratch_words = L.total;
+  ws.epoch = 0;
+  ws.cap_n = cap;
+  return cudaSuccess;
+}
+
+static inline bool all_aligned16(const MeshPtrs& m) {
+  for (int k = 0; k < 9; ++k)
+    if (reinterpret_cast<uintptr_t>(m.v[k]) & 15) return false;
+  return true;
+}
+
+static inline uint32_t next_epoch(Workspace& ws) {
+  ws.epoch++;
+  if (ws.epoch == 0) {  // wrapped: clear stale tags once
+    cudaMemset(ws.slots, 0, (size_t)ws.cap_n * 8);
+    ws.epoch = 1;
+  }
+  return ws.epoch;
+}
+
+static inline void rec(StageEvents* evs, int k, cudaStream_t st) {
+  if (evs && evs->use) cudaEventRecord(evs->ev[k], st);
+}
+
+template <int BITS, typename K>
+static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
+                               const ScratchLayout& L, int* final_buf) {
+  const int vec4 = all_aligned16(m) ? 1 : 0;
+  // zero only the descriptors this build's passes use
+  ScratchLayout Lz = L;
+  Lz.zero_end = L.desc + (size_t)sizeof(K) * div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_tile((int)sizeof(K))) * 256;
+  k_bounds<<<kBoundsBlocks, 256, 0, st>>>(m, n, vec4, ws.scratch, Lz);
+  rec(evs, 1, st);
+  const uint32_t work = vec4 ? div_up(n, 4) : n;
+  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(work, 256), 152 * 8));
+  k_morton<BITS, K><<<grid, 256, 0, st>>>(m, n, vec4, reinterpret_cast<K*>(ws.keys[0]), ws.boxes, ws.scratch, L);
+  rec(evs, 2, st);
+  cudaError_t e = run_sort<K>(ws, n, (int)sizeof(K), st, L, final_buf);
+  rec(evs, 3, st);
+  return e;
+}
+
+cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
+                          uint32_t** sorted_idx) {
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  int fb = 0;
+  cudaError_t e = lbvh_prefix<30, uint32_t>(ws, m, n, st, evs, L, &fb);
+  *sorted_idx = ws.vals[fb];
+  return e;
+}
+
+cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,
+                       StageEvents* evs, uint32_t** out_indices) {
+  cudaError_t e = workspace_reserve(ws, n);
+  if (e != cudaSuccess) return e;
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  rec(evs, 0, st);
+  int fb = 0;
+  const uint32_t epoch = next_epoch(ws);
+  const bool parents = treelet_rounds > 0;
+  if (bits == 30) {
+    e = lbvh_prefix<30, uint32_t>(ws, m, n, st, evs, L, &fb);
+    if (e != cudaSuccess) return e;
+    if (parents)
+      k_emit<uint32_t, true><<<div_up(n, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(ws.keys[fb]), ws.vals[fb],
+                                                              ws.boxes, ws.nodes, ws.slots, epoch, n);
+    else
+      k_emit<uint32_t, false><<<div_up(n, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(ws.keys[fb]), ws.vals[fb],
+                                                               ws.boxes, ws.nodes, ws.slots, epoch, n);
+  } else {
+    if (bits == 60) e = lbvh_prefix<60, unsigned long long>(ws, m, n, st, evs, L, &fb);
+    else e = lbvh_prefix<63, unsigned long long>(ws, m, n, st, evs, L, &fb);
+    if (e != cudaSuccess) return e;
+    if (parents)
+      k_emit<unsigned long long, true><<<div_up(n, 256), 256, 0, st>>>(
+          reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb], ws.boxes, ws.nodes, ws.slots, epoch, n);
+    else
+      k_emit<unsigned long long, false><<<div_up(n, 256), 256, 0, st>>>(
+          reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb], ws.boxes, ws.nodes, ws.slots, epoch, n);
+  }
+  rec(evs, 4, st);
+  if (treelet_rounds > 0 && n >= 2) {
+    e = treelet_rounds_run(ws, n, treelet_rounds, st);
+    if (e != cudaSuccess) return e;
+  }
+  rec(evs, 5, st);
+  *out_indices = ws.vals[fb];
+  return cudaGetLastError();
+}
+
+}  // namespace bvhgb

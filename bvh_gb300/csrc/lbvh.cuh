@@ -1,0 +1,88 @@
+// lbvh.cuh -- host-side interface of the build kernels (internal to the library).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace bvhgb {
+
+struct MeshPtrs {
+  const float* v[9];  // v0x v0y v0z v1x v1y v1z v2x v2y v2z (TriangleMesh order)
+};
+
+// Device workspace owned by a context; grown on demand, reused across builds.
+struct Workspace {
+  uint32_t cap_n = 0;        // triangles the buffers can hold
+  void* keys[2] = {nullptr, nullptr};
+  uint32_t* vals[2] = {nullptr, nullptr};
+  Box* boxes = nullptr;      // per-triangle AABB in input order
+  Node* nodes = nullptr;     // 2n-1 output nodes
+  unsigned long long* slots = nullptr;  // n-1 rendezvous words (epoch << 32 | endpoint)
+  uint32_t* scratch = nullptr;          // histograms, look-back descriptors, counters
+  size_t scratch_words = 0;
+  uint32_t epoch = 0;        // per-build tag for `slots`
+  // PLOC buffers
+  Box* cbox[2] = {nullptr, nullptr};
+  int32_t* cid[2] = {nullptr, nullptr};
+  int32_t* nbr = nullptr;
+  uint32_t ploc_cap = 0;
+  // device-side mesh copy for host-pointer builds
+  float* mesh_dev = nullptr;
+  uint32_t mesh_cap = 0;
+};
+
+// Scratch layout (32-bit words, offsets from Workspace::scratch).
+struct ScratchLayout {
+  size_t status;     // 1 word, device status bits
+  size_t ticket;     // 1 word, bounds-reduction arrival counter (self-resetting)
+  size_t scene;      // 8 words, SceneParams
+  size_t counters;   // 16 words, per-pass tile counters
+  size_t hist;       // passes * 256
+  size_t desc;       // passes * tiles * 256
+  size_t partials;   // bounds partials, kBoundsBlocks * 8
+  size_t ploc;       // PLOC control words (16)
+  size_t zero_begin; // first word zeroed at the start of each build
+  size_t zero_end;
+  size_t total;
+};
+
+constexpr int kBoundsBlocks = 152 * 4;
+constexpr int kSortThreads = 256;
+constexpr int kSortIpt32 = 16;  // items per thread, 32-bit keys
+constexpr int kSortIpt64 = 12;  // items per thread, 64-bit keys
+constexpr int kMaxPasses = 8;
+
+ScratchLayout scratch_layout(uint32_t n);
+int sort_tile(int key_bytes);
+
+// Builds stage events: [0] start, [1] bounds, [2] morton, [3] sort, [4] emit, [5] optimise.
+struct StageEvents {
+  cudaEvent_t ev[8];
+  bool use = false;
+};
+
+// LBVH over device-resident SoA input; result in ws.nodes / ws.vals[final].
+// morton_bits: 30, 60 or 63.  treelet_rounds > 0 selects LBVH+.
+cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int morton_bits, int treelet_rounds,
+                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices);
+
+// PLOC (radius r) over device-resident SoA input.  Node count is 2n-1.
+cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter,
+                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices, int* iterations,
+                       unsigned long long* cluster_sum, int* no_progress);
+
+// Shared pieces used by PLOC: bounds + Morton-30 + sort (indices sorted by code).
+cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
+                          uint32_t** sorted_idx);
+
+// Grow `ws` to hold n triangles (cudaMalloc; synchronising).
+cudaError_t workspace_reserve(Workspace& ws, uint32_t n);
+cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n);
+void workspace_free(Workspace& ws);
+
+// Treelet restructuring passes (LBVH+) after the first (fused) one.
+cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st);
+
+}  // namespace bvhgb

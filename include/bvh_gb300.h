@@ -1,0 +1,179 @@
+/*
+ * bvh_gb300.h -- C ABI of the GB300 BVH construction library (libbvh_gb300.so).
+ *
+ * Plain pointers and sizes only; no CUDA or C++ types appear in the signatures (streams
+ * are passed as `void*` holding a cudaStream_t, NULL = the legacy default stream).
+ *
+ * Each entry point replaces one piece of the reference (EdinHg/BVH) path:
+ *   bvh_build_host    BVHBuilder::build(const TriangleMesh&) + getNodes/getIndices
+ *                     (include/bvh_builder.h:10-37) for LBVHBuilderCUDA
+ *                     (src/cuda/lbvh_builder.cu:484-488), LBVHPlusBuilderCUDA
+ *                     (src/cuda/lbvh_plus_builder.cu:529-533) and PLOCBuilderCUDA
+ *                     (src/cuda/ploc_builder.cu:403-586): host SoA in, host BVHNode array out.
+ *   bvh_build_device  the same build on device-resident SoA input, result kept on the device
+ *                     (the reference's runCompute without prepareData/downloadResults,
+ *                     e.g. src/cuda/lbvh_builder.cu:376-463).
+ *   bvh_last_timing   getLastBuildTimeMS / getTimingBreakdown (include/bvh_builder.h:29-36).
+ *   bvh_trace         traverseBVH over explicit rays (src/render_engine.cu:289-356).
+ *   bvh_trace_pinhole kRenderKernel's primary rays + traversal (src/render_engine.cu:362-446),
+ *                     returning per-pixel hit t / primitive / counters instead of colours.
+ *   bvh_build_batched many independent meshes in one launch sequence (no reference counterpart;
+ *                     each result equals bvh_build_device of that mesh alone).
+ *
+ * Result layout: BVHNode (include/bvh_node.h:8-31), 48 bytes per node; root at index 0; a leaf
+ * has bit 31 of `left` set, the original triangle index in bits 0-30 and right = -1.
+ * Errors never terminate the process (the reference's CUDA_CHECK calls exit(),
+ * include/common.h:68-76); every call returns a bvh_status.
+ */
+#ifndef BVH_GB300_H
+#define BVH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bvh_status {
+  BVH_OK = 0,
+  BVH_ERR_INVALID_ARG = 1,   /* bad pointer, size, algorithm or parameter */
+  BVH_ERR_OUT_OF_MEMORY = 2, /* device or pinned allocation failed, or over the context budget */
+  BVH_ERR_NO_PROGRESS = 3,   /* PLOC found no mutual pair (NaN/Inf areas) or hit its iteration cap */
+  BVH_ERR_DEVICE = 4,        /* CUDA runtime error (the context may be unusable) */
+  BVH_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+  BVH_ERR_UNSUPPORTED = 6    /* combination not implemented */
+} bvh_status;
+
+typedef enum bvh_algo {
+  BVH_ALGO_LBVH = 0,      /* LBVHBuilderCUDA (30-bit) or 60/63-bit Morton */
+  BVH_ALGO_LBVH_PLUS = 1, /* LBVHPlusBuilderCUDA: Karras tree + treelet restructuring */
+  BVH_ALGO_PLOC = 2       /* PLOCBuilderCUDA(radius) */
+} bvh_algo;
+
+/* BVHNode, 48 bytes (AABB_cw = two 16-byte float3 + int32 children + padding). */
+typedef struct bvh_node {
+  float min_x, min_y, min_z, pad0;
+  float max_x, max_y, max_z, pad1;
+  int32_t left;  /* child index, or (primitive | 0x80000000) for a leaf */
+  int32_t right; /* child index, or -1 for a leaf */
+  int32_t aux0;  /* implementation detail (parent index while building); ignore */
+  int32_t aux1;
+} bvh_node;
+
+/* TriangleMesh SoA (include/mesh.h:9-12): nine float arrays of n entries.  For device builds
+ * the pointers are device pointers; 16-byte aligned arrays take the vectorised path. */
+typedef struct bvh_mesh_soa {
+  const float* v0x; const float* v0y; const float* v0z;
+  const float* v1x; const float* v1y; const float* v1z;
+  const float* v2x; const float* v2y; const float* v2z;
+  uint32_t n;
+} bvh_mesh_soa;
+
+typedef struct bvh_params {
+  int32_t algo;           /* bvh_algo */
+  int32_t morton_bits;    /* LBVH: 30 (reference LBVH), 60 (reference LBVH+ keys) or 63; PLOC: 30 */
+  int32_t treelet_rounds; /* LBVH+: refit+restructure passes (the reference runs 1) */
+  int32_t ploc_radius;    /* PLOC search radius r (reference default 25) */
+  int32_t max_iterations; /* PLOC iteration cap, 0 = 192 */
+  int32_t reserved[3];
+} bvh_params;
+
+/* A device-resident tree owned by the context; valid until the next build on that context. */
+typedef struct bvh_tree {
+  const bvh_node* nodes;   /* device pointer, n_nodes entries */
+  const uint32_t* indices; /* device pointer, n_prims entries: original index of the i-th sorted triangle */
+  uint32_t n_nodes;
+  uint32_t n_prims;
+} bvh_tree;
+
+typedef struct bvh_timing {
+  float total_ms;    /* device time of the whole build (kernels only, upload excluded) */
+  float bounds_ms;   /* scene AABB */
+  float morton_ms;   /* triangle boxes, Morton codes, histograms */
+  float sort_ms;     /* radix sort */
+  float emit_ms;     /* hierarchy + refit (LBVH) / cluster init (PLOC) */
+  float optimize_ms; /* treelet passes (LBVH+) / clustering loop (PLOC) */
+  int32_t ploc_iterations;
+  int32_t reserved;
+  uint64_t ploc_cluster_sum; /* sum of live clusters over PLOC iterations */
+} bvh_timing;
+
+/* Per-ray traversal result (HitInfo, src/render_engine.cu:279-287, minus the normal). */
+typedef struct bvh_hits {
+  float* t;              /* closest hit distance, 1e30 on a miss */
+  int32_t* prim;         /* original triangle index, -1 on a miss */
+  int32_t* nodes_visited;
+  int32_t* aabb_tests;
+  int32_t* tri_tests;
+} bvh_hits;
+
+/* Rays as six SoA arrays (origin xyz, direction xyz). */
+typedef struct bvh_rays {
+  const float* ox; const float* oy; const float* oz;
+  const float* dx; const float* dy; const float* dz;
+  uint32_t n;
+} bvh_rays;
+
+/* Camera (include/render_engine.h:24-33). */
+typedef struct bvh_camera {
+  float eye[3];
+  float look_at[3];
+  float up[3];
+  float fov_y_deg;
+} bvh_camera;
+
+typedef struct bvh_ctx bvh_ctx;
+
+const char* bvh_status_string(bvh_status s);
+/* Library version string. */
+const char* bvh_version(void);
+
+/* Create a context on `device` (CUDA ordinal).  Contexts are not thread-safe. */
+bvh_status bvh_ctx_create(bvh_ctx** out, int device);
+bvh_status bvh_ctx_destroy(bvh_ctx* ctx);
+/* Pre-allocate workspace for meshes of up to n triangles (optional; builds grow it). */
+bvh_status bvh_ctx_reserve(bvh_ctx* ctx, uint32_t n, int32_t algo);
+/* Bytes of device memory the context currently holds. */
+bvh_status bvh_ctx_device_bytes(const bvh_ctx* ctx, uint64_t* bytes);
+
+/* Defaults: LBVH, 30-bit, 1 treelet round, radius 25. */
+bvh_params bvh_default_params(int32_t algo);
+
+/* Build from device-resident SoA.  Asynchronous on `stream` for LBVH/LBVH+ (PLOC reads one
+ * counter per iteration back to the host).  The tree stays owned by the context. */
+bvh_status bvh_build_device(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
+                            bvh_tree* out);
+
+/* Build from host SoA, as BVHBuilder::build does: upload, build, download.  Synchronous.
+ * host_nodes must hold 2n-1 entries (n >= 1), host_indices n entries. */
+bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
+                          bvh_node* host_nodes, uint32_t* host_indices, uint32_t* n_nodes);
+
+/* Copy a device tree to host arrays (2n-1 nodes, n indices). */
+bvh_status bvh_tree_download(bvh_ctx* ctx, const bvh_tree* tree, void* stream, bvh_node* host_nodes,
+                             uint32_t* host_indices);
+
+/* Timing of the last build; waits for it to finish.  Also reports device-side errors. */
+bvh_status bvh_last_timing(bvh_ctx* ctx, bvh_timing* out);
+/* Wait for the last build and report device-side errors (bounded waits that gave up). */
+bvh_status bvh_sync(bvh_ctx* ctx);
+
+/* Closest-hit traversal of explicit rays (device pointers).  Asynchronous. */
+bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
+                     const bvh_rays* rays, const bvh_hits* hits, void* stream);
+/* Primary pinhole rays (generateRay, src/render_engine.cu:155-188) for a width x height
+ * image, one per pixel in row-major order, then traversal.  Asynchronous. */
+bvh_status bvh_trace_pinhole(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
+                             const bvh_camera* cam, int32_t width, int32_t height, const bvh_hits* hits,
+                             void* stream);
+/* The rays bvh_trace_pinhole generates (device pointers, width*height each). */
+bvh_status bvh_pinhole_rays(const bvh_camera* cam, int32_t width, int32_t height, float* ox, float* oy, float* oz,
+                            float* dx, float* dy, float* dz, void* stream);
+/* autoCamera (src/render_engine.cu:601-637) from the root box of a tree (host node). */
+bvh_status bvh_auto_camera(const bvh_node* host_root, bvh_camera* cam);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BVH_GB300_H */

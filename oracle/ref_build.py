@@ -1,0 +1,84 @@
+"""Build recipe for oracle/_ref/ (TEST INFRASTRUCTURE; outputs stay out of git).
+
+* With the reference sources present (REF_ROOT, default /root/reference):
+  - ref_{lbvh,lbvh_plus,ploc,render}.fatbin: the reference's own .cu files, unmodified, compiled
+    to sm_103a device code with the reference's default (non-Release) flags; *_fast.fatbin with
+    its Release flags (-O3 --use_fast_math, CMakeLists.txt:41-45).
+  - libref_eval.so: the reference's src/evaluator.cpp with ref_eval_shim.cpp (host only).
+* Anywhere (GPU machine included): libref_runner.so from ref_runner.cu (our host code that loads the
+  fatbins and replays the reference builders with CUB/Thrust).
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+REF_ROOT = os.environ.get("REF_ROOT", "/root/reference")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FATBINS = {
+    "ref_lbvh": "src/cuda/lbvh_builder.cu",
+    "ref_lbvh_plus": "src/cuda/lbvh_plus_builder.cu",
+    "ref_ploc": "src/cuda/ploc_builder.cu",
+    "ref_render": "src/render_engine.cu",
+}
+
+
+def _nvcc():
+    return shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def have_reference() -> bool:
+    return os.path.isdir(os.path.join(REF_ROOT, "src", "cuda"))
+
+
+def build_fatbins():
+    jobs = []
+    inc = ["-I" + os.path.join(REF_ROOT, "include")]
+    for name, rel in FATBINS.items():
+        src = os.path.join(REF_ROOT, rel)
+        jobs.append([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17"] + inc + [src, "-o", os.path.join(OUT, name + ".fatbin")])
+        jobs.append([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17", "-O3", "--use_fast_math"] + inc
+                    + [src, "-o", os.path.join(OUT, name + "_fast.fatbin")])
+    with cf.ThreadPoolExecutor(max_workers=8) as ex:
+        list(ex.map(_run, jobs))
+
+
+def build_eval():
+    _run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+          "-I" + os.path.join(REF_ROOT, "include"), "-I/usr/local/cuda/include",
+          os.path.join(HERE, "ref_eval_shim.cpp"), os.path.join(REF_ROOT, "src", "evaluator.cpp"),
+          "-o", os.path.join(OUT, "libref_eval.so")])
+
+
+def build_runner():
+    _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+                             os.path.join(HERE, "ref_runner.cu"), "-o", os.path.join(OUT, "libref_runner.so"),
+                             "-lcuda"])
+
+
+def fatbins_present() -> bool:
+    return all(os.path.exists(os.path.join(OUT, n + ".fatbin")) for n in FATBINS)
+
+
+def build(runner: bool = True):
+    os.makedirs(OUT, exist_ok=True)
+    if have_reference():
+        build_fatbins()
+        build_eval()
+    if runner and fatbins_present():
+        build_runner()
+
+
+if __name__ == "__main__":
+    build(runner="--no-runner" not in sys.argv)
