@@ -39,6 +39,11 @@ WORKLOADS = {
                   "10M clustered triangles, PLOC radius 25"),
     "c1_lbvhplus": ("clustered", {"n": 10_000_000, "seed": 1}, "lbvh_plus", 60, 0,
                     "10M clustered triangles, LBVH+ 60-bit, 1 treelet pass"),
+    "c1_lbvh63_4m": ("clustered", {"n": 4_000_000, "seed": 1}, "lbvh", 63, 0,
+                     "4M clustered triangles (config 1 distribution), LBVH 63-bit; profiling size"),
+    "c3_batched": ("batch", {"meshes": 4096, "lo": 64, "hi": 262144}, "lbvh_batched", 30, 0,
+                   "4,096 meshes, triangle counts logU[64, 262144], each built by LBVH-30 in one batched launch "
+                   "sequence replayed as a CUDA graph"),
     "c0_lbvh30": ("uniform_small", {"n": 100_000, "seed": 0}, "lbvh", 30, 0,
                   "100k uniform triangles, LBVH 30-bit"),
 }
@@ -283,6 +288,119 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batched(args):
+    """Config 3: many meshes in one batched, graph-captured build vs a per-mesh loop of single builds."""
+    import ctypes
+    import torch
+
+    import bvh_gb300
+    from bvh_gb300 import _capi as C
+    from bvh_gb300 import meshgen
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    counts = meshgen.batch_counts(kw["meshes"], kw["lo"], kw["hi"], seed=4)
+    mesh, offsets = meshgen.batch(counts, seed=5 + rank)
+    n = mesh.size()
+    count = offsets.shape[0] - 1
+    ctx = bvh_gb300.Context(local)
+    params = ctx.params(C.ALGO_LBVH)
+    d_in = [torch.from_numpy(a).to(dev) for a in mesh.arrays()]
+    ptrs = [t.data_ptr() for t in d_in]
+    stream = torch.cuda.Stream(device=dev)
+    s = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
+        ctx.sync()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        with ClockSampler(local) as clk:
+            ev0.record(stream)
+            for _ in range(args.steps):
+                ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+        ms = ev0.elapsed_time(ev1) / args.steps
+        # stage breakdown without the graph
+        ctx.build_batched(ptrs, offsets, params, s, use_graph=False)
+        t = ctx.last_timing()
+        stages = {"seg_bounds": round(t.bounds_ms, 4), "seg_morton_hist": round(t.morton_ms, 4),
+                  "onesweep_sort": round(t.sort_ms, 4), "delta_emit_refit": round(t.emit_ms, 4)}
+        # plain per-mesh loop of single-mesh builds on the same device-resident data
+        single = bvh_gb300.Context(local)
+        single.reserve(int(counts.max()))
+        loop_reps = 2
+        for _ in range(1):
+            for m in range(count):
+                a = int(offsets[m])
+                single.build_device([p + 4 * a for p in ptrs], int(counts[m]), params, s)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(loop_reps):
+            for m in range(count):
+                a = int(offsets[m])
+                single.build_device([p + 4 * a for p in ptrs], int(counts[m]), params, s)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        loop_ms = e0.elapsed_time(e1) / loop_reps
+        single.close()
+    value = n / (ms / 1e3) / 1e6
+    loop_value = n / (loop_ms / 1e3) / 1e6
+    peak, peak_kind = hbm_peak()
+    bpt = 444.0  # 42-bit segmented keys: B = 276 + 3*8 + 2*6*(8+4)
+    achieved = bpt * n / (ms / 1e3) / 1e9
+    # e2e: pinned host SoA -> device, batched build, nodes + indices back to pinned host memory
+    h_in = [torch.from_numpy(a).pin_memory() for a in mesh.arrays()]
+    n_nodes = 2 * n - count
+    h_nodes = torch.empty(n_nodes * 48, dtype=torch.uint8).pin_memory()
+    h_idx = torch.empty(n * 4, dtype=torch.uint8).pin_memory()
+    e2e_steps = max(1, min(args.steps, 5))
+
+    def e2e_once():
+        with torch.cuda.stream(stream):
+            for d, h in zip(d_in, h_in):
+                d.copy_(h, non_blocking=True)
+            tree = ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
+            C.check(ctx.lib.bvh_tree_download(ctx.handle, ctypes.byref(tree), ctypes.c_void_p(s),
+                                              ctypes.c_void_p(h_nodes.data_ptr()), ctypes.c_void_p(h_idx.data_ptr())))
+
+    e2e_once()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_once()
+    torch.cuda.synchronize(dev)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    line = {
+        "metric": "batched build Mtris/s (device-resident) vs per-mesh loop",
+        "value": round(value * ws, 2), "unit": "Mtris/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+u64", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
+        "config": {"workload": args.workload, "description": desc, "meshes": count, "triangles": n,
+                   "min_mesh": int(counts.min()), "max_mesh": int(counts.max()), "parallelism": f"shards x{ws}",
+                   "l2": "inputs (4.8 GB) exceed the 129 MB L2; no flush"},
+        "per_mesh_loop": {"value": round(loop_value, 2), "unit": "Mtris/s", "ms_per_step": round(loop_ms, 3),
+                          "speedup_batched_over_loop": round(value / loop_value, 2)},
+        "stage_ms": stages,
+        "roofline": {"bound": "hbm", "kernel": "whole batched build", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": bpt},
+        "e2e": {"value": round(n * ws / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
+                "d2h_bytes_per_step": 48 * n_nodes + 4 * n, "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": args.steps * 13,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_reference(args):
     ws, rank, local = dist_info()
     if rank != 0:
@@ -305,6 +423,7 @@ def run_reference(args):
             nodes, idx, ms = R.lbvh_plus(arrays)
             return ms[0], ms[7]
         nodes, idx, ms = R.lbvh(arrays)
+        once.stages = [float(x) for x in ms[1:6]]
         return ms[0], ms[6]
 
     for _ in range(args.warmup):
@@ -337,6 +456,9 @@ def run_reference(args):
                          "sample": f"whole workload on the GPU, {args.steps} builds (the reference path is CUDA)"},
         "clocks": clk.summary(),
     }
+    if getattr(once, "stages", None):
+        line["stage_ms_last"] = dict(zip(["bounds", "morton", "sort", "topology", "refit"],
+                                         [round(x, 4) for x in once.stages]))
     print(json.dumps(line), flush=True)
 
 
@@ -353,6 +475,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif WORKLOADS[args.workload][2] == "lbvh_batched":
+        run_batched(args)
     else:
         run_ours(args)
 

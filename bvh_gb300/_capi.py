@@ -65,6 +65,13 @@ class Rays(ctypes.Structure):
     _fields_ = [(f, c_void_p) for f in ("ox", "oy", "oz", "dx", "dy", "dz")] + [("n", c_uint32)]
 
 
+class Batch(ctypes.Structure):
+    _fields_ = [("mesh", MeshSoA), ("offsets", c_void_p), ("count", c_uint32)]
+
+
+BATCH_USE_GRAPH = 1
+
+
 class Camera(ctypes.Structure):
     _fields_ = [("eye", c_float * 3), ("look_at", c_float * 3), ("up", c_float * 3), ("fov_y_deg", c_float)]
 
@@ -89,6 +96,7 @@ SIGNATURES = {
                                   POINTER(Hits), c_void_p]),
     "bvh_pinhole_rays": (c_int, [POINTER(Camera), c_int32, c_int32] + [c_void_p] * 6 + [c_void_p]),
     "bvh_auto_camera": (c_int, [c_void_p, POINTER(Camera)]),
+    "bvh_build_batched": (c_int, [c_void_p, POINTER(Batch), POINTER(Params), c_void_p, POINTER(Tree)]),
 }
 
 _lib = None

@@ -109,6 +109,24 @@ class Context:
                                           ctypes.c_void_p(stream), ctypes.byref(t)), "bvh_build_device")
         return t
 
+    def build_batched(self, ptrs: Sequence[int], offsets: np.ndarray, params: C.Params, stream: int = 0,
+                      use_graph: bool = False) -> C.Tree:
+        """Build every mesh of a batch: nine device addresses of the concatenated SoA and the
+        count+1 host offsets.  Mesh m's tree is nodes[2*offsets[m]-m : 2*offsets[m+1]-m-1]."""
+        offsets = np.ascontiguousarray(offsets, np.uint32)
+        count = offsets.shape[0] - 1
+        b = C.Batch()
+        b.mesh = C.mesh_struct(ptrs, int(offsets[-1]))
+        b.offsets = offsets.ctypes.data
+        b.count = count
+        p = C.Params.from_buffer_copy(params)
+        p.reserved[0] = C.BATCH_USE_GRAPH if use_graph else 0
+        t = C.Tree()
+        C.check(self.lib.bvh_build_batched(self.handle, ctypes.byref(b), ctypes.byref(p), ctypes.c_void_p(stream),
+                                           ctypes.byref(t)), "bvh_build_batched")
+        self._batch_keep = offsets
+        return t
+
     def build_host(self, mesh: TriangleMesh, params: C.Params, stream: int = 0):
         """Upload, build, download (BVHBuilder::build).  Returns (nodes, indices)."""
         n = mesh.size()

@@ -1,8 +1,10 @@
 // capi.cu -- the C ABI (include/bvh_gb300.h): contexts, builds, timing, traversal.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/bvh_gb300.h"
 #include "lbvh.cuh"
@@ -10,9 +12,18 @@
 
 using namespace bvhgb;
 
+struct BatchGraph {
+  cudaGraphExec_t exec = nullptr;
+  const float* ptrs[9] = {};
+  uint32_t n = 0, count = 0;
+  std::vector<uint32_t> offsets;
+};
+
 struct bvh_ctx {
   int device = 0;
   Workspace ws;
+  BatchGraph bgraph;
+  cudaStream_t capture_stream = nullptr;  // for CUDA graph capture (never the legacy stream)
   StageEvents evs;
   bvh_timing last{};
   int last_algo = -1;
@@ -66,6 +77,11 @@ extern "C" bvh_status bvh_ctx_create(bvh_ctx** out, int device) {
     if (cudaEventCreate(&c->evs.ev[k]) != cudaSuccess) { delete c; return BVH_ERR_DEVICE; }
   c->evs.use = true;
   if (cudaMallocHost(&c->h_status, 64) != cudaSuccess) { delete c; return BVH_ERR_OUT_OF_MEMORY; }
+  if (prepare_kernels() != cudaSuccess) { delete c; return BVH_ERR_DEVICE; }
+  if (cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return BVH_ERR_DEVICE;
+  }
   *out = c;
   return BVH_OK;
 }
@@ -74,6 +90,8 @@ extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
   if (!ctx) return BVH_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  if (ctx->bgraph.exec) cudaGraphExecDestroy(ctx->bgraph.exec);
+  if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
   workspace_free(ctx->ws);
   for (int k = 0; k < 8; ++k) cudaEventDestroy(ctx->evs.ev[k]);
   cudaFreeHost(ctx->h_status);
@@ -107,7 +125,7 @@ static bool valid_params(const bvh_params* p) {
       return p->morton_bits == 30 || p->morton_bits == 60 || p->morton_bits == 63;
     case BVH_ALGO_LBVH_PLUS:
       return (p->morton_bits == 30 || p->morton_bits == 60 || p->morton_bits == 63) && p->treelet_rounds >= 0 &&
-             p->treelet_rounds <= 64;
+             p->treelet_rounds <= 63;
     case BVH_ALGO_PLOC:
       return p->ploc_radius >= 1 && p->ploc_radius <= 512 && p->max_iterations >= 0;
   }
@@ -267,6 +285,136 @@ extern "C" bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, con
   s = check_status_word(ctx);
   if (s == BVH_OK && n_nodes) *n_nodes = tree.n_nodes;
   return s;
+}
+
+// ---------------------------------------------------------------------------------------
+// batched builds
+// ---------------------------------------------------------------------------------------
+// Staged batch layout (pinned host copy and device copy, 32-bit words):
+//   [0, count]                  mesh offsets
+//   [items_at, items_at + 4*k)  work items (mesh, begin, end, 0), meshes split every kSegChunk
+static size_t items_at(uint32_t count) { return ((size_t)count + 1 + 3) & ~size_t(3); }
+static uint32_t count_items(const uint32_t* offsets, uint32_t count) {
+  uint64_t k = 0;
+  for (uint32_t m = 0; m < count; ++m) k += div_up(offsets[m + 1] - offsets[m], kSegChunk);
+  return (uint32_t)k;
+}
+static void stage_layout(uint32_t* dst, const uint32_t* offsets, uint32_t count) {
+  memcpy(dst, offsets, ((size_t)count + 1) * 4);
+  SegItem* it = reinterpret_cast<SegItem*>(dst + items_at(count));
+  for (uint32_t m = 0; m < count; ++m)
+    for (uint32_t b = offsets[m]; b < offsets[m + 1]; b += kSegChunk)
+      *it++ = SegItem{m, b, std::min(offsets[m + 1], b + kSegChunk), 0};
+}
+
+static cudaError_t reserve_batch(Workspace& ws, uint32_t n, uint32_t count, size_t words) {
+  cudaError_t e = workspace_reserve(ws, n);
+  if (e != cudaSuccess) return e;
+  if (ws.bat_words_cap < words || ws.bat_count_cap < count || !ws.bat_offsets) {
+    cudaDeviceSynchronize();  // the staging buffer may still be read by queued copies
+    cudaFree(ws.bat_offsets);
+    cudaFreeHost(ws.bat_offsets_h);
+    cudaFree(ws.bat_mbox);
+    ws.bat_offsets = nullptr; ws.bat_offsets_h = nullptr; ws.bat_mbox = nullptr;
+    ws.bat_count_cap = 0; ws.bat_words_cap = 0; ws.bat_items = 0;
+    size_t wcap = words < 1024 ? 1024 : words;
+    uint32_t ccap = count < 64 ? 64 : count;
+    if ((e = cudaMalloc(&ws.bat_offsets, wcap * 4)) != cudaSuccess) return e;
+    if ((e = cudaMallocHost(&ws.bat_offsets_h, wcap * 4)) != cudaSuccess) return e;
+    memset(ws.bat_offsets_h, 0, wcap * 4);
+    if ((e = cudaMalloc(&ws.bat_mbox, (size_t)ccap * 8 * 4)) != cudaSuccess) return e;
+    ws.bat_count_cap = ccap;
+    ws.bat_words_cap = wcap;
+  }
+  if (ws.bat_n_cap < n || !ws.bat_indices) {
+    cudaFree(ws.bat_indices);
+    ws.bat_indices = nullptr;
+    ws.bat_n_cap = 0;
+    if ((e = cudaMalloc(&ws.bat_indices, (size_t)(n ? n : 1) * 4)) != cudaSuccess) return e;
+    ws.bat_n_cap = n;
+  }
+  return cudaSuccess;
+}
+
+static cudaError_t enqueue_batch(bvh_ctx* ctx, const MeshPtrs& m, uint32_t n, uint32_t count, size_t words,
+                                 cudaStream_t st, bool events) {
+  Workspace& ws = ctx->ws;
+  cudaError_t e = cudaMemcpyAsync(ws.bat_offsets, ws.bat_offsets_h, words * 4, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  StageEvents none;
+  const SegItem* items = reinterpret_cast<const SegItem*>(ws.bat_offsets + items_at(count));
+  return batched_build(ws, m, n, ws.bat_offsets, count, items, ws.bat_items, ws.bat_mbox, ws.bat_indices, st,
+                       events ? &ctx->evs : &none);
+}
+
+extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_params* params, void* stream,
+                                        bvh_tree* out) {
+  if (!ctx || !batch || !out || !params || !mesh_ok(&batch->mesh) || !batch->offsets) return BVH_ERR_INVALID_ARG;
+  if (params->algo != BVH_ALGO_LBVH || params->morton_bits != 30) return BVH_ERR_UNSUPPORTED;
+  const uint32_t n = batch->mesh.n, count = batch->count;
+  if (count == 0 || count > n || count > (1u << 24) || batch->offsets[0] != 0 || batch->offsets[count] != n)
+    return BVH_ERR_INVALID_ARG;
+  for (uint32_t k = 0; k < count; ++k)
+    if (batch->offsets[k + 1] <= batch->offsets[k]) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace& ws = ctx->ws;
+  ctx->have_timing = false;
+  ctx->last = bvh_timing{};
+  ctx->last_algo = params->algo;
+  const uint32_t n_items = count_items(batch->offsets, count);
+  const size_t words = items_at(count) + 4 * (size_t)n_items;
+  cudaError_t e = reserve_batch(ws, n, count, words);
+  if (e != cudaSuccess) return from_cuda(e);
+  // the device copy reads the pinned staging buffer when it executes: rewrite it only when the
+  // layout changed, after the work that may still read it has finished
+  const bool changed = ws.bat_items != n_items ||
+                       memcmp(ws.bat_offsets_h, batch->offsets, ((size_t)count + 1) * 4) != 0;
+  if (changed) {
+    cudaDeviceSynchronize();
+    stage_layout(ws.bat_offsets_h, batch->offsets, count);
+    ws.bat_items = n_items;
+  }
+  MeshPtrs m = mesh_ptrs(&batch->mesh);
+  const bool use_graph = params->reserved[0] == BVH_BATCH_USE_GRAPH;
+  if (use_graph) {
+    BatchGraph& g = ctx->bgraph;
+    bool same = g.exec && !changed && g.n == n && g.count == count && memcmp(g.ptrs, m.v, sizeof(g.ptrs)) == 0;
+    if (!same) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+      // capture on the context's own stream: the caller's may be the legacy default stream,
+      // which cannot be captured; the graph is launched on the caller's stream
+      cudaGraph_t graph = nullptr;
+      if ((e = cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return from_cuda(e);
+      cudaError_t e2 = enqueue_batch(ctx, m, n, count, words, ctx->capture_stream, false);
+      e = cudaStreamEndCapture(ctx->capture_stream, &graph);
+      if (e2 != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return from_cuda(e2); }
+      if (e != cudaSuccess) return from_cuda(e);
+      e = cudaGraphInstantiate(&g.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) { g.exec = nullptr; return from_cuda(e); }
+      memcpy(g.ptrs, m.v, sizeof(g.ptrs));
+      g.n = n;
+      g.count = count;
+    }
+    cudaEventRecord(ctx->evs.ev[0], st);
+    if ((e = cudaGraphLaunch(g.exec, st)) != cudaSuccess) return from_cuda(e);
+    for (int k = 1; k <= 5; ++k) cudaEventRecord(ctx->evs.ev[k], st);
+  } else {
+    if ((e = enqueue_batch(ctx, m, n, count, words, st, true)) != cudaSuccess) return from_cuda(e);
+  }
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  cudaMemcpyAsync(ctx->h_status, ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(ctx->evs.ev[6], st);
+  ctx->last_stream = st;
+  ctx->have_timing = true;
+  out->nodes = reinterpret_cast<const bvh_node*>(ws.nodes);
+  out->indices = ws.bat_indices;
+  out->n_nodes = 2 * n - count;
+  out->n_prims = n;
+  return from_cuda(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------------------------------

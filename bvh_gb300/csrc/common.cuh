@@ -121,6 +121,59 @@ __device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
 __device__ __forceinline__ void st_cg(float4* p, float4 v) { __stcg(p, v); }
 __device__ __forceinline__ void st_cg(int* p, int v) { __stcg(p, v); }
 
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Decoupled look-back over tiles (Merrill & Garland): descriptor words hold a 2-bit flag and the
+// value in one word, so relaxed loads suffice.  Predecessors are read W at a time to shorten the
+// dependent chain; an unpublished word (flag 0) is polled again, at most kSpinLimit times.
+template <int W, typename T>
+__device__ __forceinline__ T lookback(const T* desc, size_t stride, int64_t tile, T flag_mask, T flag_inc,
+                                      uint32_t* status, uint32_t status_bit) {
+  T excl = 0;
+  int64_t j = tile - 1;
+  uint32_t spins = 0;
+  while (j >= 0) {
+    T v[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) v[k] = (j - k >= 0) ? ld_relaxed(desc + (size_t)(j - k) * stride) : flag_inc;
+    int k = 0;
+    bool done = false;
+#pragma unroll
+    for (; k < W; ++k) {
+      const T fl = v[k] & flag_mask;
+      if (fl == 0) break;  // not yet published: poll again from here
+      excl += v[k] & ~flag_mask;
+      if (fl == flag_inc) { done = true; break; }
+    }
+    if (done) break;
+    if (k < W) {
+      j -= k;
+      if (++spins > kSpinLimit) {
+        atomicOr(status, status_bit);
+        break;
+      }
+      continue;
+    }
+    j -= W;
+  }
+  return excl;
+}
+
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

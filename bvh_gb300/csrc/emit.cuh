@@ -1,0 +1,227 @@
+// emit.cuh -- bottom-up Karras hierarchy + refit, shared by single-mesh and batched builds.
+//
+// Reference: kBuildInternalNodes_nt (src/cuda/lbvh_builder.cu:183-229), kInitLeafNodes_nt
+// (:231-241) and kRefitHierarchy_nt (:243-274); same node ids, children and boxes.
+//
+// Step 1 (k_delta): D[k] = delta(k, k+1) + 1 for adjacent sorted positions, one byte each
+// (delta_nt, lbvh_builder.cu:33-43: common-prefix length of the codes, or 32/64 +
+// clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0 marks a segment boundary).
+// Step 2 (k_emit): one thread per sorted position climbs.  A node with range [f, l] has its
+// parent's split on the side whose adjacent delta is larger (Apetrei 2014): gamma = l when
+// D[l] > D[f-1], else gamma = f-1.  The second child to reach gamma's rendezvous word completes
+// the parent.  Karras ids: leaf i -> n-1+i, a left child's id is its last index, a right
+// child's its first, the root is 0.  Segments (batched meshes) number their nodes from their
+// own base and see delta = -1 across their boundaries.
+#pragma once
+#include "common.cuh"
+
+namespace bvhgb {
+
+// Single mesh: one segment [0, n) with node base 0; original indices are global.
+struct SegSingle {
+  uint32_t n;
+  __device__ __forceinline__ void get(uint32_t /*i*/, uint32_t& off, uint32_t& cnt, uint32_t& nbase) const {
+    off = 0;
+    cnt = n;
+    nbase = 0;
+  }
+  __device__ __forceinline__ uint32_t mesh_of_key(unsigned long long) const { return 0; }
+};
+
+// Batched meshes: key = mesh << 30 | code30; mesh m owns sorted positions
+// [offsets[m], offsets[m+1]) and node ids [2*offsets[m] - m, ...).
+struct SegBatch {
+  const unsigned long long* keys;
+  const uint32_t* offsets;
+  __device__ __forceinline__ void get(uint32_t i, uint32_t& off, uint32_t& cnt, uint32_t& nbase) const {
+    const uint32_t m = (uint32_t)(__ldg(keys + i) >> 30);
+    off = __ldg(offsets + m);
+    cnt = __ldg(offsets + m + 1) - off;
+    nbase = 2 * off - m;
+  }
+};
+
+__device__ __forceinline__ void store_node(Node* nodes, uint32_t idx, const Box& b, int32_t l, int32_t r, int32_t aux0) {
+  float4* p = reinterpret_cast<float4*>(nodes + idx);
+  __stcg(p, b.lo);
+  __stcg(p + 1, b.hi);
+  __stcg(reinterpret_cast<int4*>(p + 2), make_int4(l, r, aux0, 0));
+}
+__device__ __forceinline__ Box load_node_box(const Node* nodes, uint32_t idx) {
+  const float4* p = reinterpret_cast<const float4*>(nodes + idx);
+  Box b;
+  b.lo = __ldcg(p);
+  b.hi = __ldcg(p + 1);
+  return b;
+}
+
+__device__ __forceinline__ unsigned long long atom_exch_acq_rel(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
+
+// delta(k, k+1) + 1 as a byte.  K = key type; BATCH selects the segmented 30-bit rule.
+template <typename K, bool BATCH>
+__global__ void __launch_bounds__(256) k_delta(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                               const uint32_t* __restrict__ offsets, uint8_t* __restrict__ D,
+                                               uint32_t n) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k + 1 >= n) return;
+  const K a = __ldg(keys + k), b = __ldg(keys + k + 1);
+  int d;
+  if constexpr (BATCH) {
+    const uint32_t ma = (uint32_t)((unsigned long long)a >> 30), mb = (uint32_t)((unsigned long long)b >> 30);
+    if (ma != mb) {
+      d = -1;
+    } else if (a == b) {
+      const uint32_t off = __ldg(offsets + ma);
+      d = 32 + __clz((__ldg(vals + k) - off) ^ (__ldg(vals + k + 1) - off));
+    } else {
+      d = __clz((uint32_t)((a ^ b) & 0x3FFFFFFFull));
+    }
+  } else if constexpr (sizeof(K) == 4) {
+    d = a == b ? 32 + __clz(__ldg(vals + k) ^ __ldg(vals + k + 1)) : __clz((uint32_t)(a ^ b));
+  } else {
+    d = a == b ? 64 + __clzll((unsigned long long)(__ldg(vals + k) ^ __ldg(vals + k + 1)))
+               : __clzll((unsigned long long)(a ^ b));
+  }
+  D[k] = (uint8_t)(d + 1);
+}
+
+template <bool PARENTS>
+__device__ __forceinline__ void write_internal(Node* nodes, uint32_t nb, int32_t my, const Box& box, int32_t lc,
+                                               int32_t rc) {
+  store_node(nodes, nb + (uint32_t)my, box, lc, rc, -1);
+  if (PARENTS) {
+    __stcg(&nodes[nb + lc].aux0, my);
+    __stcg(&nodes[nb + rc].aux0, my);
+  }
+}
+
+// Climb state of one lane: the node it currently owns covers sorted positions [f, l].
+struct Climb {
+  uint32_t f, l;
+  Box box;
+  int32_t lc, rc, my;
+  bool internal;
+};
+
+template <typename Seg, bool PARENTS>
+__global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
+                                              const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
+                                              unsigned long long* __restrict__ slots, const uint32_t* epoch_word,
+                                              uint32_t n, Seg seg, uint32_t* __restrict__ out_idx) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t wbase = i - lane;  // sorted position of lane 0
+  bool active = i < n;
+  uint32_t off = 0, cnt = 1, nb = 0;
+  Climb c;
+  c.f = c.l = i;
+  c.lc = c.rc = -1;
+  c.internal = false;
+  c.my = 0;
+  c.box.lo = c.box.hi = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (active) {
+    seg.get(i, off, cnt, nb);
+    const uint32_t prim_g = __ldg(vals + i);
+    const uint32_t prim = prim_g - off;  // original index within the mesh
+    if (out_idx) out_idx[i] = prim;
+    const float4* bp = reinterpret_cast<const float4*>(tri_boxes + prim_g);
+    c.box.lo = __ldg(bp);
+    c.box.hi = __ldg(bp + 1);
+    c.my = (int32_t)(cnt - 1) + (int32_t)(i - off);
+    store_node(nodes, nb + (uint32_t)c.my, c.box, (int32_t)(prim | kLeafBit), -1, -1);
+    if (cnt == 1) active = false;
+  }
+  // ---- phase 1: merges whose two children are owned by lanes of this warp (no atomics) ----
+  // The lane of a node's first position owns it; a left child at split gamma finds its right
+  // sibling at lane gamma + 1 - wbase.
+  bool is_left = false;
+  uint32_t gamma = 0;
+  while (true) {
+    bool want = false;
+    if (active) {
+      const int dl = c.f == 0 ? -1 : (int)__ldg(D + c.f - 1) - 1;
+      const int dr = c.l + 1 >= n ? -1 : (int)__ldg(D + c.l) - 1;
+      if (dl < 0 && dr < 0) {  // segment root (internal: single-triangle meshes stopped above)
+        write_internal<PARENTS>(nodes, nb, 0, c.box, c.lc, c.rc);
+        active = false;
+      } else {
+        is_left = dr > dl;
+        gamma = is_left ? c.l : c.f - 1;
+        if (c.internal) {
+          c.my = (int32_t)((is_left ? c.l : c.f) - off);
+          write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
+          c.internal = false;  // written; `my` now names it
+        }
+        want = is_left && gamma + 1 >= wbase && gamma + 1 < wbase + 32;
+      }
+    }
+    const uint32_t p = want ? gamma + 1 - wbase : lane;
+    const bool p_active = __shfl_sync(0xffffffffu, active, p);
+    const bool p_left = __shfl_sync(0xffffffffu, is_left, p);
+    const uint32_t p_gamma = __shfl_sync(0xffffffffu, gamma, p);
+    const uint32_t p_l = __shfl_sync(0xffffffffu, c.l, p);
+    const int32_t p_my = __shfl_sync(0xffffffffu, c.my, p);
+    Box pb;
+    pb.lo.x = __shfl_sync(0xffffffffu, c.box.lo.x, p);
+    pb.lo.y = __shfl_sync(0xffffffffu, c.box.lo.y, p);
+    pb.lo.z = __shfl_sync(0xffffffffu, c.box.lo.z, p);
+    pb.hi.x = __shfl_sync(0xffffffffu, c.box.hi.x, p);
+    pb.hi.y = __shfl_sync(0xffffffffu, c.box.hi.y, p);
+    pb.hi.z = __shfl_sync(0xffffffffu, c.box.hi.z, p);
+    pb.lo.w = pb.hi.w = 0.f;
+    const bool paired = want && p_active && !p_left && p_gamma == gamma;
+    // a right lane is consumed when a left lane paired with it: the two share the match key
+    const uint32_t key = paired ? p : lane;
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const bool consumed = !paired && __popc(peers) > 1;
+    if (paired) {
+      c.lc = c.my;
+      c.rc = p_my;
+      c.l = p_l;
+      c.box = box_union(c.box, pb);
+      c.internal = true;
+    }
+    if (consumed) active = false;
+    if (!__any_sync(0xffffffffu, paired)) break;
+  }
+  if (!active) return;
+  // ---- phase 2: the remaining nodes meet their siblings through the rendezvous words ----
+  const unsigned long long tag = (unsigned long long)__ldcg(epoch_word) << 32;
+  while (true) {
+    const uint32_t far = is_left ? c.f : c.l;
+    const unsigned long long old = atom_exch_acq_rel(slots + gamma, tag | far);
+    if ((old & 0xffffffff00000000ull) != tag) return;  // first child to arrive
+    const uint32_t other = (uint32_t)old;
+    const int32_t g = (int32_t)(gamma - off);
+    int32_t sib;
+    if (is_left) {
+      sib = (other == gamma + 1) ? (int32_t)cnt + g : g + 1;
+      c.lc = c.my;
+      c.rc = sib;
+      c.l = other;
+      c.box = box_union(c.box, load_node_box(nodes, nb + (uint32_t)sib));
+    } else {
+      sib = (other == gamma) ? (int32_t)cnt - 1 + g : g;
+      c.lc = sib;
+      c.rc = c.my;
+      c.f = other;
+      c.box = box_union(load_node_box(nodes, nb + (uint32_t)sib), c.box);
+    }
+    const int dl = c.f == 0 ? -1 : (int)__ldg(D + c.f - 1) - 1;
+    const int dr = c.l + 1 >= n ? -1 : (int)__ldg(D + c.l) - 1;
+    if (dl < 0 && dr < 0) {
+      write_internal<PARENTS>(nodes, nb, 0, c.box, c.lc, c.rc);
+      return;
+    }
+    is_left = dr > dl;
+    gamma = is_left ? c.l : c.f - 1;
+    c.my = (int32_t)((is_left ? c.l : c.f) - off);
+    write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
+  }
+}
+
+}  // namespace bvhgb

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cstdio>
 
+#include "emit.cuh"
 #include "lbvh.cuh"
 
 namespace bvhgb {
@@ -31,6 +32,7 @@ ScratchLayout scratch_layout(uint32_t n) {
   size_t o = 0;
   L.status = o; o += 1;
   L.ticket = o; o += 1;
+  L.epoch = o; o += 1;
   o = (o + 3) & ~size_t(3);
   L.scene = o; o += 8;
   L.ploc = o; o += 16;
@@ -78,7 +80,11 @@ __global__ void __launch_bounds__(256) k_bounds(MeshPtrs m, uint32_t n, int vec4
     size_t words4 = (L.zero_end - L.zero_begin) / 4;
     for (size_t w = gtid; w < words4; w += gsz) z[w] = make_uint4(0, 0, 0, 0);
     for (size_t w = L.zero_begin + words4 * 4 + gtid; w < L.zero_end; w += gsz) scratch[w] = 0;
-    if (gtid == 0) scratch[L.status] = 0;
+    if (gtid == 0) {
+      scratch[L.status] = 0;
+      uint32_t e = scratch[L.epoch] + kEpochStride;
+      scratch[L.epoch] = e < kEpochStride ? kEpochStride : e;
+    }
   }
   float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
   uint32_t done = 0;
@@ -349,26 +355,12 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(const K* __restrict__ kin,
   uint32_t* desc = scratch + L.desc + ((size_t)pass * tiles) * BINS;
   uint32_t excl = 0;
   if (tile == 0) {
-    st_release(desc + b, kFlagInc | cnt);
+    st_relaxed(desc + b, kFlagInc | cnt);
   } else {
-    st_release(desc + (size_t)tile * BINS + b, kFlagAgg | cnt);
-    int64_t j = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    while (j >= 0) {
-      uint32_t v = ld_acquire(desc + (size_t)j * BINS + b);
-      uint32_t fl = v & ~kValMask;
-      if (fl == 0) {
-        if (++spins > kSpinLimit) {
-          atomicOr(scratch + L.status, kStatusSortTimeout);
-          break;
-        }
-        continue;
-      }
-      excl += v & kValMask;
-      if (fl == kFlagInc) break;
-      --j;
-    }
-    st_release(desc + (size_t)tile * BINS + b, kFlagInc | (excl + cnt));
+    st_relaxed(desc + (size_t)tile * BINS + b, kFlagAgg | cnt);
+    excl = lookback<16, uint32_t>(desc + b, BINS, (int64_t)tile, ~kValMask, kFlagInc, scratch + L.status,
+                                  kStatusSortTimeout);
+    st_relaxed(desc + (size_t)tile * BINS + b, kFlagInc | (excl + cnt));
   }
   s_gstart[b] = binbase + excl;
   __syncthreads();
@@ -405,18 +397,26 @@ size_t onesweep_smem() {
 }
 
 template <typename K>
+cudaError_t set_sort_attributes() {
+  constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
+  return cudaFuncSetAttribute(k_onesweep<K, kSortThreads, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)onesweep_smem<K>());
+}
+
+// Kernel attributes set once per device, outside any stream capture.
+cudaError_t prepare_kernels() {
+  cudaError_t e = set_sort_attributes<uint32_t>();
+  if (e == cudaSuccess) e = set_sort_attributes<unsigned long long>();
+  return e;
+}
+
+template <typename K>
 cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L, int* final_buf) {
   constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
   constexpr int TILE = kSortThreads * IPT;
   const uint32_t tiles = div_up(n, TILE);
   const size_t smem = onesweep_smem<K>();
   auto kern = k_onesweep<K, kSortThreads, IPT>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
     const K* kin = reinterpret_cast<const K*>(ws.keys[cur]);
@@ -430,117 +430,15 @@ cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, con
 }
 
 // ---------------------------------------------------------------------------------------
-// k_emit: bottom-up Karras hierarchy + refit in one pass
-// ---------------------------------------------------------------------------------------
-// delta_nt (lbvh_builder.cu:33-43) / delta_P (lbvh_plus_builder.cu:41-47): common-prefix length of
-// the (code, original index) keys; -1 outside [0, n).
-template <typename K>
-__device__ __forceinline__ int karras_delta(const K* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
-                                            int64_t i, int64_t j) {
-  if (j < 0 || j >= (int64_t)n) return -1;
-  K a = __ldg(keys + i), b = __ldg(keys + j);
-  if (a == b) {
-    uint32_t x = __ldg(vals + i) ^ __ldg(vals + j);
-    if constexpr (sizeof(K) == 4) return 32 + __clz(x);
-    else return 64 + __clzll((unsigned long long)x);
-  }
-  if constexpr (sizeof(K) == 4) return __clz((uint32_t)(a ^ b));
-  else return __clzll((unsigned long long)(a ^ b));
-}
-
-__device__ __forceinline__ void store_node(Node* nodes, int32_t idx, const Box& b, int32_t l, int32_t r, int32_t aux0) {
-  float4* p = reinterpret_cast<float4*>(nodes + idx);
-  __stcg(p, b.lo);
-  __stcg(p + 1, b.hi);
-  __stcg(reinterpret_cast<int4*>(p + 2), make_int4(l, r, aux0, 0));
-}
-__device__ __forceinline__ Box load_node_box(const Node* nodes, int32_t idx) {
-  const float4* p = reinterpret_cast<const float4*>(nodes + idx);
-  Box b;
-  b.lo = __ldcg(p);
-  b.hi = __ldcg(p + 1);
-  return b;
-}
-
-// One thread per sorted position i.  A thread owns the range [f, l] of the node it is building;
-// it finds the parent's split gamma from the neighbouring prefixes (the side with the longer
-// common prefix is the parent's, Apetrei 2014), publishes its far endpoint in slot[gamma] and the
-// second arrival continues with the union.  Internal node ids follow Karras: a left child's id is
-// its last index, a right child's id its first index, the root is 0, leaf i is n-1+i.
-template <typename K, bool PARENTS>
-__global__ void __launch_bounds__(256) k_emit(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
-                                              const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
-                                              unsigned long long* __restrict__ slots, uint32_t epoch, uint32_t n) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t prim = __ldg(vals + i);
-  Box box;
-  {
-    const float4* bp = reinterpret_cast<const float4*>(tri_boxes + prim);
-    box.lo = __ldg(bp);
-    box.hi = __ldg(bp + 1);
-  }
-  int32_t my = (int32_t)(n - 1 + i);
-  store_node(nodes, my, box, (int32_t)(prim | kLeafBit), -1, -1);
-  if (n == 1) return;
-  int64_t f = i, l = i;
-  int32_t lc = -1, rc = -1;
-  bool internal = false;
-  const unsigned long long tag = (unsigned long long)epoch << 32;
-  while (true) {
-    if (internal && f == 0 && l == (int64_t)n - 1) {
-      store_node(nodes, 0, box, lc, rc, -1);
-      if (PARENTS) {
-        __stcg(&nodes[lc].aux0, 0);
-        __stcg(&nodes[rc].aux0, 0);
-      }
-      return;
-    }
-    const int dl = karras_delta(keys, vals, n, f - 1, f);
-    const int dr = karras_delta(keys, vals, n, l, l + 1);
-    const bool is_left = dr > dl;
-    const uint32_t gamma = is_left ? (uint32_t)l : (uint32_t)(f - 1);
-    if (internal) {
-      my = (int32_t)(is_left ? l : f);
-      store_node(nodes, my, box, lc, rc, -1);
-      if (PARENTS) {
-        __stcg(&nodes[lc].aux0, my);
-        __stcg(&nodes[rc].aux0, my);
-      }
-    }
-    const uint32_t far = is_left ? (uint32_t)f : (uint32_t)l;
-    __threadfence();
-    const unsigned long long old = atomicExch(slots + gamma, tag | far);
-    if ((old & 0xffffffff00000000ull) != tag) return;  // first child to arrive
-    __threadfence();
-    const uint32_t other = (uint32_t)old;
-    int32_t sib;
-    if (is_left) {
-      sib = (other == gamma + 1) ? (int32_t)(n + gamma) : (int32_t)(gamma + 1);
-      lc = my;
-      rc = sib;
-      l = other;
-      box = box_union(box, load_node_box(nodes, sib));
-    } else {
-      sib = (other == gamma) ? (int32_t)(n - 1 + gamma) : (int32_t)gamma;
-      lc = sib;
-      rc = my;
-      f = other;
-      box = box_union(load_node_box(nodes, sib), box);
-    }
-    internal = true;
-  }
-}
-
-// ---------------------------------------------------------------------------------------
 // workspace
 // ---------------------------------------------------------------------------------------
 void workspace_free(Workspace& ws) {
   cudaFree(ws.keys[0]); cudaFree(ws.keys[1]);
   cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
-  cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch);
+  cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch); cudaFree(ws.delta);
   cudaFree(ws.cbox[0]); cudaFree(ws.cbox[1]); cudaFree(ws.cid[0]); cudaFree(ws.cid[1]); cudaFree(ws.nbr);
   cudaFree(ws.mesh_dev);
+  cudaFree(ws.bat_offsets); cudaFreeHost(ws.bat_offsets_h); cudaFree(ws.bat_mbox); cudaFree(ws.bat_indices);
   ws = Workspace();
 }
 
@@ -548,9 +446,10 @@ cudaError_t workspace_reserve(Workspace& ws, uint32_t n) {
   if (n <= ws.cap_n && ws.scratch) return cudaSuccess;
   uint32_t cap = std::max<uint32_t>(n, 1024);
   cudaFree(ws.keys[0]); cudaFree(ws.keys[1]); cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
-  cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch);
+  cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch); cudaFree(ws.delta);
   ws.keys[0] = ws.keys[1] = nullptr; ws.vals[0] = ws.vals[1] = nullptr;
-  ws.boxes = nullptr; ws.nodes = nullptr; ws.slots = nullptr; ws.scratch = nullptr; ws.cap_n = 0;
+  ws.boxes = nullptr; ws.nodes = nullptr; ws.slots = nullptr; ws.scratch = nullptr; ws.delta = nullptr;
+  ws.cap_n = 0;
   cudaError_t e;
   if ((e = cudaMalloc(&ws.keys[0], (size_t)cap * 8)) != cudaSuccess) return e;
   if ((e = cudaMalloc(&ws.keys[1], (size_t)cap * 8)) != cudaSuccess) return e;
@@ -559,12 +458,12 @@ cudaError_t workspace_reserve(Workspace& ws, uint32_t n) {
   if ((e = cudaMalloc(&ws.boxes, (size_t)cap * sizeof(Box))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&ws.nodes, (2 * (size_t)cap) * sizeof(Node))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&ws.slots, (size_t)cap * 8)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&ws.delta, (size_t)cap + 16)) != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(cap);
   if ((e = cudaMalloc(&ws.scratch, L.total * 4)) != cudaSuccess) return e;
   if ((e = cudaMemset(ws.slots, 0, (size_t)cap * 8)) != cudaSuccess) return e;
   if ((e = cudaMemset(ws.scratch, 0, L.total * 4)) != cudaSuccess) return e;
   ws.scratch_words = L.total;
-  ws.epoch = 0;
   ws.cap_n = cap;
   return cudaSuccess;
 }
@@ -573,15 +472,6 @@ static inline bool all_aligned16(const MeshPtrs& m) {
   for (int k = 0; k < 9; ++k)
     if (reinterpret_cast<uintptr_t>(m.v[k]) & 15) return false;
   return true;
-}
-
-static inline uint32_t next_epoch(Workspace& ws) {
-  ws.epoch++;
-  if (ws.epoch == 0) {  // wrapped: clear stale tags once
-    cudaMemset(ws.slots, 0, (size_t)ws.cap_n * 8);
-    ws.epoch = 1;
-  }
-  return ws.epoch;
 }
 
 static inline void rec(StageEvents* evs, int k, cudaStream_t st) {
@@ -615,6 +505,19 @@ cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStre
   return e;
 }
 
+template <typename K, bool PARENTS>
+static void launch_emit(Workspace& ws, int fb, uint32_t n, const uint32_t* epoch, cudaStream_t st) {
+  const K* keys = reinterpret_cast<const K*>(ws.keys[fb]);
+  k_delta<K, false><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], nullptr, ws.delta, n);
+  k_emit<SegSingle, PARENTS><<<div_up(n, 256), 256, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, ws.slots,
+                                                             epoch, n, SegSingle{n}, nullptr);
+}
+
+cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
+                         int* final_buf) {
+  return run_sort<unsigned long long>(ws, n, passes, st, L, final_buf);
+}
+
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,
                        StageEvents* evs, uint32_t** out_indices) {
   cudaError_t e = workspace_reserve(ws, n);
@@ -622,27 +525,19 @@ cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, i
   ScratchLayout L = scratch_layout(ws.cap_n);
   rec(evs, 0, st);
   int fb = 0;
-  const uint32_t epoch = next_epoch(ws);
+  const uint32_t* epoch = ws.scratch + L.epoch;
   const bool parents = treelet_rounds > 0;
   if (bits == 30) {
     e = lbvh_prefix<30, uint32_t>(ws, m, n, st, evs, L, &fb);
     if (e != cudaSuccess) return e;
-    if (parents)
-      k_emit<uint32_t, true><<<div_up(n, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(ws.keys[fb]), ws.vals[fb],
-                                                              ws.boxes, ws.nodes, ws.slots, epoch, n);
-    else
-      k_emit<uint32_t, false><<<div_up(n, 256), 256, 0, st>>>(reinterpret_cast<uint32_t*>(ws.keys[fb]), ws.vals[fb],
-                                                               ws.boxes, ws.nodes, ws.slots, epoch, n);
+    if (parents) launch_emit<uint32_t, true>(ws, fb, n, epoch, st);
+    else launch_emit<uint32_t, false>(ws, fb, n, epoch, st);
   } else {
     if (bits == 60) e = lbvh_prefix<60, unsigned long long>(ws, m, n, st, evs, L, &fb);
     else e = lbvh_prefix<63, unsigned long long>(ws, m, n, st, evs, L, &fb);
     if (e != cudaSuccess) return e;
-    if (parents)
-      k_emit<unsigned long long, true><<<div_up(n, 256), 256, 0, st>>>(
-          reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb], ws.boxes, ws.nodes, ws.slots, epoch, n);
-    else
-      k_emit<unsigned long long, false><<<div_up(n, 256), 256, 0, st>>>(
-          reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb], ws.boxes, ws.nodes, ws.slots, epoch, n);
+    if (parents) launch_emit<unsigned long long, true>(ws, fb, n, epoch, st);
+    else launch_emit<unsigned long long, false>(ws, fb, n, epoch, st);
   }
   rec(evs, 4, st);
   if (treelet_rounds > 0 && n >= 2) {

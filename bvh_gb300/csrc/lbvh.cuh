@@ -21,8 +21,8 @@ struct Workspace {
   Node* nodes = nullptr;     // 2n-1 output nodes
   unsigned long long* slots = nullptr;  // n-1 rendezvous words (epoch << 32 | endpoint)
   uint32_t* scratch = nullptr;          // histograms, look-back descriptors, counters
+  uint8_t* delta = nullptr;             // n-1 adjacent common-prefix lengths (+1)
   size_t scratch_words = 0;
-  uint32_t epoch = 0;        // per-build tag for `slots`
   // PLOC buffers
   Box* cbox[2] = {nullptr, nullptr};
   int32_t* cid[2] = {nullptr, nullptr};
@@ -31,12 +31,24 @@ struct Workspace {
   // device-side mesh copy for host-pointer builds
   float* mesh_dev = nullptr;
   uint32_t mesh_cap = 0;
+  // batched builds
+  uint32_t* bat_offsets = nullptr;    // device: count + 1 offsets, then the work items
+  uint32_t* bat_offsets_h = nullptr;  // pinned staging of the same
+  uint32_t bat_items = 0;             // work items in the staged layout
+  size_t bat_words_cap = 0;
+  float* bat_mbox = nullptr;          // device, count * 8
+  uint32_t* bat_indices = nullptr;    // device, n (mesh-local original indices)
+  uint32_t bat_count_cap = 0, bat_n_cap = 0;
 };
+
+// First epoch value; every build adds kEpochStride (emission uses E, treelet round r uses E+1+r).
+constexpr uint32_t kEpochStride = 64;
 
 // Scratch layout (32-bit words, offsets from Workspace::scratch).
 struct ScratchLayout {
   size_t status;     // 1 word, device status bits
   size_t ticket;     // 1 word, bounds-reduction arrival counter (self-resetting)
+  size_t epoch;      // 1 word, rendezvous tag of the current build (bumped by 64 per build)
   size_t scene;      // 8 words, SceneParams
   size_t counters;   // 16 words, per-pass tile counters
   size_t hist;       // passes * 256
@@ -77,12 +89,30 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
 cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
                           uint32_t** sorted_idx);
 
+// Kernel attributes (dynamic shared memory limits), set once per device before any capture.
+cudaError_t prepare_kernels();
+
 // Grow `ws` to hold n triangles (cudaMalloc; synchronising).
 cudaError_t workspace_reserve(Workspace& ws, uint32_t n);
 cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n);
 void workspace_free(Workspace& ws);
 
-// Treelet restructuring passes (LBVH+) after the first (fused) one.
+// Treelet restructuring passes (LBVH+) after emission.
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st);
+
+// Stable sort of ws.keys[0] (64-bit) with implicit indices over `passes` 8-bit digits.
+cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
+                         int* final_buf);
+
+// A slice of one mesh handled by one block of the batched per-mesh kernels.
+struct SegItem {
+  uint32_t mesh, begin, end, pad;
+};
+constexpr uint32_t kSegChunk = 16384;
+
+// Batched LBVH-30 over `count` meshes concatenated in one SoA (offsets and work items on the device).
+cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets, uint32_t count,
+                          const SegItem* d_items, uint32_t n_items, float* d_mbox, uint32_t* d_indices,
+                          cudaStream_t st, StageEvents* evs);
 
 }  // namespace bvhgb

@@ -155,26 +155,12 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_merge(const Box* __restri
   if (threadIdx.x == 0) {
     unsigned long long pre = 0;
     if (tile == 0) {
-      atomicExch(desc, kPFlagInc | tile_total);
+      st_relaxed(desc, kPFlagInc | tile_total);
     } else {
-      atomicExch(desc + tile, kPFlagAgg | tile_total);
-      int64_t j = (int64_t)tile - 1;
-      uint32_t spins = 0;
-      while (j >= 0) {
-        unsigned long long v = atomicAdd(desc + j, 0ull);
-        unsigned long long fl = v & ~kPValMask;
-        if (fl == 0) {
-          if (++spins > kSpinLimit) {
-            atomicOr(status, kStatusSortTimeout);
-            break;
-          }
-          continue;
-        }
-        pre += v & kPValMask;
-        if (fl == kPFlagInc) break;
-        --j;
-      }
-      atomicExch(desc + tile, kPFlagInc | (pre + tile_total));
+      st_relaxed(desc + tile, kPFlagAgg | tile_total);
+      pre = lookback<16, unsigned long long>(desc, 1, (int64_t)tile, ~kPValMask, kPFlagInc, status,
+                                             kStatusSortTimeout);
+      st_relaxed(desc + tile, kPFlagInc | (pre + tile_total));
     }
     s_prefix = pre;
     if (tile == tiles - 1) {
@@ -285,7 +271,9 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   int cur = 0;
   uint32_t* h_ctrl = nullptr;
   if ((e = cudaMallocHost(&h_ctrl, 8)) != cudaSuccess) return e;
-  const int cap_iter = max_iter > 0 ? max_iter : 4 * 32 + 64;
+  // every iteration that makes progress removes at least one cluster, so n bounds the loop;
+  // an iteration that merges nothing stops it at once (no_progress)
+  const int64_t cap_iter = max_iter > 0 ? max_iter : (int64_t)n;
   const size_t nn_smem = 6 * sizeof(float) * (kPlocThreads + 2 * (size_t)radius);
   if (nn_smem > 48 * 1024) {
     if ((e = cudaFuncSetAttribute(k_ploc_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem)) != cudaSuccess) {

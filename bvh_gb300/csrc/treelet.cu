@@ -12,6 +12,7 @@
 //
 // The DP is warp-cooperative: every warp keeps looping while any lane still climbs; lanes that
 // reached a node needing work are served one at a time by all 32 lanes.
+#include "emit.cuh"
 #include "lbvh.cuh"
 
 namespace bvhgb {
@@ -208,13 +209,13 @@ __device__ void treelet_warp(Node* nodes, int32_t root, TreeletSmem& S) {
 // One refit+optimise pass (kRefitAndOptimize(true)).  Warp-synchronous climb: lanes never
 // leave the loop early so that all 32 can serve each lane's treelet.
 __global__ void __launch_bounds__(128) k_treelet_round(Node* __restrict__ nodes, unsigned long long* __restrict__ slots,
-                                                       uint32_t epoch, uint32_t n) {
+                                                       const uint32_t* epoch_word, uint32_t round, uint32_t n) {
   __shared__ TreeletSmem S[4];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool active = i < n;
   int32_t idx = (int32_t)(n - 1 + i);
-  const unsigned long long tag = (unsigned long long)epoch << 32;
+  const unsigned long long tag = (unsigned long long)(__ldcg(epoch_word) + 1u + round) << 32;
   while (__any_sync(0xffffffffu, active)) {
     bool work = false;
     if (active) {
@@ -250,14 +251,9 @@ __global__ void __launch_bounds__(128) k_treelet_round(Node* __restrict__ nodes,
 }
 
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st) {
-  for (int r = 0; r < rounds; ++r) {
-    ws.epoch++;
-    if (ws.epoch == 0) {
-      cudaMemsetAsync(ws.slots, 0, (size_t)ws.cap_n * 8, st);
-      ws.epoch = 1;
-    }
-    k_treelet_round<<<div_up(n, 128), 128, 0, st>>>(ws.nodes, ws.slots, ws.epoch, n);
-  }
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  for (int r = 0; r < rounds && r + 1 < (int)kEpochStride; ++r)
+    k_treelet_round<<<div_up(n, 128), 128, 0, st>>>(ws.nodes, ws.slots, ws.scratch + L.epoch, (uint32_t)r, n);
   return cudaGetLastError();
 }
 

@@ -150,6 +150,31 @@ def batch_meshes(counts, seed: int = 5):
     return out
 
 
+def batch(counts, seed: int = 5):
+    """All meshes of a batch concatenated: (TriangleMesh, offsets[count+1]).  Mesh k is a
+    uniform_small-style mesh (centroids ~ U[0,1]^3, vertex offsets ~ U[-0.005,0.005]^3) scaled
+    by s_k ~ logU[0.1, 10] and moved by o_k ~ U[-10, 10]^3."""
+    counts = np.asarray(counts, np.int64)
+    g = _rng(seed)
+    total = int(counts.sum())
+    offsets = np.zeros(counts.shape[0] + 1, np.int64)
+    np.cumsum(counts, out=offsets[1:])
+    scale = np.exp(g.uniform(np.log(0.1), np.log(10.0), counts.shape[0])).astype(np.float32)
+    off = g.uniform(-10, 10, (counts.shape[0], 3)).astype(np.float32)
+    mesh_id = np.repeat(np.arange(counts.shape[0]), counts)
+    s = scale[mesh_id][:, None]
+    o = off[mesh_id]
+    c = g.random((total, 3), dtype=np.float32)
+    arrs = []
+    for _ in range(3):
+        v = c + (g.random((total, 3), dtype=np.float32) - np.float32(0.5)) * np.float32(0.01)
+        v *= s
+        v += o
+        arrs.append(v)
+    del c, s, o, mesh_id
+    return TriangleMesh.from_vertices(*arrs), offsets.astype(np.uint32)
+
+
 def scene_box(mesh: TriangleMesh):
     lo = np.array([min(mesh.v0x.min(), mesh.v1x.min(), mesh.v2x.min()),
                    min(mesh.v0y.min(), mesh.v1y.min(), mesh.v2y.min()),

@@ -75,7 +75,7 @@ typedef struct bvh_params {
   int32_t morton_bits;    /* LBVH: 30 (reference LBVH), 60 (reference LBVH+ keys) or 63; PLOC: 30 */
   int32_t treelet_rounds; /* LBVH+: refit+restructure passes (the reference runs 1) */
   int32_t ploc_radius;    /* PLOC search radius r (reference default 25) */
-  int32_t max_iterations; /* PLOC iteration cap, 0 = 192 */
+  int32_t max_iterations; /* PLOC iteration cap, 0 = n (an iteration that merges nothing always stops) */
   int32_t reserved[3];
 } bvh_params;
 
@@ -123,6 +123,19 @@ typedef struct bvh_camera {
   float fov_y_deg;
 } bvh_camera;
 
+/* Many independent meshes concatenated in one SoA (device pointers, mesh.n = total
+ * triangles).  offsets is a HOST array of count+1 entries: mesh m owns triangles
+ * [offsets[m], offsets[m+1]), offsets[0] = 0, offsets[count] = mesh.n, every mesh non-empty. */
+typedef struct bvh_batch {
+  bvh_mesh_soa mesh;
+  const uint32_t* offsets;
+  uint32_t count;
+} bvh_batch;
+
+/* bvh_params.reserved[0] for bvh_build_batched: 1 = capture the launch sequence into a CUDA
+ * graph on first use and replay it while the batch layout (pointers, offsets) is unchanged. */
+#define BVH_BATCH_USE_GRAPH 1
+
 typedef struct bvh_ctx bvh_ctx;
 
 const char* bvh_status_string(bvh_status s);
@@ -158,6 +171,14 @@ bvh_status bvh_tree_download(bvh_ctx* ctx, const bvh_tree* tree, void* stream, b
 bvh_status bvh_last_timing(bvh_ctx* ctx, bvh_timing* out);
 /* Wait for the last build and report device-side errors (bounded waits that gave up). */
 bvh_status bvh_sync(bvh_ctx* ctx);
+
+/* Build every mesh of a batch (LBVH, 30-bit Morton).  Result: 2*mesh.n - count nodes; mesh m's
+ * tree occupies nodes [2*offsets[m] - m, 2*offsets[m+1] - m - 1) with its root first and child
+ * indices relative to that first node, and indices [offsets[m], offsets[m+1]) hold mesh-local
+ * original triangle indices -- each mesh's part equals bvh_build_device of that mesh alone.
+ * Asynchronous on `stream`. */
+bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_params* params, void* stream,
+                             bvh_tree* out);
 
 /* Closest-hit traversal of explicit rays (device pointers).  Asynchronous. */
 bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,

@@ -1,0 +1,53 @@
+// Builds meshes through the C++ BVHBuilder adapters and prints node checksums (test program).
+// Compiled either against the reference's headers (drop-in check) or standalone.
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#ifndef BVH_GB300_STANDALONE
+#include "evaluator.h"
+#endif
+#include "bvh_gb300_builder.hpp"
+
+int main(int argc, char** argv) {
+  const size_t n = argc > 1 ? (size_t)atol(argv[1]) : 10000;
+  TriangleMesh mesh;
+  mesh.resize(n);
+  std::mt19937 g(1234);
+  std::uniform_real_distribution<float> u(0.0f, 1.0f);
+  for (size_t i = 0; i < n; ++i) {
+    float x = u(g), y = u(g), z = u(g);
+    mesh.v0x[i] = x; mesh.v0y[i] = y; mesh.v0z[i] = z;
+    mesh.v1x[i] = x + 0.004f; mesh.v1y[i] = y; mesh.v1z[i] = z;
+    mesh.v2x[i] = x; mesh.v2y[i] = y + 0.004f; mesh.v2z[i] = z + 0.002f;
+  }
+  Gb300LBVHBuilder lbvh;
+  Gb300LBVHPlusBuilder plus;
+  Gb300PLOCBuilder ploc(25);
+  BVHBuilder* builders[] = {&lbvh, &plus, &ploc};
+  for (BVHBuilder* b : builders) {
+    try {
+#ifndef BVH_GB300_STANDALONE
+      BVHStats st = BVHEvaluator::evaluate(b, mesh);  // the reference's own evaluator, unchanged
+      printf("%s nodes=%d leaves=%d sah=%.6f depth=%d\n", b->getName().c_str(), st.nodeCount, st.leafCount,
+             st.sahCost, st.maxDepth);
+#else
+      b->build(mesh);
+      const auto& nodes = b->getNodes();
+      unsigned long long h = 1469598103934665603ull;
+      for (const BVHNode& nd : nodes) {
+        unsigned char buf[40];
+        memcpy(buf, &nd.bbox.min, 12); memcpy(buf + 12, &nd.bbox.max, 12);
+        memcpy(buf + 24, &nd.leftChild, 4); memcpy(buf + 28, &nd.rightChild, 4);
+        memset(buf + 32, 0, 8);
+        for (int k = 0; k < 32; ++k) h = (h ^ buf[k]) * 1099511628211ull;
+      }
+      printf("%s nodes=%zu hash=%016llx ms=%.3f\n", b->getName().c_str(), nodes.size(), h, b->getLastBuildTimeMS());
+#endif
+    } catch (const std::exception& e) {
+      printf("%s error: %s\n", b->getName().c_str(), e.what());
+      return 1;
+    }
+  }
+  return 0;
+}
