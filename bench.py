@@ -180,6 +180,7 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     s = stream.cuda_stream
     ctx.reserve(n, algo_id)
+    tuning = None if args.no_autotune else ctx.autotune(n, s)
 
     # --- device-resident build throughput -------------------------------------------------
     with torch.cuda.stream(stream):
@@ -278,6 +279,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": args.steps * (2 + passes + 1 + (1 if algo == "lbvh_plus" else 0)) if algo != "ploc" else None,
         "clocks": clk.summary(),
+        "autotune": tuning,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, mesh)
@@ -307,6 +309,7 @@ def run_batched(args):
     count = offsets.shape[0] - 1
     ctx = bvh_gb300.Context(local)
     params = ctx.params(C.ALGO_LBVH)
+    tuning = None if args.no_autotune else ctx.autotune(min(n, 1 << 26))
     d_in = [torch.from_numpy(a).to(dev) for a in mesh.arrays()]
     ptrs = [t.data_ptr() for t in d_in]
     stream = torch.cuda.Stream(device=dev)
@@ -333,6 +336,7 @@ def run_batched(args):
         # plain per-mesh loop of single-mesh builds on the same device-resident data
         single = bvh_gb300.Context(local)
         single.reserve(int(counts.max()))
+        single.set_tuning(*ctx.tuning())
         loop_reps = 2
         for _ in range(1):
             for m in range(count):
@@ -395,6 +399,7 @@ def run_batched(args):
                 "d2h_bytes_per_step": 48 * n_nodes + 4 * n, "ms_per_step": round(e2e_ms, 3)},
         "gpu_launches": args.steps * 13,
         "clocks": clk.summary(),
+        "autotune": tuning,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -470,6 +475,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c1_lbvh63")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default sort variants")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -127,6 +127,21 @@ class Context:
         self._batch_keep = offsets
         return t
 
+    def autotune(self, n: int, stream: int = 0) -> dict:
+        """Time every radix-sort variant on n keys, keep the fastest (bvh_autotune); returns the table."""
+        import json
+        buf = ctypes.create_string_buffer(8192)
+        C.check(self.lib.bvh_autotune(self.handle, n, ctypes.c_void_p(stream), buf, len(buf)), "bvh_autotune")
+        return json.loads(buf.value.decode())
+
+    def tuning(self):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        C.check(self.lib.bvh_tuning_get(self.handle, ctypes.byref(a), ctypes.byref(b)), "bvh_tuning_get")
+        return a.value, b.value
+
+    def set_tuning(self, v32: int, v64: int):
+        C.check(self.lib.bvh_tuning_set(self.handle, v32, v64), "bvh_tuning_set")
+
     def build_host(self, mesh: TriangleMesh, params: C.Params, stream: int = 0):
         """Upload, build, download (BVHBuilder::build).  Returns (nodes, indices)."""
         n = mesh.size()

@@ -149,7 +149,7 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   int mbits = 1;
   while (mbits < 34 && (1ull << mbits) < count) ++mbits;
   const int passes = (30 + mbits + 7) / 8;
-  L.zero_end = L.desc + (size_t)passes * div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_tile(8)) * 256;
+  L.zero_end = L.desc + (size_t)passes * div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_variant_tile(8, ws.sort_variant[1])) * 256;
   if (evs && evs->use) cudaEventRecord(evs->ev[0], st);
   k_seg_init<<<152 * 4, 256, 0, st>>>(d_mbox, count, ws.scratch, L);
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(n_items, 152 * 8));

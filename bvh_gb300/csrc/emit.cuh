@@ -6,7 +6,8 @@
 // Step 1 (k_delta): D[k] = delta(k, k+1) + 1 for adjacent sorted positions, one byte each
 // (delta_nt, lbvh_builder.cu:33-43: common-prefix length of the codes, or 32/64 +
 // clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0 marks a segment boundary).
-// Step 2 (k_emit): one thread per sorted position climbs.  A node with range [f, l] has its
+// Step 2 (k_emit): one thread per sorted position climbs; merges whose two children belong to
+// threads of one block happen in shared memory, the rest through global rendezvous words.  A node with range [f, l] has its
 // parent's split on the side whose adjacent delta is larger (Apetrei 2014): gamma = l when
 // D[l] > D[f-1], else gamma = f-1.  The second child to reach gamma's rendezvous word completes
 // the parent.  Karras ids: leaf i -> n-1+i, a left child's id is its last index, a right
@@ -112,9 +113,16 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
                                               const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
                                               unsigned long long* __restrict__ slots, const uint32_t* epoch_word,
                                               uint32_t n, Seg seg, uint32_t* __restrict__ out_idx) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t wbase = i - lane;  // sorted position of lane 0
+  constexpr uint32_t T = 256;
+  // per-position state published for the block-local pairing rounds
+  __shared__ uint32_t s_gamma[T], s_l[T];
+  __shared__ int32_t s_my[T];
+  __shared__ uint8_t s_state[T];  // bit0 active, bit1 is_left
+  __shared__ uint8_t s_claim[T];
+  __shared__ float s_box[6][T];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t i = blockIdx.x * T + tid;
+  const uint32_t bbase = blockIdx.x * T;  // sorted position of thread 0
   bool active = i < n;
   uint32_t off = 0, cnt = 1, nb = 0;
   Climb c;
@@ -135,9 +143,10 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
     store_node(nodes, nb + (uint32_t)c.my, c.box, (int32_t)(prim | kLeafBit), -1, -1);
     if (cnt == 1) active = false;
   }
-  // ---- phase 1: merges whose two children are owned by lanes of this warp (no atomics) ----
-  // The lane of a node's first position owns it; a left child at split gamma finds its right
-  // sibling at lane gamma + 1 - wbase.
+  s_claim[tid] = 0;
+  // ---- phase 1: merges whose two children are owned by threads of this block (no atomics) ----
+  // The thread of a node's first position owns it; a left child at split gamma finds its right
+  // sibling at thread gamma + 1 - bbase.
   bool is_left = false;
   uint32_t gamma = 0;
   while (true) {
@@ -156,37 +165,39 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
           write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
           c.internal = false;  // written; `my` now names it
         }
-        want = is_left && gamma + 1 >= wbase && gamma + 1 < wbase + 32;
+        want = is_left && gamma + 1 >= bbase && gamma + 1 < bbase + T;
       }
     }
-    const uint32_t p = want ? gamma + 1 - wbase : lane;
-    const bool p_active = __shfl_sync(0xffffffffu, active, p);
-    const bool p_left = __shfl_sync(0xffffffffu, is_left, p);
-    const uint32_t p_gamma = __shfl_sync(0xffffffffu, gamma, p);
-    const uint32_t p_l = __shfl_sync(0xffffffffu, c.l, p);
-    const int32_t p_my = __shfl_sync(0xffffffffu, c.my, p);
-    Box pb;
-    pb.lo.x = __shfl_sync(0xffffffffu, c.box.lo.x, p);
-    pb.lo.y = __shfl_sync(0xffffffffu, c.box.lo.y, p);
-    pb.lo.z = __shfl_sync(0xffffffffu, c.box.lo.z, p);
-    pb.hi.x = __shfl_sync(0xffffffffu, c.box.hi.x, p);
-    pb.hi.y = __shfl_sync(0xffffffffu, c.box.hi.y, p);
-    pb.hi.z = __shfl_sync(0xffffffffu, c.box.hi.z, p);
-    pb.lo.w = pb.hi.w = 0.f;
-    const bool paired = want && p_active && !p_left && p_gamma == gamma;
-    // a right lane is consumed when a left lane paired with it: the two share the match key
-    const uint32_t key = paired ? p : lane;
-    const uint32_t peers = __match_any_sync(0xffffffffu, key);
-    const bool consumed = !paired && __popc(peers) > 1;
-    if (paired) {
-      c.lc = c.my;
-      c.rc = p_my;
-      c.l = p_l;
-      c.box = box_union(c.box, pb);
-      c.internal = true;
+    s_state[tid] = (active ? 1 : 0) | (is_left ? 2 : 0);
+    s_gamma[tid] = gamma;
+    s_l[tid] = c.l;
+    s_my[tid] = c.my;
+    s_box[0][tid] = c.box.lo.x; s_box[1][tid] = c.box.lo.y; s_box[2][tid] = c.box.lo.z;
+    s_box[3][tid] = c.box.hi.x; s_box[4][tid] = c.box.hi.y; s_box[5][tid] = c.box.hi.z;
+    __syncthreads();
+    bool paired = false;
+    if (want) {
+      const uint32_t p = gamma + 1 - bbase;
+      if (s_state[p] == 1 && s_gamma[p] == gamma) {  // active right child of the same parent
+        paired = true;
+        Box pb;
+        pb.lo = make_float4(s_box[0][p], s_box[1][p], s_box[2][p], 0.f);
+        pb.hi = make_float4(s_box[3][p], s_box[4][p], s_box[5][p], 0.f);
+        c.lc = c.my;
+        c.rc = s_my[p];
+        c.l = s_l[p];
+        c.box = box_union(c.box, pb);
+        c.internal = true;
+        s_claim[p] = 1;
+      }
     }
-    if (consumed) active = false;
-    if (!__any_sync(0xffffffffu, paired)) break;
+    const int any = __syncthreads_or(paired ? 1 : 0);
+    if (s_claim[tid]) {
+      active = false;
+      s_claim[tid] = 0;
+    }
+    if (!any) break;
+    __syncthreads();  // state arrays are rewritten next round
   }
   if (!active) return;
   // ---- phase 2: the remaining nodes meet their siblings through the rendezvous words ----

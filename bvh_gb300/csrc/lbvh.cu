@@ -25,7 +25,7 @@ namespace bvhgb {
 // ---------------------------------------------------------------------------------------
 // scratch
 // ---------------------------------------------------------------------------------------
-int sort_tile(int key_bytes) { return kSortThreads * (key_bytes == 4 ? kSortIpt32 : kSortIpt64); }
+int sort_tile(int key_bytes) { return kSortThreads * (key_bytes == 4 ? 8 : 6); }  // smallest variant tile
 
 ScratchLayout scratch_layout(uint32_t n) {
   ScratchLayout L;
@@ -283,8 +283,8 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan_u64(unsigned 
   return before + x - v;
 }
 
-template <typename K, int THREADS, int IPT>
-__global__ void __launch_bounds__(THREADS) k_onesweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+template <typename K, int THREADS, int IPT, int W, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                       K* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                                       int pass, uint32_t* __restrict__ scratch, ScratchLayout L,
                                                       uint32_t tiles) {
@@ -351,20 +351,11 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(const K* __restrict__ kin,
   unsigned long long ex = block_exclusive_scan_u64<THREADS>(packed, s_scan);
   s_binstart[b] = (uint32_t)ex;                 // tile-local start of bin b
   const uint32_t binbase = (uint32_t)(ex >> 32);  // global start of bin b
-  // decoupled look-back on bin b
+  // publish this tile's count first so that successors can proceed
   uint32_t* desc = scratch + L.desc + ((size_t)pass * tiles) * BINS;
-  uint32_t excl = 0;
-  if (tile == 0) {
-    st_relaxed(desc + b, kFlagInc | cnt);
-  } else {
-    st_relaxed(desc + (size_t)tile * BINS + b, kFlagAgg | cnt);
-    excl = lookback<16, uint32_t>(desc + b, BINS, (int64_t)tile, ~kValMask, kFlagInc, scratch + L.status,
-                                  kStatusSortTimeout);
-    st_relaxed(desc + (size_t)tile * BINS + b, kFlagInc | (excl + cnt));
-  }
-  s_gstart[b] = binbase + excl;
-  __syncthreads();
-  // local scatter into tile order
+  st_relaxed(desc + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | cnt);
+  __syncthreads();  // s_binstart complete
+  // local scatter into tile order (independent of the global offsets); frees the key registers
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
     uint32_t idx = wbase + (uint32_t)k * 32u + lane;
@@ -375,6 +366,14 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(const K* __restrict__ kin,
       s_vals[pos] = val[k];
     }
   }
+  // decoupled look-back on bin b, 32 predecessors per round
+  uint32_t excl = 0;
+  if (tile != 0) {
+    excl = lookback<W, uint32_t>(desc + b, BINS, (int64_t)tile, ~kValMask, kFlagInc, scratch + L.status,
+                                 kStatusSortTimeout);
+    st_relaxed(desc + (size_t)tile * BINS + b, kFlagInc | (excl + cnt));
+  }
+  s_gstart[b] = binbase + excl;
   __syncthreads();
   const uint32_t len = min((uint32_t)TILE, n - base);
   for (uint32_t i = tid; i < len; i += THREADS) {
@@ -388,45 +387,153 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(const K* __restrict__ kin,
   }
 }
 
-template <typename K>
-size_t onesweep_smem() {
-  constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
-  constexpr int TILE = kSortThreads * IPT;
-  return (size_t)TILE * sizeof(K) + (size_t)TILE * 4 + (size_t)(kSortThreads / 32) * 256 * 4 + 2 * 256 * 4 +
-         32 * 8 + 16;
+// Onesweep variants (items per thread, look-back window, minimum blocks per SM); the autotuner
+// (bvh_autotune) times them and each context keeps the fastest per key width.
+struct SortVariant {
+  const void* fn;
+  int ipt, window, minb;
+  size_t smem;
+};
+
+template <typename K, int IPT, int W, int MINB>
+constexpr SortVariant make_variant() {
+  return SortVariant{reinterpret_cast<const void*>(&k_onesweep<K, kSortThreads, IPT, W, MINB>), IPT, W, MINB,
+                     (size_t)kSortThreads * IPT * sizeof(K) + (size_t)kSortThreads * IPT * 4 +
+                         (size_t)(kSortThreads / 32) * 256 * 4 + 2 * 256 * 4 + 32 * 8 + 16};
 }
 
-template <typename K>
-cudaError_t set_sort_attributes() {
-  constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
-  return cudaFuncSetAttribute(k_onesweep<K, kSortThreads, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)onesweep_smem<K>());
+static const SortVariant kVariants32[] = {
+    make_variant<uint32_t, 16, 32, 2>(), make_variant<uint32_t, 16, 16, 3>(), make_variant<uint32_t, 12, 32, 3>(),
+    make_variant<uint32_t, 8, 32, 4>(),
+};
+static const SortVariant kVariants64[] = {
+    make_variant<unsigned long long, 12, 32, 2>(), make_variant<unsigned long long, 12, 16, 3>(),
+    make_variant<unsigned long long, 8, 32, 3>(), make_variant<unsigned long long, 6, 32, 4>(),
+};
+constexpr int kNumVariants = 4;
+
+static const SortVariant& variant(int key_bytes, int v) {
+  v = v < 0 || v >= kNumVariants ? 0 : v;
+  return key_bytes == 4 ? kVariants32[v] : kVariants64[v];
+}
+
+int sort_variant_count() { return kNumVariants; }
+int sort_variant_tile(int key_bytes, int v) { return kSortThreads * variant(key_bytes, v).ipt; }
+void sort_variant_describe(int key_bytes, int v, int* ipt, int* window, int* minb) {
+  const SortVariant& sv = variant(key_bytes, v);
+  *ipt = sv.ipt;
+  *window = sv.window;
+  *minb = sv.minb;
 }
 
 // Kernel attributes set once per device, outside any stream capture.
 cudaError_t prepare_kernels() {
-  cudaError_t e = set_sort_attributes<uint32_t>();
-  if (e == cudaSuccess) e = set_sort_attributes<unsigned long long>();
-  return e;
+  for (int v = 0; v < kNumVariants; ++v) {
+    for (int kb : {4, 8}) {
+      const SortVariant& sv = variant(kb, v);
+      cudaError_t e = cudaFuncSetAttribute(sv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv.smem);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
 }
 
 template <typename K>
 cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L, int* final_buf) {
-  constexpr int IPT = sizeof(K) == 4 ? kSortIpt32 : kSortIpt64;
-  constexpr int TILE = kSortThreads * IPT;
-  const uint32_t tiles = div_up(n, TILE);
-  const size_t smem = onesweep_smem<K>();
-  auto kern = k_onesweep<K, kSortThreads, IPT>;
+  const SortVariant& sv = variant((int)sizeof(K), ws.sort_variant[sizeof(K) == 4 ? 0 : 1]);
+  const uint32_t tile = (uint32_t)kSortThreads * sv.ipt;
+  uint32_t tiles = div_up(n, tile);
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
     const K* kin = reinterpret_cast<const K*>(ws.keys[cur]);
     const uint32_t* vin = p == 0 ? nullptr : ws.vals[cur];
-    kern<<<tiles, kSortThreads, smem, st>>>(kin, vin, reinterpret_cast<K*>(ws.keys[cur ^ 1]), ws.vals[cur ^ 1], n, p,
-                                            ws.scratch, L, tiles);
+    K* kout = reinterpret_cast<K*>(ws.keys[cur ^ 1]);
+    uint32_t* vout = ws.vals[cur ^ 1];
+    uint32_t* scratch = ws.scratch;
+    ScratchLayout Lc = L;
+    void* args[] = {(void*)&kin, (void*)&vin, (void*)&kout, (void*)&vout, (void*)&n, (void*)&p, (void*)&scratch,
+                    (void*)&Lc, (void*)&tiles};
+    cudaError_t e = cudaLaunchKernel(sv.fn, dim3(tiles), dim3(kSortThreads), args, sv.smem, st);
+    if (e != cudaSuccess) return e;
     cur ^= 1;
   }
   *final_buf = cur;
-  return cudaGetLastError();
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------------------
+// autotuning of the sort
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Pseudo-random keys (63 or 30 bits) with the radix histograms of every pass.
+template <typename K>
+__global__ void __launch_bounds__(256) k_tune_keys(K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
+  constexpr int P = (int)sizeof(K);
+  __shared__ uint32_t s_hist[P][256];
+  for (int k = threadIdx.x; k < P * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long z = mix64(i);
+    const K k = sizeof(K) == 4 ? (K)(z >> 34) : (K)(z >> 1);
+    keys[i] = k;
+#pragma unroll
+    for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p][(uint32_t)(k >> (8 * p)) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < P * 256; k += blockDim.x)
+    if ((&s_hist[0][0])[k]) atomicAdd(hist + k, (&s_hist[0][0])[k]);
+}
+
+template <typename K>
+static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const ScratchLayout& L, float* ms) {
+  const int kb = (int)sizeof(K);
+  cudaError_t e = cudaMemsetAsync(ws.scratch + L.zero_begin, 0, (L.zero_end - L.zero_begin) * 4, st);
+  if (e != cudaSuccess) return e;
+  k_tune_keys<K><<<152 * 8, 256, 0, st>>>(reinterpret_cast<K*>(ws.keys[0]), n, ws.scratch + L.hist);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = 0;
+  for (int v = 0; v < kNumVariants; ++v) {
+    ws.sort_variant[kb == 4 ? 0 : 1] = v;
+    float vbest = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      // tile counters and look-back words start at zero; the histograms stay valid (the keys
+      // are a permutation of the same multiset after an even number of passes)
+      cudaMemsetAsync(ws.scratch + L.counters, 0, 16 * 4, st);
+      cudaMemsetAsync(ws.scratch + L.desc, 0, (L.zero_end - L.desc) * 4, st);
+      int fb = 0;
+      cudaEventRecord(e0, st);
+      e = run_sort<K>(ws, n, kb, st, L, &fb);
+      cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) break;
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0 && t < vbest) vbest = t;  // first run warms up
+    }
+    if (e != cudaSuccess) break;
+    ms[v] = vbest;
+    if (vbest < ms[best]) best = v;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ws.sort_variant[kb == 4 ? 0 : 1] = best;
+  return e;
+}
+
+cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out) {
+  cudaError_t e = workspace_reserve(ws, n);
+  if (e != cudaSuccess) return e;
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  if ((e = tune_width<uint32_t>(ws, n, st, L, ms_out)) != cudaSuccess) return e;
+  return tune_width<unsigned long long>(ws, n, st, L, ms_out + kNumVariants);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -484,7 +591,9 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   const int vec4 = all_aligned16(m) ? 1 : 0;
   // zero only the descriptors this build's passes use
   ScratchLayout Lz = L;
-  Lz.zero_end = L.desc + (size_t)sizeof(K) * div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_tile((int)sizeof(K))) * 256;
+  const int kb = (int)sizeof(K);
+  Lz.zero_end = L.desc + (size_t)kb * div_up(std::max<uint32_t>(n, 1),
+                                             (uint32_t)sort_variant_tile(kb, ws.sort_variant[kb == 4 ? 0 : 1])) * 256;
   k_bounds<<<kBoundsBlocks, 256, 0, st>>>(m, n, vec4, ws.scratch, Lz);
   rec(evs, 1, st);
   const uint32_t work = vec4 ? div_up(n, 4) : n;

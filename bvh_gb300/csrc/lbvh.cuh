@@ -15,6 +15,7 @@ struct MeshPtrs {
 // Device workspace owned by a context; grown on demand, reused across builds.
 struct Workspace {
   uint32_t cap_n = 0;        // triangles the buffers can hold
+  int sort_variant[2] = {0, 0};  // onesweep variant for 32-bit / 64-bit keys (bvh_autotune)
   void* keys[2] = {nullptr, nullptr};
   uint32_t* vals[2] = {nullptr, nullptr};
   Box* boxes = nullptr;      // per-triangle AABB in input order
@@ -62,12 +63,15 @@ struct ScratchLayout {
 
 constexpr int kBoundsBlocks = 152 * 4;
 constexpr int kSortThreads = 256;
-constexpr int kSortIpt32 = 16;  // items per thread, 32-bit keys
-constexpr int kSortIpt64 = 12;  // items per thread, 64-bit keys
 constexpr int kMaxPasses = 8;
 
 ScratchLayout scratch_layout(uint32_t n);
-int sort_tile(int key_bytes);
+int sort_tile(int key_bytes);  // smallest tile over all variants (sizes the look-back scratch)
+int sort_variant_count();
+int sort_variant_tile(int key_bytes, int v);
+void sort_variant_describe(int key_bytes, int v, int* ipt, int* window, int* minb);
+// Times every onesweep variant on `n` pseudo-random keys of each width and keeps the fastest in ws.
+cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out /* 2 x variants */);
 
 // Builds stage events: [0] start, [1] bounds, [2] morton, [3] sort, [4] emit, [5] optimise.
 struct StageEvents {

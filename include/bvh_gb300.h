@@ -180,6 +180,14 @@ bvh_status bvh_sync(bvh_ctx* ctx);
 bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_params* params, void* stream,
                              bvh_tree* out);
 
+/* Autotuner (no reference counterpart): times every radix-sort variant (items per thread,
+ * look-back window, blocks per SM) on n pseudo-random keys of each width, keeps the fastest in
+ * the context and writes a JSON table of the timings to json_out (may be NULL).  Synchronous. */
+bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char* json_out, size_t json_cap);
+/* Read or set the sort variants a context uses (index per key width: 32-bit, 64-bit). */
+bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant32, int32_t* variant64);
+bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant32, int32_t variant64);
+
 /* Closest-hit traversal of explicit rays (device pointers).  Asynchronous. */
 bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
                      const bvh_rays* rays, const bvh_hits* hits, void* stream);
