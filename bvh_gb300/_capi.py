@@ -100,6 +100,7 @@ SIGNATURES = {
     "bvh_autotune": (c_int, [c_void_p, c_uint32, c_void_p, c_char_p, ctypes.c_size_t]),
     "bvh_tuning_get": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
     "bvh_tuning_set": (c_int, [c_void_p, c_int32, c_int32]),
+    "bvh_build_lbvh_static": (c_int, [POINTER(MeshSoA), c_int32, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

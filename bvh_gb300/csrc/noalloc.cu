@@ -1,0 +1,97 @@
+// noalloc.cu -- an LBVH build that allocates no memory (bvh_build_lbvh_static).
+//
+// For callers that cannot call cudaMalloc: code that runs inside a host application's
+// real-time or pre-allocated memory budget, plugins whose host forbids device allocations
+// after start-up, and callers that must not take the device-wide synchronisation that
+// cudaMalloc/cudaFree can imply.  Everything except the caller's inputs and outputs lives in
+// one file-scope __device__ array of fixed size, which every GPU that loads this library holds
+// until the process exits.  All calls share that array, so calls that overlap on the GPU (two
+// streams, two threads) race and corrupt each other's results; serialise them.
+#include <mutex>
+
+#include "../../include/bvh_gb300.h"
+#include "lbvh.cuh"
+
+using namespace bvhgb;
+
+namespace {
+
+constexpr uint32_t kStaticMaxTris = 1u << 18;  // 262,144 triangles
+
+// Layout of the static scratch for kStaticMaxTris (bytes, 256-aligned pieces).
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kKeysBytes = align256((size_t)kStaticMaxTris * 8);
+constexpr size_t kValsBytes = align256((size_t)kStaticMaxTris * 4);
+constexpr size_t kBoxBytes = align256((size_t)kStaticMaxTris * sizeof(Box));
+constexpr size_t kSlotBytes = align256((size_t)kStaticMaxTris * 8);
+constexpr size_t kDeltaBytes = align256((size_t)kStaticMaxTris + 16);
+// scratch words: fixed part + look-back descriptors for the smallest sort tile (6 x 256 keys)
+constexpr size_t kDescWords = (size_t)kMaxPasses * ((kStaticMaxTris + 1535) / 1536) * 256;
+constexpr size_t kScratchBytes = align256((8 + 16 + 8 + 16 + (size_t)kBoundsBlocks * 8 + 16 + kMaxPasses * 256 +
+                                           kDescWords + 64) * 4);
+constexpr size_t kStaticBytes = 2 * kKeysBytes + kValsBytes + kBoxBytes + kSlotBytes + kDeltaBytes + kScratchBytes;
+
+__device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mutex;
+unsigned char* g_ptr[kMaxDevices] = {};  // device address of g_static_scratch, per device
+
+// Once per device, with that device current: the array's device address (host code must not
+// use the symbol itself, which is only a host-side stand-in).
+cudaError_t static_scratch(int device, unsigned char** out) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    e = prepare_kernels();  // kernel attributes only; allocates nothing
+    if (e != cudaSuccess) return e;
+    g_ptr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_ptr[device];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t morton_bits, bvh_node* nodes,
+                                            uint32_t* indices, void* stream) {
+  if (!mesh || (morton_bits != 30 && morton_bits != 60 && morton_bits != 63)) return BVH_ERR_INVALID_ARG;
+  const uint32_t n = mesh->n;
+  if (n == 0) return BVH_OK;
+  if (n > kStaticMaxTris || !nodes || !indices) return BVH_ERR_INVALID_ARG;
+  const float* v[9] = {mesh->v0x, mesh->v0y, mesh->v0z, mesh->v1x, mesh->v1y, mesh->v1z,
+                       mesh->v2x, mesh->v2y, mesh->v2z};
+  MeshPtrs m;
+  for (int k = 0; k < 9; ++k) {
+    if (!v[k]) return BVH_ERR_INVALID_ARG;
+    m.v[k] = v[k];
+  }
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return BVH_ERR_DEVICE;
+  unsigned char* base = nullptr;
+  if (static_scratch(device, &base) != cudaSuccess) return BVH_ERR_DEVICE;
+  // A workspace view over the static array and the caller's outputs: the radix sort's last pass
+  // writes the sorted indices into `indices` (an even number of passes ends in buffer 0) and the
+  // emission writes `nodes`.  Slots are epoch-tagged and the per-build scratch is cleared by the
+  // first kernel, so nothing left from the previous call needs clearing here.
+  Workspace ws;
+  size_t o = 0;
+  ws.keys[0] = base + o; o += kKeysBytes;
+  ws.keys[1] = base + o; o += kKeysBytes;
+  ws.vals[0] = indices;
+  ws.vals[1] = reinterpret_cast<uint32_t*>(base + o); o += kValsBytes;
+  ws.boxes = reinterpret_cast<Box*>(base + o); o += kBoxBytes;
+  ws.slots = reinterpret_cast<unsigned long long*>(base + o); o += kSlotBytes;
+  ws.delta = base + o; o += kDeltaBytes;
+  ws.scratch = reinterpret_cast<uint32_t*>(base + o);
+  ws.nodes = reinterpret_cast<Node*>(nodes);
+  ws.cap_n = kStaticMaxTris;
+  ws.scratch_words = kScratchBytes / 4;
+  if (scratch_layout(kStaticMaxTris).total > ws.scratch_words) return BVH_ERR_DEVICE;  // layout guard
+  uint32_t* out_idx = nullptr;
+  cudaError_t e = lbvh_build(ws, m, n, morton_bits, 0, reinterpret_cast<cudaStream_t>(stream), nullptr, &out_idx);
+  if (e != cudaSuccess) return BVH_ERR_DEVICE;
+  return out_idx == indices ? BVH_OK : BVH_ERR_DEVICE;
+}

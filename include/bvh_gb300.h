@@ -188,6 +188,18 @@ bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char* json_out, 
 bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant32, int32_t* variant64);
 bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant32, int32_t variant64);
 
+/* LBVH build that allocates nothing (no counterpart in the reference).  For callers that cannot
+ * call cudaMalloc -- a host that forbids device allocations after start-up, a real-time loop
+ * with a fixed memory budget -- and so cannot create a bvh_ctx.  Inputs (device SoA) and
+ * outputs (device: 2n-1 nodes, n indices) come from the caller; all other scratch is one
+ * fixed __device__ array inside the library (about 17 MB per GPU that loads it, held until
+ * exit), so n may be at most 262,144 (BVH_ERR_INVALID_ARG beyond).  morton_bits: 30, 60 or 63;
+ * the result equals bvh_build_device's.  Asynchronous on `stream`.  The first call on a device
+ * looks up the array's device address; make that first call before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race, so serialise them. */
+bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t morton_bits, bvh_node* nodes, uint32_t* indices,
+                                 void* stream);
+
 /* Closest-hit traversal of explicit rays (device pointers).  Asynchronous. */
 bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
                      const bvh_rays* rays, const bvh_hits* hits, void* stream);
