@@ -41,9 +41,21 @@ WORKLOADS = {
                     "10M clustered triangles, LBVH+ 60-bit, 1 treelet pass"),
     "c1_lbvh63_4m": ("clustered", {"n": 4_000_000, "seed": 1}, "lbvh", 63, 0,
                      "4M clustered triangles (config 1 distribution), LBVH 63-bit; profiling size"),
+    "c2a_ploc25": ("icosphere", {"levels": 8, "seed": 2}, "ploc", 30, 25,
+                   "1,310,720-triangle displaced icosphere (0.05 fBm), PLOC radius 25"),
+    "c2a_lbvhplus": ("icosphere", {"levels": 8, "seed": 2}, "lbvh_plus", 60, 0,
+                     "1,310,720-triangle displaced icosphere (0.05 fBm), LBVH+ 60-bit, 1 treelet pass"),
+    "c2b_ploc25": ("strands", {"n_strands": 20000, "segments": 100, "seed": 3}, "ploc", 30, 25,
+                   "2,000,000 thin triangles on 20,000 random-walk strands, PLOC radius 25"),
+    "c2b_lbvhplus": ("strands", {"n_strands": 20000, "segments": 100, "seed": 3}, "lbvh_plus", 60, 0,
+                     "2,000,000 thin triangles on 20,000 random-walk strands, LBVH+ 60-bit, 1 treelet pass"),
     "c3_batched": ("batch", {"meshes": 4096, "lo": 64, "hi": 262144}, "lbvh_batched", 30, 0,
                    "4,096 meshes, triangle counts logU[64, 262144], each built by LBVH-30 in one batched launch "
                    "sequence replayed as a CUDA graph"),
+    "c4_serve": ("serve", {"rate": 2000.0, "duration_s": 3.0, "lo": 1000, "hi": 2_000_000, "rays": 65536,
+                           "pool": 32, "budget_gb": 40, "slots": 16}, "serve", 30, 0,
+                 "Poisson stream (2,000 req/s) of build+trace requests, meshes logU[1e3, 2e6] triangles, "
+                 "65,536 rays each, 40 GB HBM budget"),
     "c0_lbvh30": ("uniform_small", {"n": 100_000, "seed": 0}, "lbvh", 30, 0,
                   "100k uniform triangles, LBVH 30-bit"),
 }
@@ -406,6 +418,117 @@ def run_batched(args):
     ctx.close()
 
 
+def run_serve(args):
+    """Config 4: continuously batched build+trace serving; p50/p99 latency and aggregate rates."""
+    import threading as th
+
+    import torch
+
+    from bvh_gb300 import meshgen
+    from bvh_gb300.serve import Server
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    g = np.random.default_rng(7 + rank)
+    sizes = np.exp(g.uniform(np.log(kw["lo"]), np.log(kw["hi"]), kw["pool"])).astype(np.int64)
+    pool = []
+    for k, n in enumerate(sizes):
+        if k % 2:
+            m = meshgen.strands(max(1, int(n) // 100), 100, seed=300 + k)
+        else:
+            m = meshgen.clustered(int(n), seed=300 + k)
+        ro, rd = meshgen.sphere_rays(m, kw["rays"], seed=400 + k)
+        mesh_h = [torch.from_numpy(a).pin_memory() for a in m.arrays()]
+        rays_h = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+                  for x in (ro[:, 0], ro[:, 1], ro[:, 2], rd[:, 0], rd[:, 1], rd[:, 2])]
+        pool.append((m.size(), mesh_h, rays_h))
+    nr = kw["rays"]
+    free_hits = [[torch.empty(nr, dtype=torch.float32).pin_memory()] +
+                 [torch.empty(nr, dtype=torch.int32).pin_memory() for _ in range(4)] for _ in range(512)]
+    sv = Server(budget_bytes=kw["budget_gb"] << 30, slots=kw["slots"], morton_bits=30, device=local,
+                max_triangles=int(max(p[0] for p in pool)), max_rays=nr)
+    results = []
+    in_use = {}
+    lock = th.Lock()
+    stop = th.Event()
+
+    def poller():
+        while not stop.is_set() or in_use:
+            for r in sv.poll(256, 5):
+                with lock:
+                    free_hits.append(in_use.pop(r["tag"]))
+                results.append(r)
+
+    pt = th.Thread(target=poller, daemon=True)
+    pt.start()
+
+    def submit(tag, k):
+        while True:
+            with lock:
+                if free_hits:
+                    h = free_hits.pop()
+                    in_use[tag] = h
+                    break
+            time.sleep(0.0001)
+        n, mesh_h, rays_h = pool[k]
+        sv.submit(tag, mesh_h, rays_h, h)
+
+    # warm-up: every pool mesh once
+    for k in range(len(pool)):
+        submit(10_000_000 + k, k)
+    while len(results) < len(pool):
+        time.sleep(0.01)
+    results.clear()
+    n_req = int(kw["rate"] * kw["duration_s"])
+    arrivals = np.cumsum(g.exponential(1.0 / kw["rate"], n_req))
+    picks = g.integers(0, len(pool), n_req)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for tag in range(n_req):
+            delay = t0 + arrivals[tag] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            submit(tag, int(picks[tag]))
+        while len(results) < n_req:
+            time.sleep(0.005)
+        t1 = time.perf_counter()
+    stop.set()
+    pt.join(timeout=10)
+    st = sv.stats()
+    sv.close()
+    lat = np.array([(r["t_done_ns"] - r["t_submit_ns"]) / 1e6 for r in results])
+    queue_ms = np.array([(r["t_admit_ns"] - r["t_submit_ns"]) / 1e6 for r in results])
+    tris = sum(r["triangles"] for r in results)
+    rays = sum(r["rays"] for r in results)
+    span = (max(r["t_done_ns"] for r in results) - min(r["t_submit_ns"] for r in results)) / 1e9
+    ok = all(r["status"] == 0 for r in results)
+    line = {
+        "metric": "serve p50/p99 request latency (ms) + aggregate Mtris/s and Mrays/s",
+        "value": round(float(np.percentile(lat, 50)), 3), "unit": "ms (p50 latency)", "n_gpus": ws,
+        "steps": n_req, "warmup": len(pool), "ms_per_step": round(float(lat.mean()), 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32",
+        "data": "synthetic (seeded pool of clustered/strand meshes, bvh_gb300/meshgen.py)",
+        "config": {"workload": args.workload, "description": desc, "requests": n_req, "rate_per_s": kw["rate"],
+                   "pool_meshes": len(pool), "slots": kw["slots"], "budget_gb": kw["budget_gb"],
+                   "rays_per_request": nr, "offered_mtris_per_s": round(float(np.mean(sizes)) * kw["rate"] / 1e6, 1)},
+        "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p90": round(float(np.percentile(lat, 90)), 3),
+                       "p99": round(float(np.percentile(lat, 99)), 3), "max": round(float(lat.max()), 3),
+                       "queue_p50": round(float(np.percentile(queue_ms, 50)), 3),
+                       "queue_p99": round(float(np.percentile(queue_ms, 99)), 3)},
+        "throughput": {"mtris_per_s": round(tris / span / 1e6, 1), "mrays_per_s": round(rays / span / 1e6, 1),
+                       "requests_per_s": round(n_req / span, 1), "all_ok": ok},
+        "server": {k: int(v) for k, v in st.items()},
+        "e2e": {"value": round(tris / span / 1e6, 1), "unit": "Mtris/s",
+                "h2d_bytes_per_step": int(np.mean([36 * pool[k][0] + 24 * nr for k in picks])),
+                "d2h_bytes_per_step": 20 * nr},
+        "gpu_launches": n_req * 14,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     ws, rank, local = dist_info()
     if rank != 0:
@@ -483,6 +606,8 @@ def main():
         run_reference(args)
     elif WORKLOADS[args.workload][2] == "lbvh_batched":
         run_batched(args)
+    elif WORKLOADS[args.workload][2] == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

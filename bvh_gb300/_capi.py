@@ -76,6 +76,30 @@ class Camera(ctypes.Structure):
     _fields_ = [("eye", c_float * 3), ("look_at", c_float * 3), ("up", c_float * 3), ("fov_y_deg", c_float)]
 
 
+class EvalStats(ctypes.Structure):
+    _fields_ = [("sah", ctypes.c_double), ("avg_leaf_depth", ctypes.c_double), ("node_count", c_uint64),
+                ("leaf_count", c_uint64), ("max_depth", c_uint32), ("reserved", c_uint32)]
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_uint64), ("slots", c_int32), ("morton_bits", c_int32), ("device", c_int32),
+                ("max_triangles", c_uint32), ("max_rays", c_uint32), ("reserved", c_int32 * 3)]
+
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("mesh", MeshSoA), ("rays", Rays), ("hits", Hits), ("tag", c_uint64)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("tag", c_uint64), ("status", c_int32), ("triangles", c_uint32), ("rays", c_uint32),
+                ("reserved", c_uint32), ("t_submit_ns", c_uint64), ("t_admit_ns", c_uint64), ("t_done_ns", c_uint64)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(f, c_uint64) for f in ("submitted", "admitted", "completed", "rejected", "budget_waits", "triangles",
+                                        "rays", "in_flight_bytes", "peak_in_flight_bytes", "queued")]
+
+
 # Every symbol include/bvh_gb300.h declares, with its ctypes signature.
 SIGNATURES = {
     "bvh_status_string": (c_char_p, [c_int]),
@@ -101,6 +125,13 @@ SIGNATURES = {
     "bvh_tuning_get": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
     "bvh_tuning_set": (c_int, [c_void_p, c_int32, c_int32]),
     "bvh_build_lbvh_static": (c_int, [POINTER(MeshSoA), c_int32, c_void_p, c_void_p, c_void_p]),
+    "bvh_evaluate": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p, POINTER(EvalStats)]),
+    "bvh_serve_default_config": (ServeConfig, []),
+    "bvh_serve_open": (c_int, [POINTER(ServeConfig), POINTER(c_void_p)]),
+    "bvh_serve_submit": (c_int, [c_void_p, POINTER(ServeRequest)]),
+    "bvh_serve_poll": (c_int32, [c_void_p, POINTER(ServeResult), c_int32, c_int32]),
+    "bvh_serve_stats_get": (c_int, [c_void_p, POINTER(ServeStats)]),
+    "bvh_serve_close": (c_int, [c_void_p]),
 }
 
 _lib = None

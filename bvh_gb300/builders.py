@@ -127,6 +127,14 @@ class Context:
         self._batch_keep = offsets
         return t
 
+    def evaluate(self, nodes_ptr: int, n_nodes: int, stream: int = 0) -> dict:
+        """BVHEvaluator statistics of a device node array, computed on the GPU (bvh_evaluate)."""
+        st = C.EvalStats()
+        C.check(self.lib.bvh_evaluate(self.handle, ctypes.c_void_p(nodes_ptr), n_nodes, ctypes.c_void_p(stream),
+                                      ctypes.byref(st)), "bvh_evaluate")
+        return {"sah": st.sah, "avg_leaf_depth": st.avg_leaf_depth, "node_count": st.node_count,
+                "leaf_count": st.leaf_count, "max_depth": st.max_depth}
+
     def autotune(self, n: int, stream: int = 0) -> dict:
         """Time every radix-sort variant on n keys, keep the fastest (bvh_autotune); returns the table."""
         import json

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) k_seg_morton(MeshPtrs m, const SegItem* _
 cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets, uint32_t count,
                           const SegItem* d_items, uint32_t n_items, float* d_mbox, uint32_t* d_indices,
                           cudaStream_t st, StageEvents* evs) {
-  cudaError_t e = workspace_reserve(ws, n);
+  cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(ws.cap_n);
   int mbits = 1;
@@ -164,8 +164,12 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   if (evs && evs->use) cudaEventRecord(evs->ev[3], st);
   const unsigned long long* keys = reinterpret_cast<const unsigned long long*>(ws.keys[fb]);
   k_delta<unsigned long long, true><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], d_offsets, ws.delta, n);
-  k_emit<SegBatch, false><<<div_up(n, 256), 256, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, ws.slots,
-                                                          ws.scratch + L.epoch, n, SegBatch{keys, d_offsets}, d_indices);
+  uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
+  uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer
+  k_emit<SegBatch, false><<<div_up(n, 256), 256, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n,
+                                                          SegBatch{keys, d_offsets}, d_indices, frontier, fcount);
+  k_emit_climb<SegBatch, false><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
+      ws.delta, ws.nodes, ws.slots, ws.scratch + L.epoch, n, SegBatch{keys, d_offsets}, frontier, fcount);
   if (evs && evs->use) {
     cudaEventRecord(evs->ev[4], st);
     cudaEventRecord(evs->ev[5], st);

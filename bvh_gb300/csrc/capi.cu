@@ -25,6 +25,8 @@ struct bvh_ctx {
   Workspace ws;
   BatchGraph bgraph;
   cudaStream_t capture_stream = nullptr;  // for CUDA graph capture (never the legacy stream)
+  void* eval_buf = nullptr;               // bvh_evaluate scratch
+  size_t eval_bytes = 0;
   StageEvents evs;
   bvh_timing last{};
   int last_algo = -1;
@@ -77,7 +79,7 @@ extern "C" bvh_status bvh_ctx_create(bvh_ctx** out, int device) {
   for (int k = 0; k < 8; ++k)
     if (cudaEventCreate(&c->evs.ev[k]) != cudaSuccess) { delete c; return BVH_ERR_DEVICE; }
   c->evs.use = true;
-  if (cudaMallocHost(&c->h_status, 64) != cudaSuccess) { delete c; return BVH_ERR_OUT_OF_MEMORY; }
+  if (cudaMallocHost(&c->h_status, 128) != cudaSuccess) { delete c; return BVH_ERR_OUT_OF_MEMORY; }
   if (prepare_kernels() != cudaSuccess) { delete c; return BVH_ERR_DEVICE; }
   if (cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
@@ -94,6 +96,7 @@ extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
   if (ctx->bgraph.exec) cudaGraphExecDestroy(ctx->bgraph.exec);
   if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
   workspace_free(ctx->ws);
+  cudaFree(ctx->eval_buf);
   for (int k = 0; k < 8; ++k) cudaEventDestroy(ctx->evs.ev[k]);
   cudaFreeHost(ctx->h_status);
   delete ctx;
@@ -103,8 +106,10 @@ extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
 extern "C" bvh_status bvh_ctx_reserve(bvh_ctx* ctx, uint32_t n, int32_t algo) {
   if (!ctx) return BVH_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
-  cudaError_t e = workspace_reserve(ctx->ws, n);
+  // zero on the legacy stream and wait, so that builds on any stream see the cleared buffers
+  cudaError_t e = workspace_reserve(ctx->ws, n, nullptr);
   if (e == cudaSuccess && algo == BVH_ALGO_PLOC) e = workspace_reserve_ploc(ctx->ws, n);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
   return from_cuda(e);
 }
 
@@ -167,13 +172,8 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   uint32_t* idx = nullptr;
   cudaError_t e;
   if (params->algo == BVH_ALGO_PLOC) {
-    int it = 0, np = 0;
-    unsigned long long cs = 0;
-    e = ploc_build(ctx->ws, m, n, params->ploc_radius, params->max_iterations, st, &ctx->evs, &idx, &it, &cs, &np);
-    ctx->last.ploc_iterations = it;
-    ctx->last.ploc_cluster_sum = cs;
+    e = ploc_build(ctx->ws, m, n, params->ploc_radius, params->max_iterations, st, &ctx->evs, &idx);
     if (e != cudaSuccess) return from_cuda(e);
-    if (np) return BVH_ERR_NO_PROGRESS;
   } else {
     int rounds = params->algo == BVH_ALGO_LBVH_PLUS ? params->treelet_rounds : 0;
     e = lbvh_build(ctx->ws, m, n, params->morton_bits, rounds, st, &ctx->evs, &idx);
@@ -181,6 +181,8 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   }
   ScratchLayout L = scratch_layout(ctx->ws.cap_n);
   cudaMemcpyAsync(ctx->h_status, ctx->ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
+  if (params->algo == BVH_ALGO_PLOC)  // iterations and live-cluster sum, read at bvh_sync
+    cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.ploc, 16 * 4, cudaMemcpyDeviceToHost, st);
   cudaEventRecord(ctx->evs.ev[6], st);
   out->nodes = reinterpret_cast<const bvh_node*>(ctx->ws.nodes);
   out->indices = idx;
@@ -208,6 +210,11 @@ extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
   if (!ctx->have_timing) return BVH_OK;
   cudaError_t e = cudaEventSynchronize(ctx->evs.ev[6]);
   if (e != cudaSuccess) return from_cuda(e);
+  if (ctx->last_algo == BVH_ALGO_PLOC) {
+    const uint32_t* w = ctx->h_status + 4;
+    ctx->last.ploc_iterations = (int32_t)w[kPlocIterWord];
+    ctx->last.ploc_cluster_sum = (uint64_t)w[kPlocSumWord + 1] << 32 | w[kPlocSumWord];
+  }
   return check_status_word(ctx);
 }
 
@@ -308,8 +315,8 @@ static void stage_layout(uint32_t* dst, const uint32_t* offsets, uint32_t count)
       *it++ = SegItem{m, b, std::min(offsets[m + 1], b + kSegChunk), 0};
 }
 
-static cudaError_t reserve_batch(Workspace& ws, uint32_t n, uint32_t count, size_t words) {
-  cudaError_t e = workspace_reserve(ws, n);
+static cudaError_t reserve_batch(Workspace& ws, uint32_t n, uint32_t count, size_t words, cudaStream_t st) {
+  cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   if (ws.bat_words_cap < words || ws.bat_count_cap < count || !ws.bat_offsets) {
     cudaDeviceSynchronize();  // the staging buffer may still be read by queued copies
@@ -365,7 +372,7 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   ctx->last_algo = params->algo;
   const uint32_t n_items = count_items(batch->offsets, count);
   const size_t words = items_at(count) + 4 * (size_t)n_items;
-  cudaError_t e = reserve_batch(ws, n, count, words);
+  cudaError_t e = reserve_batch(ws, n, count, words, st);
   if (e != cudaSuccess) return from_cuda(e);
   // the device copy reads the pinned staging buffer when it executes: rewrite it only when the
   // layout changed, after the work that may still read it has finished
@@ -416,6 +423,36 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   out->n_nodes = 2 * n - count;
   out->n_prims = n;
   return from_cuda(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------------------
+// evaluation
+// ---------------------------------------------------------------------------------------
+extern "C" bvh_status bvh_evaluate(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, void* stream,
+                                   bvh_eval_stats* out) {
+  if (!ctx || !out || (n_nodes && !nodes) || n_nodes > 0x7fffffffu) return BVH_ERR_INVALID_ARG;
+  *out = bvh_eval_stats{};
+  if (n_nodes == 0) return BVH_OK;
+  cudaSetDevice(ctx->device);
+  const size_t need = evaluate_scratch_bytes(n_nodes);
+  if (ctx->eval_bytes < need) {
+    cudaFree(ctx->eval_buf);
+    ctx->eval_buf = nullptr;
+    ctx->eval_bytes = 0;
+    cudaError_t e = cudaMalloc(&ctx->eval_buf, need);
+    if (e != cudaSuccess) return from_cuda(e);
+    ctx->eval_bytes = need;
+  }
+  EvalResult r;
+  cudaError_t e = evaluate_tree(reinterpret_cast<const Node*>(nodes), n_nodes, ctx->eval_buf,
+                                reinterpret_cast<cudaStream_t>(stream), &r);
+  if (e != cudaSuccess) return from_cuda(e);
+  out->sah = r.sah;
+  out->avg_leaf_depth = r.avg_leaf_depth;
+  out->node_count = r.nodes;
+  out->leaf_count = r.leaves;
+  out->max_depth = r.max_depth;
+  return BVH_OK;
 }
 
 // ---------------------------------------------------------------------------------------

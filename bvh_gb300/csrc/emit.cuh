@@ -7,7 +7,8 @@
 // (delta_nt, lbvh_builder.cu:33-43: common-prefix length of the codes, or 32/64 +
 // clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0 marks a segment boundary).
 // Step 2 (k_emit): one thread per sorted position climbs; merges whose two children belong to
-// threads of one block happen in shared memory, the rest through global rendezvous words.  A node with range [f, l] has its
+// threads of one block happen in shared memory.  Nodes whose sibling is built by another block
+// are listed as a frontier, from which k_emit_climb continues through global rendezvous words.  A node with range [f, l] has its
 // parent's split on the side whose adjacent delta is larger (Apetrei 2014): gamma = l when
 // D[l] > D[f-1], else gamma = f-1.  The second child to reach gamma's rendezvous word completes
 // the parent.  Karras ids: leaf i -> n-1+i, a left child's id is its last index, a right
@@ -111,8 +112,8 @@ struct Climb {
 template <typename Seg, bool PARENTS>
 __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
                                               const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
-                                              unsigned long long* __restrict__ slots, const uint32_t* epoch_word,
-                                              uint32_t n, Seg seg, uint32_t* __restrict__ out_idx) {
+                                              uint32_t n, Seg seg, uint32_t* __restrict__ out_idx,
+                                              uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count) {
   constexpr uint32_t T = 256;
   // per-position state published for the block-local pairing rounds
   __shared__ uint32_t s_gamma[T], s_l[T];
@@ -199,39 +200,72 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
     if (!any) break;
     __syncthreads();  // state arrays are rewritten next round
   }
-  if (!active) return;
-  // ---- phase 2: the remaining nodes meet their siblings through the rendezvous words ----
+  // ---- nodes whose sibling lies (partly) outside the block continue in k_emit_climb ----
+  __shared__ uint32_t s_count, s_base;
+  if (tid == 0) s_count = 0;
+  __syncthreads();
+  uint32_t slot_in_block = 0;
+  if (active) slot_in_block = atomicAdd(&s_count, 1u);
+  __syncthreads();
+  if (tid == 0 && s_count) s_base = atomicAdd(frontier_count, s_count);
+  __syncthreads();
+  if (active) frontier[s_base + slot_in_block] = make_uint2(c.f, c.l);
+}
+
+// Climb from every frontier node (a finished node whose parent needs a sibling built by
+// another block) through the rendezvous words; the second child to arrive completes the parent.
+template <typename Seg, bool PARENTS>
+__global__ void __launch_bounds__(256) k_emit_climb(const uint8_t* __restrict__ D, Node* __restrict__ nodes,
+                                                    unsigned long long* __restrict__ slots,
+                                                    const uint32_t* epoch_word, uint32_t n, Seg seg,
+                                                    const uint2* __restrict__ frontier,
+                                                    const uint32_t* __restrict__ frontier_count) {
+  const uint32_t count = __ldcg(frontier_count);
   const unsigned long long tag = (unsigned long long)__ldcg(epoch_word) << 32;
-  while (true) {
-    const uint32_t far = is_left ? c.f : c.l;
-    const unsigned long long old = atom_exch_acq_rel(slots + gamma, tag | far);
-    if ((old & 0xffffffff00000000ull) != tag) return;  // first child to arrive
-    const uint32_t other = (uint32_t)old;
-    const int32_t g = (int32_t)(gamma - off);
-    int32_t sib;
-    if (is_left) {
-      sib = (other == gamma + 1) ? (int32_t)cnt + g : g + 1;
-      c.lc = c.my;
-      c.rc = sib;
-      c.l = other;
-      c.box = box_union(c.box, load_node_box(nodes, nb + (uint32_t)sib));
-    } else {
-      sib = (other == gamma) ? (int32_t)cnt - 1 + g : g;
-      c.lc = sib;
-      c.rc = c.my;
-      c.f = other;
-      c.box = box_union(load_node_box(nodes, nb + (uint32_t)sib), c.box);
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const uint2 fl = __ldcg(frontier + e);
+    Climb c;
+    c.f = fl.x;
+    c.l = fl.y;
+    uint32_t off, cnt, nb;
+    seg.get(c.f, off, cnt, nb);
+    int dl = c.f == 0 ? -1 : (int)__ldg(D + c.f - 1) - 1;
+    int dr = c.l + 1 >= n ? -1 : (int)__ldg(D + c.l) - 1;
+    bool is_left = dr > dl;
+    uint32_t gamma = is_left ? c.l : c.f - 1;
+    c.my = c.f == c.l ? (int32_t)(cnt - 1 + (c.f - off)) : (int32_t)((is_left ? c.l : c.f) - off);
+    c.box = load_node_box(nodes, nb + (uint32_t)c.my);
+    while (true) {
+      const uint32_t far = is_left ? c.f : c.l;
+      const unsigned long long old = atom_exch_acq_rel(slots + gamma, tag | far);
+      if ((old & 0xffffffff00000000ull) != tag) break;  // first child to arrive
+      const uint32_t other = (uint32_t)old;
+      const int32_t g = (int32_t)(gamma - off);
+      int32_t sib;
+      if (is_left) {
+        sib = (other == gamma + 1) ? (int32_t)cnt + g : g + 1;
+        c.lc = c.my;
+        c.rc = sib;
+        c.l = other;
+        c.box = box_union(c.box, load_node_box(nodes, nb + (uint32_t)sib));
+      } else {
+        sib = (other == gamma) ? (int32_t)cnt - 1 + g : g;
+        c.lc = sib;
+        c.rc = c.my;
+        c.f = other;
+        c.box = box_union(load_node_box(nodes, nb + (uint32_t)sib), c.box);
+      }
+      dl = c.f == 0 ? -1 : (int)__ldg(D + c.f - 1) - 1;
+      dr = c.l + 1 >= n ? -1 : (int)__ldg(D + c.l) - 1;
+      if (dl < 0 && dr < 0) {
+        write_internal<PARENTS>(nodes, nb, 0, c.box, c.lc, c.rc);
+        break;
+      }
+      is_left = dr > dl;
+      gamma = is_left ? c.l : c.f - 1;
+      c.my = (int32_t)((is_left ? c.l : c.f) - off);
+      write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
     }
-    const int dl = c.f == 0 ? -1 : (int)__ldg(D + c.f - 1) - 1;
-    const int dr = c.l + 1 >= n ? -1 : (int)__ldg(D + c.l) - 1;
-    if (dl < 0 && dr < 0) {
-      write_internal<PARENTS>(nodes, nb, 0, c.box, c.lc, c.rc);
-      return;
-    }
-    is_left = dr > dl;
-    gamma = is_left ? c.l : c.f - 1;
-    c.my = (int32_t)((is_left ? c.l : c.f) - off);
-    write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
   }
 }
 

@@ -529,7 +529,7 @@ static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const 
 }
 
 cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out) {
-  cudaError_t e = workspace_reserve(ws, n);
+  cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(ws.cap_n);
   if ((e = tune_width<uint32_t>(ws, n, st, L, ms_out)) != cudaSuccess) return e;
@@ -543,13 +543,18 @@ void workspace_free(Workspace& ws) {
   cudaFree(ws.keys[0]); cudaFree(ws.keys[1]);
   cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
   cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch); cudaFree(ws.delta);
+  if (ws.ploc_exec) cudaGraphExecDestroy(ws.ploc_exec);
   cudaFree(ws.cbox[0]); cudaFree(ws.cbox[1]); cudaFree(ws.cid[0]); cudaFree(ws.cid[1]); cudaFree(ws.nbr);
   cudaFree(ws.mesh_dev);
   cudaFree(ws.bat_offsets); cudaFreeHost(ws.bat_offsets_h); cudaFree(ws.bat_mbox); cudaFree(ws.bat_indices);
   ws = Workspace();
 }
 
-cudaError_t workspace_reserve(Workspace& ws, uint32_t n) {
+// Grows the build buffers to n triangles.  The first-use zeroing (rendezvous slots, scratch) is
+// enqueued on `st`, the stream the next build runs on, so that it is ordered before that build's
+// kernels even when `st` is a non-blocking stream (a synchronous cudaMemset would run on the
+// legacy stream, unordered with respect to non-blocking streams).
+cudaError_t workspace_reserve(Workspace& ws, uint32_t n, cudaStream_t st) {
   if (n <= ws.cap_n && ws.scratch) return cudaSuccess;
   uint32_t cap = std::max<uint32_t>(n, 1024);
   cudaFree(ws.keys[0]); cudaFree(ws.keys[1]); cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
@@ -568,8 +573,8 @@ cudaError_t workspace_reserve(Workspace& ws, uint32_t n) {
   if ((e = cudaMalloc(&ws.delta, (size_t)cap + 16)) != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(cap);
   if ((e = cudaMalloc(&ws.scratch, L.total * 4)) != cudaSuccess) return e;
-  if ((e = cudaMemset(ws.slots, 0, (size_t)cap * 8)) != cudaSuccess) return e;
-  if ((e = cudaMemset(ws.scratch, 0, L.total * 4)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(ws.slots, 0, (size_t)cap * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(ws.scratch, 0, L.total * 4, st)) != cudaSuccess) return e;
   ws.scratch_words = L.total;
   ws.cap_n = cap;
   return cudaSuccess;
@@ -615,11 +620,16 @@ cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStre
 }
 
 template <typename K, bool PARENTS>
-static void launch_emit(Workspace& ws, int fb, uint32_t n, const uint32_t* epoch, cudaStream_t st) {
+static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& L, cudaStream_t st) {
   const K* keys = reinterpret_cast<const K*>(ws.keys[fb]);
+  const uint32_t* epoch = ws.scratch + L.epoch;
+  uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
+  uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer, 8 B per position
   k_delta<K, false><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], nullptr, ws.delta, n);
-  k_emit<SegSingle, PARENTS><<<div_up(n, 256), 256, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, ws.slots,
-                                                             epoch, n, SegSingle{n}, nullptr);
+  k_emit<SegSingle, PARENTS><<<div_up(n, 256), 256, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n,
+                                                             SegSingle{n}, nullptr, frontier, fcount);
+  k_emit_climb<SegSingle, PARENTS><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
+      ws.delta, ws.nodes, ws.slots, epoch, n, SegSingle{n}, frontier, fcount);
 }
 
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
@@ -629,24 +639,23 @@ cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st,
 
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,
                        StageEvents* evs, uint32_t** out_indices) {
-  cudaError_t e = workspace_reserve(ws, n);
+  cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(ws.cap_n);
   rec(evs, 0, st);
   int fb = 0;
-  const uint32_t* epoch = ws.scratch + L.epoch;
   const bool parents = treelet_rounds > 0;
   if (bits == 30) {
     e = lbvh_prefix<30, uint32_t>(ws, m, n, st, evs, L, &fb);
     if (e != cudaSuccess) return e;
-    if (parents) launch_emit<uint32_t, true>(ws, fb, n, epoch, st);
-    else launch_emit<uint32_t, false>(ws, fb, n, epoch, st);
+    if (parents) launch_emit<uint32_t, true>(ws, fb, n, L, st);
+    else launch_emit<uint32_t, false>(ws, fb, n, L, st);
   } else {
     if (bits == 60) e = lbvh_prefix<60, unsigned long long>(ws, m, n, st, evs, L, &fb);
     else e = lbvh_prefix<63, unsigned long long>(ws, m, n, st, evs, L, &fb);
     if (e != cudaSuccess) return e;
-    if (parents) launch_emit<unsigned long long, true>(ws, fb, n, epoch, st);
-    else launch_emit<unsigned long long, false>(ws, fb, n, epoch, st);
+    if (parents) launch_emit<unsigned long long, true>(ws, fb, n, L, st);
+    else launch_emit<unsigned long long, false>(ws, fb, n, L, st);
   }
   rec(evs, 4, st);
   if (treelet_rounds > 0 && n >= 2) {

@@ -29,6 +29,11 @@ struct Workspace {
   int32_t* cid[2] = {nullptr, nullptr};
   int32_t* nbr = nullptr;
   uint32_t ploc_cap = 0;
+  cudaGraphExec_t ploc_exec = nullptr;  // clustering loop graph, valid for the key below
+  uint32_t ploc_key_n = 0;
+  int ploc_key_r = 0;
+  const void* ploc_key_nodes = nullptr;
+  const void* ploc_key_scratch = nullptr;
   // device-side mesh copy for host-pointer builds
   float* mesh_dev = nullptr;
   uint32_t mesh_cap = 0;
@@ -64,6 +69,7 @@ struct ScratchLayout {
 constexpr int kBoundsBlocks = 152 * 4;
 constexpr int kSortThreads = 256;
 constexpr int kMaxPasses = 8;
+constexpr int kFrontierCounter = 15;  // counters[15]: emission frontier length (passes use 0..7)
 
 ScratchLayout scratch_layout(uint32_t n);
 int sort_tile(int key_bytes);  // smallest tile over all variants (sizes the look-back scratch)
@@ -84,10 +90,14 @@ struct StageEvents {
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int morton_bits, int treelet_rounds,
                        cudaStream_t st, StageEvents* evs, uint32_t** out_indices);
 
-// PLOC (radius r) over device-resident SoA input.  Node count is 2n-1.
+// PLOC (radius r) over device-resident SoA input, fully asynchronous (the clustering loop is a
+// CUDA graph WHILE node).  Node count is 2n-1; iterations and the live-cluster sum are left in
+// the PLOC control words (kPlocIterWord, kPlocSumWord) and a loop that cannot finish sets
+// kStatusNoProgress.
 cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter,
-                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices, int* iterations,
-                       unsigned long long* cluster_sum, int* no_progress);
+                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices);
+constexpr int kPlocIterWord = 6;
+constexpr int kPlocSumWord = 8;
 
 // Shared pieces used by PLOC: bounds + Morton-30 + sort (indices sorted by code).
 cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
@@ -97,9 +107,18 @@ cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStre
 cudaError_t prepare_kernels();
 
 // Grow `ws` to hold n triangles (cudaMalloc; synchronising).
-cudaError_t workspace_reserve(Workspace& ws, uint32_t n);
+cudaError_t workspace_reserve(Workspace& ws, uint32_t n, cudaStream_t st);
 cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n);
 void workspace_free(Workspace& ws);
+
+// Tree statistics on the device (BVHEvaluator, src/evaluator.cpp:38-113).
+struct EvalResult {
+  double sah = 0, avg_leaf_depth = 0;
+  unsigned long long nodes = 0, leaves = 0;
+  uint32_t max_depth = 0;
+};
+size_t evaluate_scratch_bytes(uint32_t n_nodes);
+cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cudaStream_t st, EvalResult* out);
 
 // Treelet restructuring passes (LBVH+) after emission.
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st);

@@ -6,9 +6,12 @@
 // order-preserving compaction (:267-293), same root move to index 0 (:563-582).
 //
 // Differences by design: new node ids are handed out in ascending cluster order through a
-// scan (the reference uses atomicAdd, so its ids vary run to run); the merge and the
-// compaction are one kernel with a decoupled look-back scan; the host reads back one word per
-// iteration instead of five.
+// scan (the reference uses atomicAdd, so its ids vary run to run); merge and compaction are one
+// kernel with a decoupled look-back scan; and the iteration loop runs on the device as a CUDA
+// graph WHILE node (the reference synchronises with the host five times per iteration,
+// :489-548): a one-thread step kernel swaps the cluster buffers, stops on convergence, on an
+// iteration that merges nothing (NaN/Inf areas, where the reference loops forever) or at the
+// iteration cap, and sets the loop condition.
 #include <algorithm>
 
 #include "lbvh.cuh"
@@ -19,76 +22,95 @@ constexpr int kPlocThreads = 256;
 constexpr int kPlocIpt = 8;
 constexpr int kPlocTile = kPlocThreads * kPlocIpt;
 
-// control words (scratch + L.ploc): [0] clusters, [1] next node id, [2] tile counter
-__global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __restrict__ tri_boxes, Box* __restrict__ cbox,
-                            int32_t* __restrict__ cid, Node* __restrict__ nodes, uint32_t n,
-                            uint32_t* __restrict__ ctrl) {
+// control words (scratch + L.ploc):
+//   [0] live clusters  [1] next node id  [2] merge tile counter  [3] buffer parity
+//   [4] survivors (next iteration)  [5] next node id (next iteration)  [6] iterations  [7] cap
+//   [8..9] sum of live clusters over iterations (64-bit)
+struct PlocBufs {
+  Box* cbox[2];
+  int32_t* cid[2];
+  int32_t* nbr;
+  unsigned long long* desc;
+  Node* nodes;
+  uint32_t* ctrl;
+  uint32_t* status;
+};
+
+__global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __restrict__ tri_boxes, PlocBufs B, uint32_t n,
+                            uint32_t cap) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
-    ctrl[0] = n;
-    ctrl[1] = n;
+    B.ctrl[0] = n;
+    B.ctrl[1] = n;
+    B.ctrl[2] = 0;
+    B.ctrl[3] = 0;
+    B.ctrl[6] = 0;
+    B.ctrl[7] = cap;
+    B.ctrl[8] = 0;
+    B.ctrl[9] = 0;
   }
   if (i >= n) return;
   uint32_t prim = __ldg(sidx + i);
   const float4* bp = reinterpret_cast<const float4*>(tri_boxes + prim);
   float4 lo = __ldg(bp), hi = __ldg(bp + 1);
-  reinterpret_cast<float4*>(cbox + i)[0] = lo;
-  reinterpret_cast<float4*>(cbox + i)[1] = hi;
-  cid[i] = (int32_t)i;
-  float4* np = reinterpret_cast<float4*>(nodes + i);
+  reinterpret_cast<float4*>(B.cbox[0] + i)[0] = lo;
+  reinterpret_cast<float4*>(B.cbox[0] + i)[1] = hi;
+  B.cid[0][i] = (int32_t)i;
+  float4* np = reinterpret_cast<float4*>(B.nodes + i);
   np[0] = lo;
   np[1] = hi;
   reinterpret_cast<int4*>(np + 2)[0] = make_int4((int32_t)(prim | kLeafBit), -1, 0, 0);
 }
 
-// Nearest neighbour in the +-r window, staged through shared memory.  Also clears the
-// look-back descriptors and tile counter used by the following merge kernel.
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(const Box* __restrict__ cbox, int32_t* __restrict__ nbr,
-                                                          int r, uint32_t* __restrict__ ctrl,
-                                                          unsigned long long* __restrict__ desc, uint32_t desc_words) {
+// Nearest neighbour in the +-r window, one 256-cluster tile per block iteration, the window
+// staged in shared memory.  Also clears the merge kernel's look-back words and tile counter.
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   extern __shared__ float sb[];  // 6 planes of (kPlocThreads + 2r) floats
-  const uint32_t c = __ldcg(ctrl + 0);
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const Box* __restrict__ cbox = B.cbox[__ldcg(B.ctrl + 3) & 1u];
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  for (uint32_t w = gtid; w < desc_words; w += gridDim.x * blockDim.x) desc[w] = 0ull;
-  if (gtid == 0) ctrl[2] = 0;
-  const int64_t base = (int64_t)blockIdx.x * kPlocThreads;
-  if (base >= (int64_t)c) return;
+  const uint32_t mtiles = div_up(c, kPlocTile);
+  for (uint32_t w = gtid; w < mtiles; w += gridDim.x * blockDim.x) B.desc[w] = 0ull;
+  if (gtid == 0) B.ctrl[2] = 0;
   const int span = kPlocThreads + 2 * r;
-  const int64_t lo = base - r;
-  for (int k = threadIdx.x; k < span; k += blockDim.x) {
-    int64_t j = lo + k;
-    if (j >= 0 && j < (int64_t)c) {
-      const float4* bp = reinterpret_cast<const float4*>(cbox + j);
-      float4 a = __ldg(bp), b = __ldg(bp + 1);
-      sb[0 * span + k] = a.x; sb[1 * span + k] = a.y; sb[2 * span + k] = a.z;
-      sb[3 * span + k] = b.x; sb[4 * span + k] = b.y; sb[5 * span + k] = b.z;
+  for (int64_t base = (int64_t)blockIdx.x * kPlocThreads; base < (int64_t)c; base += (int64_t)gridDim.x * kPlocThreads) {
+    const int64_t lo = base - r;
+    __syncthreads();  // previous tile's window no longer read
+    for (int k = threadIdx.x; k < span; k += blockDim.x) {
+      int64_t j = lo + k;
+      if (j >= 0 && j < (int64_t)c) {
+        const float4* bp = reinterpret_cast<const float4*>(cbox + j);
+        float4 a = __ldcg(bp), b = __ldcg(bp + 1);
+        sb[0 * span + k] = a.x; sb[1 * span + k] = a.y; sb[2 * span + k] = a.z;
+        sb[3 * span + k] = b.x; sb[4 * span + k] = b.y; sb[5 * span + k] = b.z;
+      }
     }
-  }
-  __syncthreads();
-  const int64_t i = base + threadIdx.x;
-  if (i >= (int64_t)c) return;
-  const int li = (int)(i - lo);
-  const float ax = sb[li], ay = sb[span + li], az = sb[2 * span + li];
-  const float bx = sb[3 * span + li], by = sb[4 * span + li], bz = sb[5 * span + li];
-  const int64_t s = i - r < 0 ? 0 : i - r;
-  const int64_t e = i + r > (int64_t)c - 1 ? (int64_t)c - 1 : i + r;
-  float best = FLT_MAX;
-  int64_t bj = -1;
-  for (int64_t j = s; j <= e; ++j) {
-    if (j == i) continue;
-    const int lj = (int)(j - lo);
-    float x = __fsub_rn(fmaxf(bx, sb[3 * span + lj]), fminf(ax, sb[lj]));
-    float y = __fsub_rn(fmaxf(by, sb[4 * span + lj]), fminf(ay, sb[span + lj]));
-    float z = __fsub_rn(fmaxf(bz, sb[5 * span + lj]), fminf(az, sb[2 * span + lj]));
-    float d = sa_xyz(x, y, z);
-    if (d < best) {
-      best = d;
-      bj = j;
-    } else if (d == best) {
-      if (bj == -1 || j < bj) bj = j;
+    __syncthreads();
+    const int64_t i = base + threadIdx.x;
+    if (i >= (int64_t)c) continue;
+    const int li = (int)(i - lo);
+    const float ax = sb[li], ay = sb[span + li], az = sb[2 * span + li];
+    const float bx = sb[3 * span + li], by = sb[4 * span + li], bz = sb[5 * span + li];
+    const int64_t s = i - r < 0 ? 0 : i - r;
+    const int64_t e = i + r > (int64_t)c - 1 ? (int64_t)c - 1 : i + r;
+    float best = FLT_MAX;
+    int64_t bj = -1;
+    for (int64_t j = s; j <= e; ++j) {
+      if (j == i) continue;
+      const int lj = (int)(j - lo);
+      float x = __fsub_rn(fmaxf(bx, sb[3 * span + lj]), fminf(ax, sb[lj]));
+      float y = __fsub_rn(fmaxf(by, sb[4 * span + lj]), fminf(ay, sb[span + lj]));
+      float z = __fsub_rn(fmaxf(bz, sb[5 * span + lj]), fminf(az, sb[2 * span + lj]));
+      float d = sa_xyz(x, y, z);
+      if (d < best) {
+        best = d;
+        bj = j;
+      } else if (d == best) {
+        if (bj == -1 || j < bj) bj = j;
+      }
     }
+    B.nbr[i] = (int32_t)bj;
   }
-  nbr[i] = (int32_t)bj;
 }
 
 constexpr unsigned long long kPFlagAgg = 1ull << 62;
@@ -96,117 +118,140 @@ constexpr unsigned long long kPFlagInc = 2ull << 62;
 constexpr unsigned long long kPValMask = (1ull << 62) - 1;
 
 // Merge mutual pairs (i < j keeps position i) and compact the survivors; counts are packed as
-// merges << 31 | survivors.
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_merge(const Box* __restrict__ cin, const int32_t* __restrict__ idin,
-                                                             Box* __restrict__ cout, int32_t* __restrict__ idout,
-                                                             const int32_t* __restrict__ nbr, Node* __restrict__ nodes,
-                                                             uint32_t* __restrict__ ctrl, unsigned long long* __restrict__ desc,
-                                                             uint32_t* __restrict__ status) {
+// merges << 31 | survivors.  Persistent blocks take tiles in order from a counter.
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_merge(PlocBufs B) {
   __shared__ uint32_t s_tile;
   __shared__ unsigned long long s_warp[kPlocThreads / 32];
   __shared__ unsigned long long s_prefix;
-  const uint32_t c = __ldcg(ctrl + 0);
-  const uint32_t next = __ldcg(ctrl + 1);
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const uint32_t next = __ldcg(B.ctrl + 1);
+  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
+  const Box* __restrict__ cin = B.cbox[par];
+  const int32_t* __restrict__ idin = B.cid[par];
+  Box* __restrict__ cout = B.cbox[par ^ 1u];
+  int32_t* __restrict__ idout = B.cid[par ^ 1u];
+  const int32_t* __restrict__ nbr = B.nbr;
   const uint32_t tiles = div_up(c, kPlocTile);
-  if (threadIdx.x == 0) s_tile = atomicAdd(ctrl + 2, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  if (tile >= tiles) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // blocked arrangement: thread t owns items base + t*IPT .. + IPT-1 (keeps order for the scan)
-  const uint32_t first = tile * kPlocTile + threadIdx.x * kPlocIpt;
-  uint32_t mflags = 0, vflags = 0;
-  int32_t nj[kPlocIpt];
+  while (true) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_tile = atomicAdd(B.ctrl + 2, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= tiles) return;
+    // blocked arrangement: thread t owns items base + t*IPT .. + IPT-1 (keeps order for the scan)
+    const uint32_t first = tile * kPlocTile + threadIdx.x * kPlocIpt;
+    uint32_t mflags = 0, vflags = 0;
+    int32_t nj[kPlocIpt];
 #pragma unroll
-  for (int k = 0; k < kPlocIpt; ++k) {
-    uint32_t i = first + k;
-    nj[k] = -1;
-    if (i < c) {
-      int32_t j = __ldg(nbr + i);
-      nj[k] = j;
-      bool mutual = j >= 0 && (uint32_t)j < c && __ldg(nbr + j) == (int32_t)i;
-      if (mutual && (int32_t)i < j) mflags |= 1u << k;
-      if (!(mutual && j < (int32_t)i)) vflags |= 1u << k;
+    for (int k = 0; k < kPlocIpt; ++k) {
+      uint32_t i = first + k;
+      nj[k] = -1;
+      if (i < c) {
+        int32_t j = __ldcg(nbr + i);
+        nj[k] = j;
+        bool mutual = j >= 0 && (uint32_t)j < c && __ldcg(nbr + j) == (int32_t)i;
+        if (mutual && (int32_t)i < j) mflags |= 1u << k;
+        if (!(mutual && j < (int32_t)i)) vflags |= 1u << k;
+      }
     }
-  }
-  unsigned long long mine = ((unsigned long long)__popc(mflags) << 31) | (unsigned long long)__popc(vflags);
-  // block exclusive scan
-  unsigned long long x = mine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_warp[w] = x;
-  __syncthreads();
-  if (w == 0) {
-    unsigned long long t = lane < kPlocThreads / 32 ? s_warp[lane] : 0ull;
+    unsigned long long mine = ((unsigned long long)__popc(mflags) << 31) | (unsigned long long)__popc(vflags);
+    unsigned long long x = mine;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= o) t += y;
+      unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
     }
-    if (lane < kPlocThreads / 32) s_warp[lane] = t;
-  }
-  __syncthreads();
-  const unsigned long long tile_total = s_warp[kPlocThreads / 32 - 1];
-  unsigned long long excl_in_tile = (w ? s_warp[w - 1] : 0ull) + x - mine;
-  // decoupled look-back over tiles (single thread)
-  if (threadIdx.x == 0) {
-    unsigned long long pre = 0;
-    if (tile == 0) {
-      st_relaxed(desc, kPFlagInc | tile_total);
-    } else {
-      st_relaxed(desc + tile, kPFlagAgg | tile_total);
-      pre = lookback<16, unsigned long long>(desc, 1, (int64_t)tile, ~kPValMask, kPFlagInc, status,
-                                             kStatusSortTimeout);
-      st_relaxed(desc + tile, kPFlagInc | (pre + tile_total));
-    }
-    s_prefix = pre;
-    if (tile == tiles - 1) {
-      unsigned long long tot = pre + tile_total;
-      ctrl[4] = (uint32_t)(tot & 0x7fffffffull);           // survivors
-      ctrl[5] = next + (uint32_t)(tot >> 31);               // next node id
-    }
-  }
-  __syncthreads();
-  unsigned long long ex = s_prefix + excl_in_tile;
-  uint32_t mpos = (uint32_t)(ex >> 31), vpos = (uint32_t)(ex & 0x7fffffffull);
+    if (lane == 31) s_warp[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      unsigned long long t = lane < kPlocThreads / 32 ? s_warp[lane] : 0ull;
 #pragma unroll
-  for (int k = 0; k < kPlocIpt; ++k) {
-    uint32_t i = first + k;
-    if (i >= c) break;
-    const float4* ip = reinterpret_cast<const float4*>(cin + i);
-    float4 lo = __ldg(ip), hi = __ldg(ip + 1);
-    int32_t id = __ldg(idin + i);
-    if ((mflags >> k) & 1u) {
-      int32_t j = nj[k];
-      const float4* jp = reinterpret_cast<const float4*>(cin + j);
-      float4 jlo = __ldg(jp), jhi = __ldg(jp + 1);
-      lo = make_float4(fminf(lo.x, jlo.x), fminf(lo.y, jlo.y), fminf(lo.z, jlo.z), 0.f);
-      hi = make_float4(fmaxf(hi.x, jhi.x), fmaxf(hi.y, jhi.y), fmaxf(hi.z, jhi.z), 0.f);
-      int32_t nid = (int32_t)(next + mpos);
-      if ((uint32_t)nid >= 2 * next) break;  // counts inconsistent only after a timed-out wait
-      float4* np = reinterpret_cast<float4*>(nodes + nid);
-      np[0] = lo;
-      np[1] = hi;
-      reinterpret_cast<int4*>(np + 2)[0] = make_int4(id, __ldg(idin + j), 0, 0);
-      id = nid;
-      mpos++;
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      if (lane < kPlocThreads / 32) s_warp[lane] = t;
     }
-    if (((vflags >> k) & 1u) && vpos < c) {
-      float4* op = reinterpret_cast<float4*>(cout + vpos);
-      op[0] = lo;
-      op[1] = hi;
-      idout[vpos] = id;
-      vpos++;
+    __syncthreads();
+    const unsigned long long tile_total = s_warp[kPlocThreads / 32 - 1];
+    const unsigned long long excl_in_tile = (w ? s_warp[w - 1] : 0ull) + x - mine;
+    if (threadIdx.x == 0) {
+      unsigned long long pre = 0;
+      if (tile == 0) {
+        st_relaxed(B.desc, kPFlagInc | tile_total);
+      } else {
+        st_relaxed(B.desc + tile, kPFlagAgg | tile_total);
+        pre = lookback<16, unsigned long long>(B.desc, 1, (int64_t)tile, ~kPValMask, kPFlagInc, B.status,
+                                               kStatusSortTimeout);
+        st_relaxed(B.desc + tile, kPFlagInc | (pre + tile_total));
+      }
+      s_prefix = pre;
+      if (tile == tiles - 1) {
+        const unsigned long long tot = pre + tile_total;
+        B.ctrl[4] = (uint32_t)(tot & 0x7fffffffull);  // survivors
+        B.ctrl[5] = next + (uint32_t)(tot >> 31);      // next node id
+      }
+    }
+    __syncthreads();
+    const unsigned long long ex = s_prefix + excl_in_tile;
+    uint32_t mpos = (uint32_t)(ex >> 31), vpos = (uint32_t)(ex & 0x7fffffffull);
+#pragma unroll
+    for (int k = 0; k < kPlocIpt; ++k) {
+      uint32_t i = first + k;
+      if (i >= c) break;
+      const float4* ip = reinterpret_cast<const float4*>(cin + i);
+      float4 lo = __ldcg(ip), hi = __ldcg(ip + 1);
+      int32_t id = __ldcg(idin + i);
+      if ((mflags >> k) & 1u) {
+        int32_t j = nj[k];
+        const float4* jp = reinterpret_cast<const float4*>(cin + j);
+        float4 jlo = __ldcg(jp), jhi = __ldcg(jp + 1);
+        lo = make_float4(fminf(lo.x, jlo.x), fminf(lo.y, jlo.y), fminf(lo.z, jlo.z), 0.f);
+        hi = make_float4(fmaxf(hi.x, jhi.x), fmaxf(hi.y, jhi.y), fmaxf(hi.z, jhi.z), 0.f);
+        int32_t nid = (int32_t)(next + mpos);
+        if ((uint32_t)nid >= 2 * next) break;  // counts inconsistent only after a timed-out wait
+        float4* np = reinterpret_cast<float4*>(B.nodes + nid);
+        np[0] = lo;
+        np[1] = hi;
+        reinterpret_cast<int4*>(np + 2)[0] = make_int4(id, __ldcg(idin + j), 0, 0);
+        id = nid;
+        mpos++;
+      }
+      if (((vflags >> k) & 1u) && vpos < c) {
+        float4* op = reinterpret_cast<float4*>(cout + vpos);
+        op[0] = lo;
+        op[1] = hi;
+        idout[vpos] = id;
+        vpos++;
+      }
     }
   }
 }
 
+// End of one iteration: publish the survivors, swap buffers, decide whether to go on.
+__global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t c = B.ctrl[0], nc = B.ctrl[4], it = B.ctrl[6] + 1, cap = B.ctrl[7];
+  unsigned long long sum = ((unsigned long long)B.ctrl[9] << 32 | B.ctrl[8]) + c;
+  B.ctrl[8] = (uint32_t)sum;
+  B.ctrl[9] = (uint32_t)(sum >> 32);
+  B.ctrl[6] = it;
+  B.ctrl[0] = nc;
+  B.ctrl[1] = B.ctrl[5];
+  B.ctrl[3] ^= 1u;
+  bool go = nc > 1;
+  if (go && (nc >= c || it >= cap)) {  // no mutual pair anywhere, or the cap: stop and report
+    atomicOr(B.status, kStatusNoProgress);
+    go = false;
+  }
+  cudaGraphSetConditional(handle, go ? 1u : 0u);
+}
+
 // Move the root (last node) to index 0 and swap every reference to 0 and the root
-// (ploc_builder.cu:563-582).  Thread 0 owns nodes 0 and R.
-__global__ void k_ploc_root(Node* __restrict__ nodes, uint32_t total) {
+// (ploc_builder.cu:563-582); skipped when the loop did not converge.  Thread 0 owns 0 and R.
+__global__ void k_ploc_root(Node* __restrict__ nodes, uint32_t total, const uint32_t* __restrict__ ctrl) {
+  if (__ldcg(ctrl + 0) != 1) return;
   const uint32_t R = total - 1;
   auto fix = [&](int32_t c) -> int32_t {
     if (c < 0) return c;
@@ -234,6 +279,10 @@ __global__ void k_ploc_root(Node* __restrict__ nodes, uint32_t total) {
 cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   if (n <= ws.ploc_cap && ws.nbr) return cudaSuccess;
   uint32_t cap = std::max<uint32_t>(n, 1024);
+  if (ws.ploc_exec) {
+    cudaGraphExecDestroy(ws.ploc_exec);
+    ws.ploc_exec = nullptr;
+  }
   cudaFree(ws.cbox[0]); cudaFree(ws.cbox[1]); cudaFree(ws.cid[0]); cudaFree(ws.cid[1]); cudaFree(ws.nbr);
   ws.cbox[0] = ws.cbox[1] = nullptr; ws.cid[0] = ws.cid[1] = nullptr; ws.nbr = nullptr; ws.ploc_cap = 0;
   cudaError_t e;
@@ -248,68 +297,94 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   return cudaSuccess;
 }
 
+static size_t nn_smem(int radius) { return 6 * sizeof(float) * (kPlocThreads + 2 * (size_t)radius); }
+
+// The loop as a graph: WHILE(cond) { nn; merge; step }.  Grids are persistent (sized for n), the
+// kernels read the live cluster count from the control words.
+static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n, int radius, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle handle;
+  cudaStream_t cs = nullptr;
+  cudaGraphNode_t node;
+  cudaGraphNodeParams cp = {};
+  do {
+    if ((e = cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if ((e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp)) != cudaSuccess) break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+      break;
+    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocThreads), 152 * 8));
+    const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 4));
+    k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), cs>>>(B, radius);
+    k_ploc_merge<<<mg_grid, kPlocThreads, 0, cs>>>(B);
+    k_ploc_step<<<1, 32, 0, cs>>>(B, handle);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e2 = cudaGetLastError();
+    e = cudaStreamEndCapture(cs, &captured);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) break;
+    e = cudaGraphInstantiate(out, g, 0);
+  } while (false);
+  if (cs) cudaStreamDestroy(cs);
+  cudaGraphDestroy(g);
+  return e;
+}
+
 cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter, cudaStream_t st,
-                       StageEvents* evs, uint32_t** out_indices, int* iterations, unsigned long long* cluster_sum,
-                       int* no_progress) {
-  *no_progress = 0;
-  cudaError_t e = workspace_reserve(ws, n);
+                       StageEvents* evs, uint32_t** out_indices) {
+  cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   if ((e = workspace_reserve_ploc(ws, n)) != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(ws.cap_n);
+  PlocBufs B;
+  B.cbox[0] = ws.cbox[0];
+  B.cbox[1] = ws.cbox[1];
+  B.cid[0] = ws.cid[0];
+  B.cid[1] = ws.cid[1];
+  B.nbr = ws.nbr;
+  B.desc = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(ws.nbr) +
+                                                  (((size_t)ws.ploc_cap * 4 + 15) & ~size_t(15)));
+  B.nodes = ws.nodes;
+  B.ctrl = ws.scratch + L.ploc;
+  B.status = ws.scratch + L.status;
+  if (nn_smem(radius) > 48 * 1024) {
+    if ((e = cudaFuncSetAttribute(k_ploc_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem(radius))) !=
+        cudaSuccess)
+      return e;
+  }
+  // every iteration that makes progress removes at least one cluster, so n bounds the loop
+  const uint32_t cap = max_iter > 0 ? (uint32_t)max_iter : n;
+  if (n > 1) {
+    const bool same = ws.ploc_exec && ws.ploc_key_n == n && ws.ploc_key_r == radius && ws.ploc_key_nodes == ws.nodes &&
+                      ws.ploc_key_scratch == ws.scratch;
+    if (!same) {
+      if (ws.ploc_exec) cudaGraphExecDestroy(ws.ploc_exec);
+      ws.ploc_exec = nullptr;
+      if ((e = make_loop_graph(ws, B, n, radius, &ws.ploc_exec)) != cudaSuccess) return e;
+      ws.ploc_key_n = n;
+      ws.ploc_key_r = radius;
+      ws.ploc_key_nodes = ws.nodes;
+      ws.ploc_key_scratch = ws.scratch;
+    }
+  }
   if (evs && evs->use) cudaEventRecord(evs->ev[0], st);
   uint32_t* sidx = nullptr;
   if ((e = prefix_sort30(ws, m, n, st, evs, &sidx)) != cudaSuccess) return e;
   *out_indices = sidx;
-  uint32_t* ctrl = ws.scratch + L.ploc;
-  k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, ws.cbox[0], ws.cid[0], ws.nodes, n, ctrl);
+  k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap);
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
-  unsigned long long* desc =
-      reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(ws.nbr) + (((size_t)ws.ploc_cap * 4 + 15) & ~size_t(15)));
-  uint32_t c = n;
-  int it = 0;
-  unsigned long long csum = 0;
-  int cur = 0;
-  uint32_t* h_ctrl = nullptr;
-  if ((e = cudaMallocHost(&h_ctrl, 8)) != cudaSuccess) return e;
-  // every iteration that makes progress removes at least one cluster, so n bounds the loop;
-  // an iteration that merges nothing stops it at once (no_progress)
-  const int64_t cap_iter = max_iter > 0 ? max_iter : (int64_t)n;
-  const size_t nn_smem = 6 * sizeof(float) * (kPlocThreads + 2 * (size_t)radius);
-  if (nn_smem > 48 * 1024) {
-    if ((e = cudaFuncSetAttribute(k_ploc_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem)) != cudaSuccess) {
-      cudaFreeHost(h_ctrl);
-      return e;
-    }
+  if (n > 1) {
+    if ((e = cudaGraphLaunch(ws.ploc_exec, st)) != cudaSuccess) return e;
+    k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
   }
-  while (c > 1) {
-    if (it >= cap_iter) {
-      *no_progress = 1;
-      break;
-    }
-    csum += c;
-    const uint32_t tiles = div_up(c, kPlocTile);
-    k_ploc_nn<<<div_up(c, kPlocThreads), kPlocThreads, nn_smem, st>>>(ws.cbox[cur], ws.nbr, radius, ctrl, desc,
-                                                                       tiles);
-    k_ploc_merge<<<tiles, kPlocThreads, 0, st>>>(ws.cbox[cur], ws.cid[cur], ws.cbox[cur ^ 1], ws.cid[cur ^ 1], ws.nbr,
-                                                 ws.nodes, ctrl, desc, ws.scratch + L.status);
-    // publish the new count for the next iteration and read it back
-    cudaMemcpyAsync(ctrl, ctrl + 4, 8, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(h_ctrl, ctrl + 4, 8, cudaMemcpyDeviceToHost, st);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
-    cur ^= 1;
-    it++;
-    uint32_t nc = h_ctrl[0];
-    if (nc >= c) {  // no mutual pair anywhere (NaN or infinite areas): the reference loops forever
-      *no_progress = 1;
-      break;
-    }
-    c = nc;
-  }
-  cudaFreeHost(h_ctrl);
-  if (iterations) *iterations = it;
-  if (cluster_sum) *cluster_sum = csum;
-  if (e != cudaSuccess || *no_progress) return e;
-  if (n > 1) k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1);
   if (evs && evs->use) cudaEventRecord(evs->ev[5], st);
   return cudaGetLastError();
 }

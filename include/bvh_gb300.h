@@ -200,6 +200,74 @@ bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant32, int32_t variant64);
 bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t morton_bits, bvh_node* nodes, uint32_t* indices,
                                  void* stream);
 
+/* ---- serving (no reference counterpart) ----------------------------------------------------
+ * A continuously batched build+trace server: requests are admitted oldest-first whenever a slot
+ * is free and their device-memory estimate fits the HBM budget beside everything in flight;
+ * admitted requests run concurrently (one stream and workspace per slot).  Each request uploads
+ * its host mesh and rays, builds an LBVH, traces the rays and downloads the hits into the
+ * caller's host buffers, which must stay valid until its result is polled (pinned buffers let
+ * uploads and downloads overlap other requests).  A request's result does not depend on what
+ * else is in flight. */
+typedef struct bvh_server bvh_server;
+
+typedef struct bvh_serve_config {
+  uint64_t hbm_budget_bytes; /* admission budget for all requests in flight */
+  int32_t slots;             /* requests in flight at most */
+  int32_t morton_bits;       /* LBVH keys: 30, 60 or 63 */
+  int32_t device;
+  uint32_t max_triangles;    /* per-slot buffers allocated up front for this size (0: grow on demand) */
+  uint32_t max_rays;
+  int32_t reserved[3];
+} bvh_serve_config;
+
+typedef struct bvh_serve_request {
+  bvh_mesh_soa mesh; /* host pointers */
+  bvh_rays rays;     /* host pointers */
+  bvh_hits hits;     /* host pointers, rays.n entries each (NULL entries are skipped) */
+  uint64_t tag;      /* returned in the result */
+} bvh_serve_request;
+
+typedef struct bvh_serve_result {
+  uint64_t tag;
+  int32_t status;       /* bvh_status; BVH_ERR_OUT_OF_MEMORY if it can never fit the budget */
+  uint32_t triangles;
+  uint32_t rays;
+  uint32_t reserved;
+  uint64_t t_submit_ns; /* steady-clock times: submitted, admitted to a slot, completed */
+  uint64_t t_admit_ns;
+  uint64_t t_done_ns;
+} bvh_serve_result;
+
+typedef struct bvh_serve_stats {
+  uint64_t submitted, admitted, completed, rejected, budget_waits;
+  uint64_t triangles, rays;
+  uint64_t in_flight_bytes, peak_in_flight_bytes, queued;
+} bvh_serve_stats;
+
+bvh_serve_config bvh_serve_default_config(void);
+bvh_status bvh_serve_open(const bvh_serve_config* cfg, bvh_server** out);
+/* Queue a request (does not block on the GPU). */
+bvh_status bvh_serve_submit(bvh_server* sv, const bvh_serve_request* req);
+/* Move up to max_results finished requests into out, waiting up to wait_ms for the first. */
+int32_t bvh_serve_poll(bvh_server* sv, bvh_serve_result* out, int32_t max_results, int32_t wait_ms);
+bvh_status bvh_serve_stats_get(bvh_server* sv, bvh_serve_stats* out);
+/* Finish every queued request, then release the server. */
+bvh_status bvh_serve_close(bvh_server* sv);
+
+/* Tree statistics (BVHEvaluator::evaluate, src/evaluator.cpp:7-113) computed on the GPU for a
+ * device node array: SAH with the reference's costs (3 per internal node, 2 per leaf, areas
+ * relative to the root), reachable node and leaf counts, maximum and average leaf depth.  The
+ * per-node terms are the host evaluator's; they are summed in double.  Synchronous. */
+typedef struct bvh_eval_stats {
+  double sah;
+  double avg_leaf_depth;
+  uint64_t node_count;
+  uint64_t leaf_count;
+  uint32_t max_depth;
+  uint32_t reserved;
+} bvh_eval_stats;
+bvh_status bvh_evaluate(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, void* stream, bvh_eval_stats* out);
+
 /* Closest-hit traversal of explicit rays (device pointers).  Asynchronous. */
 bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_nodes, const bvh_mesh_soa* mesh,
                      const bvh_rays* rays, const bvh_hits* hits, void* stream);

@@ -80,3 +80,18 @@ def test_pinhole_counters_vs_reference_render_kernel(ctx, gpu):
     assert same.mean() >= 0.999, same.mean()
     bg = np.all(np.isclose(rgb, [0.15, 0.15, 0.18]), axis=1)
     assert ((got[1] < 0) == bg).mean() >= 0.999
+
+
+@pytest.mark.parametrize("algo", [C.ALGO_LBVH, C.ALGO_PLOC, C.ALGO_LBVH_PLUS])
+def test_gpu_evaluator_matches_reference_evaluator_restatement(ctx, gpu, oracle_lib, algo):
+    """bvh_evaluate against the oracle's restatement of BVHEvaluator (itself pinned bit-equal to
+    the reference's evaluator.cpp): SAH within 1e-5 relative, counts and depths exact."""
+    O = oracle_lib
+    m = meshgen.clustered(50_000, seed=31)
+    nodes, idx, tree, _ = build(ctx, gpu, m, ctx.params(algo))
+    st = ctx.evaluate(tree.nodes, tree.n_nodes, stream(gpu))
+    sah = O.sah(nodes)
+    md, avg, lc = O.depth_stats(nodes)
+    assert abs(st["sah"] - sah) <= 1e-5 * abs(sah)
+    assert st["node_count"] == nodes.shape[0] and st["leaf_count"] == lc and st["max_depth"] == md
+    assert abs(st["avg_leaf_depth"] - avg) <= 1e-5 * avg
