@@ -167,7 +167,8 @@ __global__ void __launch_bounds__(256) k_bounds(MeshPtrs m, uint32_t n, int vec4
 }
 
 // ---------------------------------------------------------------------------------------
-// k_morton: AABB + centroid + Morton code + digit histograms of every pass
+// k_morton: AABB + centroid + Morton code + digit histograms of the 4 sort passes
+// (32-bit keys: bits 0..31; 64-bit keys: the high 32 bits, from bit BITS-32)
 // ---------------------------------------------------------------------------------------
 template <int BITS, typename K>
 __device__ __forceinline__ K tri_code(float x0, float y0, float z0, float x1, float y1, float z1, float x2,
@@ -189,7 +190,8 @@ template <int BITS, typename K>
 __global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4, K* __restrict__ keys,
                                                 Box* __restrict__ boxes, uint32_t* __restrict__ scratch,
                                                 ScratchLayout L) {
-  constexpr int P = (int)sizeof(K);  // 8-bit digit passes
+  constexpr int P = 4;                                   // 8-bit digit passes
+  constexpr int S0 = sizeof(K) == 8 ? BITS - 32 : 0;     // first sorted bit
   __shared__ uint32_t s_hist[P][256];
   for (int i = threadIdx.x; i < P * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0;
   __shared__ float s_scene[8];
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4
         bp[2 * e] = b[e].lo;
         bp[2 * e + 1] = b[e].hi;
 #pragma unroll
-        for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c[e] >> (8 * p2)) & 255u], 1u);
+        for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c[e] >> (S0 + 8 * p2)) & 255u], 1u);
       }
     }
     done = n4 << 2;
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4
     keys[i] = c;
     boxes[i] = b;
 #pragma unroll
-    for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c >> (8 * p2)) & 255u], 1u);
+    for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c >> (S0 + 8 * p2)) & 255u], 1u);
   }
   __syncthreads();
   uint32_t* gh = scratch + L.hist;
@@ -286,7 +288,7 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan_u64(unsigned 
 template <typename K, int THREADS, int IPT, int W, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                       K* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
-                                                      int pass, uint32_t* __restrict__ scratch, ScratchLayout L,
+                                                      int pass, int shift0, uint32_t* __restrict__ scratch, ScratchLayout L,
                                                       uint32_t tiles) {
   constexpr int BINS = 256, NW = THREADS / 32, TILE = THREADS * IPT;
   static_assert(THREADS == BINS, "one thread per bin");
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict_
   uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_scan + 32);
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int shift = 8 * pass;
+  const int shift = shift0 + 8 * pass;  // digit `pass` of the bits sorted by this sequence of passes
   if (tid == 0) *s_tile = atomicAdd(scratch + L.counters + pass, 1u);
   for (int b = tid; b < NW * BINS; b += THREADS) s_whist[b] = 0;
   __syncthreads();
@@ -439,7 +441,8 @@ cudaError_t prepare_kernels() {
 }
 
 template <typename K>
-cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L, int* final_buf) {
+cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L, int* final_buf,
+                     int shift0 = 0) {
   const SortVariant& sv = variant((int)sizeof(K), ws.sort_variant[sizeof(K) == 4 ? 0 : 1]);
   const uint32_t tile = (uint32_t)kSortThreads * sv.ipt;
   uint32_t tiles = div_up(n, tile);
@@ -451,7 +454,7 @@ cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, con
     uint32_t* vout = ws.vals[cur ^ 1];
     uint32_t* scratch = ws.scratch;
     ScratchLayout Lc = L;
-    void* args[] = {(void*)&kin, (void*)&vin, (void*)&kout, (void*)&vout, (void*)&n, (void*)&p, (void*)&scratch,
+    void* args[] = {(void*)&kin, (void*)&vin, (void*)&kout, (void*)&vout, (void*)&n, (void*)&p, (void*)&shift0, (void*)&scratch,
                     (void*)&Lc, (void*)&tiles};
     cudaError_t e = cudaLaunchKernel(sv.fn, dim3(tiles), dim3(kSortThreads), args, sv.smem, st);
     if (e != cudaSuccess) return e;
@@ -471,10 +474,12 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 
-// Pseudo-random keys (63 or 30 bits) with the radix histograms of every pass.
+// Pseudo-random keys (63 or 30 bits) with the radix histograms of the 4 passes that start at
+// bit shift0.
 template <typename K>
-__global__ void __launch_bounds__(256) k_tune_keys(K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
-  constexpr int P = (int)sizeof(K);
+__global__ void __launch_bounds__(256) k_tune_keys(K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
+                                                   int shift0) {
+  constexpr int P = 4;
   __shared__ uint32_t s_hist[P][256];
   for (int k = threadIdx.x; k < P * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
   __syncthreads();
@@ -483,7 +488,7 @@ __global__ void __launch_bounds__(256) k_tune_keys(K* __restrict__ keys, uint32_
     const K k = sizeof(K) == 4 ? (K)(z >> 34) : (K)(z >> 1);
     keys[i] = k;
 #pragma unroll
-    for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p][(uint32_t)(k >> (8 * p)) & 255u], 1u);
+    for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p][(uint32_t)(k >> (shift0 + 8 * p)) & 255u], 1u);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < P * 256; k += blockDim.x)
@@ -495,7 +500,9 @@ static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const 
   const int kb = (int)sizeof(K);
   cudaError_t e = cudaMemsetAsync(ws.scratch + L.zero_begin, 0, (L.zero_end - L.zero_begin) * 4, st);
   if (e != cudaSuccess) return e;
-  k_tune_keys<K><<<152 * 8, 256, 0, st>>>(reinterpret_cast<K*>(ws.keys[0]), n, ws.scratch + L.hist);
+  // the builds sort 64-bit keys by their high 32 bits (then fix runs), 32-bit keys whole
+  const int shift0 = kb == 8 ? 31 : 0;
+  k_tune_keys<K><<<152 * 8, 256, 0, st>>>(reinterpret_cast<K*>(ws.keys[0]), n, ws.scratch + L.hist, shift0);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -510,7 +517,7 @@ static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const 
       cudaMemsetAsync(ws.scratch + L.desc, 0, (L.zero_end - L.desc) * 4, st);
       int fb = 0;
       cudaEventRecord(e0, st);
-      e = run_sort<K>(ws, n, kb, st, L, &fb);
+      e = run_sort<K>(ws, n, 4, st, L, &fb, shift0);
       cudaEventRecord(e1, st);
       if (e == cudaSuccess) e = cudaEventSynchronize(e1);
       if (e != cudaSuccess) break;
@@ -597,7 +604,7 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   // zero only the descriptors this build's passes use
   ScratchLayout Lz = L;
   const int kb = (int)sizeof(K);
-  Lz.zero_end = L.desc + (size_t)kb * div_up(std::max<uint32_t>(n, 1),
+  Lz.zero_end = L.desc + (size_t)4 * div_up(std::max<uint32_t>(n, 1),
                                              (uint32_t)sort_variant_tile(kb, ws.sort_variant[kb == 4 ? 0 : 1])) * 256;
   k_bounds<<<kBoundsBlocks, 256, 0, st>>>(m, n, vec4, ws.scratch, Lz);
   rec(evs, 1, st);
@@ -605,7 +612,15 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(work, 256), 152 * 8));
   k_morton<BITS, K><<<grid, 256, 0, st>>>(m, n, vec4, reinterpret_cast<K*>(ws.keys[0]), ws.boxes, ws.scratch, L);
   rec(evs, 2, st);
-  cudaError_t e = run_sort<K>(ws, n, (int)sizeof(K), st, L, final_buf);
+  // 32-bit keys: 4 passes sort them whole.  64-bit keys: 4 passes sort by the high 32 bits
+  // (BITS-32 .. BITS-1), then each run of equal high halves is ordered by its low bits.
+  constexpr int S0 = sizeof(K) == 8 ? BITS - 32 : 0;
+  cudaError_t e = run_sort<K>(ws, n, 4, st, L, final_buf, S0);
+  if (e == cudaSuccess && sizeof(K) == 8) {
+    const int fb = *final_buf;
+    e = sort_fix_runs(reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb],
+                      reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, S0, st);
+  }
   rec(evs, 3, st);
   return e;
 }

@@ -120,6 +120,12 @@ struct EvalResult {
 size_t evaluate_scratch_bytes(uint32_t n_nodes);
 cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cudaStream_t st, EvalResult* out);
 
+// Completes a sort of 64-bit keys whose radix passes covered only bits lbits..lbits+31: orders
+// every run of equal key >> lbits by (key low bits, position), in place; tkeys/tvals (the other
+// ping-pong buffers) are scratch for runs longer than 64.
+cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
+                          uint32_t n, int lbits, cudaStream_t st);
+
 // Treelet restructuring passes (LBVH+) after emission.
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st);
 

@@ -30,6 +30,17 @@ def clumped(n, seed=8):
     return TriangleMesh.from_vertices(c, c + np.float32(1e-8), c + np.float32([0, 2e-8, 0]))
 
 
+def dense_cell(n, size=2e-4, spread=0.1, seed=10):
+    """Most triangles in one small cube of a unit scene: with 60/63-bit codes they share the high
+    32 code bits but differ below (long runs for the run fix-up after the high-half sort)."""
+    g = np.random.default_rng(seed)
+    c = g.random((n, 3), dtype=np.float32) * np.float32(size) + np.float32(0.3)
+    k = int(n * spread)
+    c[:k] = g.random((k, 3), dtype=np.float32)
+    d = np.float32(size * 0.01)
+    return TriangleMesh.from_vertices(c, c + d, c + np.float32([0, 1, 0]) * d)
+
+
 def negative_scaled(n, seed=9):
     m = meshgen.uniform_small(n, seed=seed, scale=123.0, offset=(-400.0, 7.0, -0.001))
     return m
@@ -45,4 +56,6 @@ def small_cases():
     out["clumped5000"] = clumped(5000)
     out["negscaled3000"] = negative_scaled(3000)
     out["clustered20000"] = meshgen.clustered(20000, seed=11)
+    out["densecell6000"] = dense_cell(6000)                   # runs of thousands
+    out["mediumcell3000"] = dense_cell(3000, size=4e-3)       # runs of about ten
     return out

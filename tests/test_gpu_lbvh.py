@@ -43,6 +43,18 @@ def test_lbvh_clustered_bit_exact(ctx, gpu, oracle_lib, n, bits):
     assert O.node_fields_equal(nodes, onodes)
 
 
+@pytest.mark.parametrize("bits", [60, 63])
+@pytest.mark.parametrize("n,size", [(200_000, 1e-4), (300_000, 2e-3), (300_000, 2e-2)])
+def test_lbvh_long_runs_across_tiles(ctx, gpu, oracle_lib, bits, n, size):
+    """Runs of equal high code halves spanning many fix-up tiles (block-wide path) and many
+    runs of a few dozen (shared-memory ranks), against the oracle's full-key sort."""
+    m = meshes.dense_cell(n, size=size, spread=0.02, seed=n)
+    nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=bits))
+    onodes, oidx, _ = oracle_lib.lbvh(m.arrays(), bits)
+    assert np.array_equal(idx, oidx)
+    assert oracle_lib.node_fields_equal(nodes, onodes)
+
+
 def test_lbvh_unaligned_input_takes_scalar_path(ctx, gpu, oracle_lib):
     O = oracle_lib
     m = meshgen.uniform_small(5000, seed=42)
