@@ -115,12 +115,13 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
                                               uint32_t n, Seg seg, uint32_t* __restrict__ out_idx,
                                               uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count) {
   constexpr uint32_t T = 256;
-  // per-position state published for the block-local pairing rounds
-  __shared__ uint32_t s_gamma[T], s_l[T];
-  __shared__ int32_t s_my[T];
-  __shared__ uint8_t s_state[T];  // bit0 active, bit1 is_left
-  __shared__ uint8_t s_claim[T];
-  __shared__ float s_box[6][T];
+  // D of positions bbase-1 .. bbase+T-1 (0 outside [0, n-1) : a segment boundary)
+  __shared__ uint8_t s_D[T + 1];
+  // rendezvous slot k <-> split gamma = bbase + k: one side per child (0 left, 1 right)
+  __shared__ uint32_t s_flag[T];
+  __shared__ float s_bx[2][6][T];
+  __shared__ int32_t s_id[2][T];
+  __shared__ uint32_t s_end[2][T];  // the child's far end: f of a left child, l of a right child
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * T + tid;
   const uint32_t bbase = blockIdx.x * T;  // sorted position of thread 0
@@ -131,7 +132,6 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
   c.lc = c.rc = -1;
   c.internal = false;
   c.my = 0;
-  c.box.lo = c.box.hi = make_float4(0.f, 0.f, 0.f, 0.f);
   if (active) {
     seg.get(i, off, cnt, nb);
     const uint32_t prim_g = __ldg(vals + i);
@@ -142,74 +142,91 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, con
     c.box.hi = __ldg(bp + 1);
     c.my = (int32_t)(cnt - 1) + (int32_t)(i - off);
     store_node(nodes, nb + (uint32_t)c.my, c.box, (int32_t)(prim | kLeafBit), -1, -1);
-    if (cnt == 1) active = false;
+    if (cnt == 1) active = false;  // a one-triangle mesh: the leaf is the root
   }
-  s_claim[tid] = 0;
-  // ---- phase 1: merges whose two children are owned by threads of this block (no atomics) ----
-  // The thread of a node's first position owns it; a left child at split gamma finds its right
-  // sibling at thread gamma + 1 - bbase.
-  bool is_left = false;
-  uint32_t gamma = 0;
-  while (true) {
-    bool want = false;
-    if (active) {
-      const int dl = c.f == 0 ? -1 : (int)__ldg(D + c.f - 1) - 1;
-      const int dr = c.l + 1 >= n ? -1 : (int)__ldg(D + c.l) - 1;
-      if (dl < 0 && dr < 0) {  // segment root (internal: single-triangle meshes stopped above)
-        write_internal<PARENTS>(nodes, nb, 0, c.box, c.lc, c.rc);
-        active = false;
-      } else {
-        is_left = dr > dl;
-        gamma = is_left ? c.l : c.f - 1;
-        if (c.internal) {
-          c.my = (int32_t)((is_left ? c.l : c.f) - off);
-          write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
-          c.internal = false;  // written; `my` now names it
-        }
-        want = is_left && gamma + 1 >= bbase && gamma + 1 < bbase + T;
-      }
+  {
+    const int64_t j = (int64_t)bbase - 1 + tid;
+    s_D[tid] = (j >= 0 && j + 1 < (int64_t)n) ? __ldg(D + j) : (uint8_t)0;
+    if (tid == 0) {
+      const uint64_t jl = (uint64_t)bbase + T - 1;
+      s_D[T] = jl + 1 < n ? __ldg(D + jl) : (uint8_t)0;
     }
-    s_state[tid] = (active ? 1 : 0) | (is_left ? 2 : 0);
-    s_gamma[tid] = gamma;
-    s_l[tid] = c.l;
-    s_my[tid] = c.my;
-    s_box[0][tid] = c.box.lo.x; s_box[1][tid] = c.box.lo.y; s_box[2][tid] = c.box.lo.z;
-    s_box[3][tid] = c.box.hi.x; s_box[4][tid] = c.box.hi.y; s_box[5][tid] = c.box.hi.z;
-    __syncthreads();
-    bool paired = false;
-    if (want) {
-      const uint32_t p = gamma + 1 - bbase;
-      if (s_state[p] == 1 && s_gamma[p] == gamma) {  // active right child of the same parent
-        paired = true;
-        Box pb;
-        pb.lo = make_float4(s_box[0][p], s_box[1][p], s_box[2][p], 0.f);
-        pb.hi = make_float4(s_box[3][p], s_box[4][p], s_box[5][p], 0.f);
-        c.lc = c.my;
-        c.rc = s_my[p];
-        c.l = s_l[p];
-        c.box = box_union(c.box, pb);
-        c.internal = true;
-        s_claim[p] = 1;
-      }
-    }
-    const int any = __syncthreads_or(paired ? 1 : 0);
-    if (s_claim[tid]) {
-      active = false;
-      s_claim[tid] = 0;
-    }
-    if (!any) break;
-    __syncthreads();  // state arrays are rewritten next round
   }
-  // ---- nodes whose sibling lies (partly) outside the block continue in k_emit_climb ----
+  s_flag[tid] = 0;
+  __syncthreads();
+  // ---- climb inside the block: the second child to reach a split completes the parent ----
+  // A node [f, l] with both ends in this block reads D[f-1] and D[l] from s_D; its parent's
+  // split is gamma = l (it is the left child) when D[l] > D[f-1], else gamma = f-1.
+  bool to_frontier = false;
+  while (active) {
+    const int dl = (int)s_D[c.f - bbase] - 1;
+    const int dr = (int)s_D[c.l - bbase + 1] - 1;
+    if (dl < 0 && dr < 0) {  // segment root
+      write_internal<PARENTS>(nodes, nb, 0, c.box, c.lc, c.rc);
+      break;
+    }
+    const bool is_left = dr > dl;
+    const uint32_t gamma = is_left ? c.l : c.f - 1;
+    if (c.internal) {  // its id is known now: a left child is named by its last index
+      c.my = (int32_t)((is_left ? c.l : c.f) - off);
+      write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
+      c.internal = false;
+    }
+    if (is_left ? gamma + 1 >= bbase + T : gamma < bbase) {  // sibling starts outside the block
+      to_frontier = true;
+      break;
+    }
+    const uint32_t k = gamma - bbase;
+    const int side = is_left ? 0 : 1;
+    s_bx[side][0][k] = c.box.lo.x; s_bx[side][1][k] = c.box.lo.y; s_bx[side][2][k] = c.box.lo.z;
+    s_bx[side][3][k] = c.box.hi.x; s_bx[side][4][k] = c.box.hi.y; s_bx[side][5][k] = c.box.hi.z;
+    s_id[side][k] = c.my;
+    s_end[side][k] = is_left ? c.f : c.l;
+    __threadfence_block();
+    if (atomicOr(&s_flag[k], 1u << side) == 0u) break;  // first to arrive
+    __threadfence_block();
+    const int o = side ^ 1;
+    Box sb;
+    sb.lo = make_float4(s_bx[o][0][k], s_bx[o][1][k], s_bx[o][2][k], 0.f);
+    sb.hi = make_float4(s_bx[o][3][k], s_bx[o][4][k], s_bx[o][5][k], 0.f);
+    if (is_left) {
+      c.lc = c.my;
+      c.rc = s_id[o][k];
+      c.l = s_end[o][k];
+      c.box = box_union(c.box, sb);
+    } else {
+      c.lc = s_id[o][k];
+      c.rc = c.my;
+      c.f = s_end[o][k];
+      c.box = box_union(sb, c.box);
+    }
+    c.internal = true;
+  }
+  __syncthreads();
+  // ---- finished nodes whose parent needs a sibling built elsewhere continue in k_emit_climb:
+  // those stopped at the block edge and those whose in-block sibling never completed ----
+  uint2 fr0 = make_uint2(c.f, c.l), fr1 = make_uint2(0u, 0u);
+  uint32_t nf = to_frontier ? 1u : 0u;
+  if (tid < T - 1) {
+    const uint32_t fl = s_flag[tid];
+    const uint32_t g = bbase + tid;
+    uint2 e = fl == 1u ? make_uint2(s_end[0][tid], g) : make_uint2(g + 1, s_end[1][tid]);
+    if (fl == 1u || fl == 2u) {
+      if (nf) fr1 = e;
+      else fr0 = e;
+      ++nf;
+    }
+  }
   __shared__ uint32_t s_count, s_base;
   if (tid == 0) s_count = 0;
   __syncthreads();
   uint32_t slot_in_block = 0;
-  if (active) slot_in_block = atomicAdd(&s_count, 1u);
+  if (nf) slot_in_block = atomicAdd(&s_count, nf);
   __syncthreads();
   if (tid == 0 && s_count) s_base = atomicAdd(frontier_count, s_count);
   __syncthreads();
-  if (active) frontier[s_base + slot_in_block] = make_uint2(c.f, c.l);
+  if (nf) frontier[s_base + slot_in_block] = fr0;
+  if (nf > 1) frontier[s_base + slot_in_block + 1] = fr1;
 }
 
 // Climb from every frontier node (a finished node whose parent needs a sibling built by
