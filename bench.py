@@ -41,6 +41,10 @@ WORKLOADS = {
                     "10M clustered triangles, LBVH+ 60-bit, 1 treelet pass"),
     "c1_lbvh63_4m": ("clustered", {"n": 4_000_000, "seed": 1}, "lbvh", 63, 0,
                      "4M clustered triangles (config 1 distribution), LBVH 63-bit; profiling size"),
+    "c1_lbvhplus_2m": ("clustered", {"n": 2_000_000, "seed": 1}, "lbvh_plus", 60, 0,
+                       "2M clustered triangles (config 1 distribution), LBVH+ 60-bit, 1 pass; profiling size"),
+    "c1_ploc25_2m": ("clustered", {"n": 2_000_000, "seed": 1}, "ploc", 30, 25,
+                     "2M clustered triangles (config 1 distribution), PLOC radius 25; profiling size"),
     "c2a_ploc25": ("icosphere", {"levels": 8, "seed": 2}, "ploc", 30, 25,
                    "1,310,720-triangle displaced icosphere (0.05 fBm), PLOC radius 25"),
     "c2a_lbvhplus": ("icosphere", {"levels": 8, "seed": 2}, "lbvh_plus", 60, 0,
@@ -61,11 +65,56 @@ WORKLOADS = {
 }
 
 
-def bytes_per_tri(algo: str, bits: int) -> float:
-    """Algorithmic HBM bytes per triangle of a whole build: B(K) = 276 + 3kb + 2D(kb+4)."""
+def bytes_per_tri(algo: str, bits: int, rounds: int = 0, cluster_sum_per_tri: float = 0.0) -> float:
+    """Algorithmic HBM bytes per triangle of a whole build.  LBVH: B(K) = 276 + 3kb + 2D(kb+4)
+    with D = ceil(K/8) 8-bit digits (the bytes an 8-bit LSD sort of the whole key moves; the
+    library's 64-bit sort moves fewer, so B(K) is a property of the problem, not of this
+    implementation).  LBVH+: B(60) + 144 per treelet pass.  PLOC: 264 + 160 * (live clusters
+    summed over iterations) / n."""
+    if algo == "ploc":
+        return 264.0 + 160.0 * cluster_sum_per_tri
     kb = 4 if bits == 30 else 8
-    d = kb  # 8-bit digits: one pass per key byte
-    return 276 + 3 * kb + 2 * d * (kb + 4)
+    d = (bits + 7) // 8
+    b = 276 + 3 * kb + 2 * d * (kb + 4)
+    return b + 144.0 * rounds if algo == "lbvh_plus" else b
+
+
+def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, cluster_sum_per_tri: float = 0.0):
+    """Algorithmic bytes per triangle of one build stage (the split of B(K) above)."""
+    kb = 4 if bits == 30 else 8
+    d = (bits + 7) // 8
+    if stage == "scene_bounds":
+        return 36.0
+    if stage == "morton_boxes_hist":
+        return 36.0 + kb + 4 + 32.0
+    if stage == "onesweep_sort":
+        return kb + 2.0 * d * (kb + 4)
+    if stage == "emit_refit":  # PLOC: leaf nodes + cluster init in this slot
+        return 116.0 if algo == "ploc" else kb + 4 + 36 + 48 + 12 + 48 + 4 + 48
+    if algo == "ploc":
+        return 160.0 * cluster_sum_per_tri
+    return 144.0 * rounds
+
+
+def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0) -> int:
+    """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
+    fix-up for 64-bit keys, delta + emission + frontier climb; one per treelet pass; PLOC adds
+    cluster init, 3 per clustering iteration (neighbours, merge, loop control) and the root fix
+    (its 30-bit prefix stops after the sort)."""
+    if algo == "ploc":
+        return 2 + 4 + 1 + 3 * ploc_iterations + 1
+    n = 2 + 4 + (1 if bits != 30 else 0) + 3
+    return n + (rounds if algo == "lbvh_plus" else 0)
+
+
+STAGE_KERNELS = {
+    "scene_bounds": "k_bounds",
+    "morton_boxes_hist": "k_morton",
+    "onesweep_sort": "k_onesweep x4 (+ k_fixrun for 60/63-bit keys)",
+    "emit_refit": "k_delta + k_emit + k_emit_climb",
+    "treelet_or_ploc_loop": "k_treelet_round (LBVH+) / k_ploc_nn + k_ploc_merge + k_ploc_step per iteration"
+                            " + k_ploc_root (PLOC)",
+}
 
 
 def hbm_peak():
@@ -219,6 +268,7 @@ def run_ours(args):
             ctx.build_device(ptrs, n, params, s)
             t = ctx.last_timing()
             stages.append((t.bounds_ms, t.morton_ms, t.sort_ms, t.emit_ms, t.optimize_ms, t.total_ms))
+            ploc_iters, ploc_csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
     elapsed_ms = ev0.elapsed_time(ev1)
     if ws > 1:
         tt = torch.tensor([elapsed_ms], device=dev)
@@ -230,24 +280,24 @@ def run_ours(args):
     st = np.array(stages, np.float64)
     med = np.median(st, axis=0)
     peak, peak_kind = hbm_peak()
-    kb = 4 if bits == 30 else 8
-    passes = kb
-    # dominant kernel: the one stage with the largest share of device time
+    rounds = 1 if algo == "lbvh_plus" else 0
+    csum = ploc_csum / n if algo == "ploc" else 0.0
+    # dominant stage: the largest share of device time (stage events on the launching stream)
     shares = {"scene_bounds": med[0], "morton_boxes_hist": med[1], "onesweep_sort": med[2], "emit_refit": med[3],
               "treelet_or_ploc_loop": med[4]}
     dom = max(shares, key=shares.get)
-    per_unit = {"scene_bounds": 36.0, "morton_boxes_hist": 36.0 + kb + 32.0,
-                "onesweep_sort": 2.0 * (kb + 4), "emit_refit": kb + 4 + 36 + 48 + 12 + 48 + 4 + 48,
-                "treelet_or_ploc_loop": 144.0}[dom]
-    launches_per_stage = passes if dom == "onesweep_sort" else 1
-    launch_ms = shares[dom] / launches_per_stage
-    achieved = per_unit * n / (launch_ms / 1e3) / 1e9
-    build_gbs = bytes_per_tri(algo, bits) * n / (med[5] / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": f"of {peak_kind}",
-                "algorithmic_bytes_per_tri": per_unit,
-                "whole_build": {"bytes_per_tri": bytes_per_tri(algo, bits), "achieved": round(build_gbs, 1),
+    per_unit = stage_bytes_per_tri(dom, algo, bits, rounds, csum)
+    achieved = per_unit * n / (shares[dom] / 1e3) / 1e9
+    whole = bytes_per_tri(algo, bits, rounds, csum)
+    build_gbs = whole * n / (med[5] / 1e3) / 1e9
+    kernels = "k_ploc_init" if (algo == "ploc" and dom == "emit_refit") else STAGE_KERNELS[dom]
+    roofline = {"bound": "hbm", "kernel": dom, "kernels": kernels, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": round(per_unit, 2),
+                "whole_build": {"bytes_per_tri": round(whole, 2), "achieved": round(build_gbs, 1),
                                 "frac": round(build_gbs / peak, 4), "median_build_ms": round(med[5], 4)}}
+    if algo == "ploc":
+        roofline["ploc"] = {"iterations": ploc_iters, "cluster_sum": ploc_csum}
     stage_ms = {k: round(v, 4) for k, v in shares.items()}
 
     # --- end to end through the C ABI with pinned host buffers ----------------------------
@@ -289,7 +339,7 @@ def run_ours(args):
         "stage_ms_median": stage_ms,
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": args.steps * (2 + passes + 1 + (1 if algo == "lbvh_plus" else 0)) if algo != "ploc" else None,
+        "gpu_launches": args.steps * kernels_per_build(algo, bits, rounds, ploc_iters),
         "clocks": clk.summary(),
         "autotune": tuning,
     }

@@ -138,11 +138,24 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun(unsigned long long* __re
   const uint32_t tile_end = min(n, a + (uint32_t)kFixTile);
   const unsigned long long lmask = (1ull << lbits) - 1ull;
   if (t == 0) s_nlong = 0;
-  for (uint32_t q = lo + t; q < hi; q += kFixThreads) {
-    const unsigned long long k = keys[q];
-    s_h[q - a + 1] = (uint32_t)(k >> lbits);
-    s_l[q - a + 1] = (uint32_t)(k & lmask);
-    s_dst[q - a + 1] = kNone;
+  {
+    // all of this thread's loads first (kSpan / 256 + 1 per thread), then the stores
+    constexpr int kPer = (kSpan + kFixThreads - 1) / kFixThreads;
+    unsigned long long k[kPer];
+#pragma unroll
+    for (int r = 0; r < kPer; ++r) {
+      const uint32_t q = lo + t + (uint32_t)r * kFixThreads;
+      k[r] = q < hi ? keys[q] : 0ull;
+    }
+#pragma unroll
+    for (int r = 0; r < kPer; ++r) {
+      const uint32_t q = lo + t + (uint32_t)r * kFixThreads;
+      if (q < hi) {
+        s_h[q - a + 1] = (uint32_t)(k[r] >> lbits);
+        s_l[q - a + 1] = (uint32_t)(k[r] & lmask);
+        s_dst[q - a + 1] = kNone;
+      }
+    }
   }
   __syncthreads();
 #define H(q) s_h[(q) - a + 1]

@@ -10,8 +10,8 @@
 // second child arrives, so the result is independent of scheduling and equal to any
 // children-before-parent order (the oracle uses post-order).
 //
-// The DP is warp-cooperative: every warp keeps looping while any lane still climbs; lanes that
-// reached a node needing work are served one at a time by all 32 lanes.
+// Every warp keeps looping while any lane still climbs.  Lanes that reached a node grow and
+// rebuild their own treelets in parallel; the subset DP of each is done by all 32 lanes.
 #include "emit.cuh"
 #include "lbvh.cuh"
 
@@ -31,15 +31,43 @@ __device__ __forceinline__ int2 ldcg_children(const Node* nodes, int32_t idx) {
   return __ldcg(reinterpret_cast<const int2*>(&nodes[idx].left));
 }
 
-// Per-warp shared state for one treelet.
-struct TreeletSmem {
-  float cost[1 << kTlMax];
-  float area[1 << kTlMax];
-  uint8_t part[1 << kTlMax];
-  Box leafbox[kTlMax];
+// Subsets of {0..6} with 2..7 members, by size, increasing within a size.  For a treelet of
+// n < 7 leaves the subsets of its full mask are the entries <= (1 << n) - 1, in the same order.
+__constant__ uint8_t c_subsets[120] = {
+    3, 5, 6, 9, 10, 12, 17, 18, 20, 24, 33, 34, 36, 40, 48, 65, 66, 68, 72, 80, 96,
+    7, 11, 13, 14, 19, 21, 22, 25, 26, 28, 35, 37, 38, 41, 42, 44, 49, 50, 52, 56, 67, 69, 70, 73, 74, 76, 81,
+    82, 84, 88, 97, 98, 100, 104, 112,
+    15, 23, 27, 29, 30, 39, 43, 45, 46, 51, 53, 54, 57, 58, 60, 71, 75, 77, 78, 83, 85, 86, 89, 90, 92, 99,
+    101, 102, 105, 106, 108, 113, 114, 116, 120,
+    31, 47, 55, 59, 61, 62, 79, 87, 91, 93, 94, 103, 107, 109, 110, 115, 117, 118, 121, 122, 124,
+    63, 95, 111, 119, 123, 125, 126,
+    127};
+__constant__ uint8_t c_sub_off[9] = {0, 0, 0, 21, 56, 91, 112, 119, 120};  // first entry of size k
+
+// One lane's treelet: its leaves (node ids, boxes, cached children), the expansions that grew
+// it (which the id reuse walks instead of reloading nodes) and the DP's best partitions.
+struct LaneTreelet {
+  float box[6][kTlMax];  // lo.x lo.y lo.z hi.x hi.y hi.z of each leaf
   int32_t act[kTlMax];
+  int32_t chl[kTlMax], chr[kTlMax];  // children of each leaf node (left has kLeafBit for a BVH leaf)
+  int32_t exp_node[kTlMax - 1], exp_l[kTlMax - 1], exp_r[kTlMax - 1];
+  uint8_t part[1 << kTlMax];
   int32_t n;
 };
+
+__device__ __forceinline__ Box leaf_box(const LaneTreelet& T, int i) {
+  Box b;
+  b.lo = make_float4(T.box[0][i], T.box[1][i], T.box[2][i], 0.f);
+  b.hi = make_float4(T.box[3][i], T.box[4][i], T.box[5][i], 0.f);
+  return b;
+}
+__device__ __forceinline__ void set_leaf(LaneTreelet& T, int i, int32_t id, const Box& b, int2 ch) {
+  T.act[i] = id;
+  T.box[0][i] = b.lo.x; T.box[1][i] = b.lo.y; T.box[2][i] = b.lo.z;
+  T.box[3][i] = b.hi.x; T.box[4][i] = b.hi.y; T.box[5][i] = b.hi.z;
+  T.chl[i] = ch.x;
+  T.chr[i] = ch.y;
+}
 
 // pdep of the low bits of m into the set bits of mask (m-th nonempty subset of mask in
 // increasing numeric order, m >= 1).
@@ -53,169 +81,174 @@ __device__ __forceinline__ uint32_t deposit_bits(uint32_t m, uint32_t mask) {
   return r;
 }
 
-// Warp-cooperative optimizeTreeletSerial at `root` (lbvh_plus_builder.cu:71-247).
-__device__ void treelet_warp(Node* nodes, int32_t root, TreeletSmem& S) {
-  const int lane = threadIdx.x & 31;
-  // 1. grow the treelet (:73-114): lane 0 walks, others wait
-  if (lane == 0) {
-    int cnt = 1;
-    S.act[0] = root;
-    S.leafbox[0] = ldcg_box(nodes, root);
-    for (int step = 0; step < kTlMax - 1; ++step) {
-      int best = -1;
-      float max_area = -1.0f;
-      for (int i = 0; i < cnt; ++i) {
-        int2 ch = ldcg_children(nodes, S.act[i]);
-        if (!((uint32_t)ch.x & kLeafBit)) {
-          float a = box_area(S.leafbox[i]);
-          if (a > max_area) { max_area = a; best = i; }
-        }
+// 1. Grow the treelet at `root` (lbvh_plus_builder.cu:73-114): up to 6 times, expand the leaf
+//    with the largest area among those that are internal nodes (first such on ties).  Run by
+//    one lane; the lanes of a warp grow their own treelets side by side.
+__device__ void treelet_grow(const Node* nodes, int32_t root, LaneTreelet& T) {
+  set_leaf(T, 0, root, ldcg_box(nodes, root), ldcg_children(nodes, root));
+  int cnt = 1;
+  for (int step = 0; step < kTlMax - 1; ++step) {
+    int best = -1;
+    float max_area = -1.0f;
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i) {
+      if (i < cnt && !((uint32_t)T.chl[i] & kLeafBit)) {
+        const float a = box_area(leaf_box(T, i));
+        if (a > max_area) { max_area = a; best = i; }
       }
-      if (best == -1) break;
-      int2 ch = ldcg_children(nodes, S.act[best]);
-      S.act[best] = ch.x;
-      S.leafbox[best] = ldcg_box(nodes, ch.x);
-      S.act[cnt] = ch.y;
-      S.leafbox[cnt] = ldcg_box(nodes, ch.y);
-      cnt++;
     }
-    S.n = cnt;
+    if (best < 0) break;
+    const int32_t l = T.chl[best], r = T.chr[best];
+    T.exp_node[step] = T.act[best];
+    T.exp_l[step] = l;
+    T.exp_r[step] = r;
+    const Box bl = ldcg_box(nodes, l), br = ldcg_box(nodes, r);
+    const int2 cl = ldcg_children(nodes, l), cr = ldcg_children(nodes, r);
+    set_leaf(T, best, l, bl, cl);
+    set_leaf(T, cnt, r, br, cr);
+    ++cnt;
   }
-  __syncwarp();
-  const int n = S.n;
-  if (n < 2) return;
+  T.n = cnt;
+}
+
+// 2+3. Subset areas and the DP over subsets by size (:119-165), by the whole warp for one
+//    lane's treelet.  cost[s] = min over splits (cost[p] + cost[s^p]) + area[s], leaves cost 0;
+//    the best split is the first minimum in the enumeration p = increasing nonempty subsets of
+//    s without its lowest member.  Sizes 2..5 take one lane per subset, size 6 four lanes and
+//    size 7 the whole warp, each lane scanning a contiguous run of that enumeration.
+__device__ void treelet_dp(LaneTreelet& T, float* cost, float* area) {
+  const int lane = threadIdx.x & 31;
+  const int n = T.n;
   const uint32_t full = (1u << n) - 1u;
-  // 2. subset areas and leaf costs (:119-129); the union is exact in any order
   for (uint32_t s = 1 + lane; s <= full; s += 32) {
     Box b = box_empty();
-    for (int i = 0; i < n; ++i)
-      if ((s >> i) & 1u) b = box_union(b, S.leafbox[i]);
-    S.area[s] = box_area(b);
-    S.cost[s] = __popc(s) == 1 ? 0.0f : kTlInf;
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i)
+      if ((s >> i) & 1u) b = box_union(b, leaf_box(T, i));
+    area[s] = box_area(b);
+    cost[s] = __popc(s) == 1 ? 0.0f : kTlInf;
   }
   __syncwarp();
-  // 3. DP by subset size (:131-165).  Work items are (subset, partition) pairs; the best
-  //    partition is the minimum cost, first in the reference's enumeration order on ties.
   for (int k = 2; k <= n; ++k) {
+    const uint32_t L = k <= 5 ? 1u : (k == 6 ? 4u : 32u);
+    const uint32_t base = c_sub_off[k], count = c_sub_off[k + 1] - base;
     const uint32_t nparts = (1u << (k - 1)) - 1u;
-    // lanes per subset: spread partitions over several lanes for the large subsets
-    const uint32_t lps = nparts >= 32 ? 32u : (nparts >= 16 ? 16u : (nparts >= 8 ? 8u : (nparts >= 4 ? 4u : 1u)));
-    const uint32_t groups = 32u / lps;
-    // enumerate subsets of size k in increasing numeric order, `groups` at a time
-    uint32_t s_iter = (1u << k) - 1u;  // smallest subset with k bits
-    while (s_iter <= full) {
-      // each group takes the g-th next subset
-      const uint32_t g = (uint32_t)lane / lps, sub = (uint32_t)lane % lps;
-      uint32_t s = s_iter;
-      for (uint32_t t = 0; t < g && s <= full; ++t) {  // Gosper's hack: next subset with k bits
-        uint32_t c = s & (0u - s), r = s + c;
-        s = (((r ^ s) >> 2) / c) | r;
-      }
+    const uint32_t chunk = (nparts + L - 1) / L;
+    for (uint32_t r0 = 0; r0 < count * L; r0 += 32) {
+      const uint32_t slot = r0 + (uint32_t)lane, e = slot / L, j = slot % L;
+      const uint32_t s = e < count ? c_subsets[base + e] : 0u;
+      const bool valid = e < count && s <= full;
       float best = kTlInf;
       uint32_t best_ord = 0xffffffffu, best_p = 0;
-      if (s <= full) {
-        const uint32_t delta = (s - 1u) & s;
-        for (uint32_t ord = sub; ord < nparts; ord += lps) {
-          uint32_t p = deposit_bits(ord + 1u, delta);
-          float c = __fadd_rn(S.cost[p], S.cost[s ^ p]);
+      if (valid) {
+        const uint32_t delta = s & (s - 1u);
+        const uint32_t o0 = j * chunk, o1 = min(o0 + chunk, nparts);
+        uint32_t p = o0 < o1 ? deposit_bits(o0 + 1u, delta) : 0u;
+        for (uint32_t ord = o0; ord < o1; ++ord) {
+          const float c = __fadd_rn(cost[p], cost[s ^ p]);
           if (c < best) { best = c; best_ord = ord; best_p = p; }
+          p = (p - delta) & delta;  // next subset of delta
         }
       }
-      // reduce within the lane group: min cost, then smallest enumeration order
-      for (uint32_t o = 1; o < lps; o <<= 1) {
-        float ob = __shfl_xor_sync(0xffffffffu, best, o);
-        uint32_t oo = __shfl_xor_sync(0xffffffffu, best_ord, o);
-        uint32_t op = __shfl_xor_sync(0xffffffffu, best_p, o);
+      for (uint32_t o = 1; o < L; o <<= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const uint32_t oo = __shfl_xor_sync(0xffffffffu, best_ord, o);
+        const uint32_t op = __shfl_xor_sync(0xffffffffu, best_p, o);
         if (ob < best || (ob == best && oo < best_ord)) { best = ob; best_ord = oo; best_p = op; }
       }
-      if (sub == 0 && s <= full) {
+      if (valid && j == 0) {
         // the reference starts from INF with strict <, so an all-INF subset keeps INF / -1
-        S.cost[s] = __fadd_rn(best, S.area[s]);
-        S.part[s] = (uint8_t)(best_ord == 0xffffffffu ? 0xffu : best_p);
+        cost[s] = __fadd_rn(best, area[s]);
+        T.part[s] = (uint8_t)(best_ord == 0xffffffffu ? 0xffu : best_p);
       }
-      // advance s_iter by `groups` subsets
-      for (uint32_t t = 0; t < groups && s_iter <= full; ++t) {
-        uint32_t c = s_iter & (0u - s_iter), r = s_iter + c;
-        s_iter = (((r ^ s_iter) >> 2) / c) | r;
-      }
-      __syncwarp();
     }
     __syncwarp();
   }
-  // 4. reuse internal ids (DFS, right child popped first, :167-191) and rebuild breadth-first
-  //    (:194-246); at most 6 internal nodes, done by lane 0
-  if (lane == 0) {
-    int avail[kTlMax];
-    int n_avail = 0;
-    int stack[kTlMax + 8];
-    int top = 0;
-    stack[top++] = root;
-    while (top > 0) {
-      int cur = stack[--top];
-      bool in_leaves = false;
-      for (int i = 0; i < n; ++i)
-        if (S.act[i] == cur) { in_leaves = true; break; }
-      if (!in_leaves && n_avail < kTlMax && top + 2 <= kTlMax + 8) {
-        avail[n_avail++] = cur;
-        int2 ch = ldcg_children(nodes, cur);
-        stack[top++] = ch.x;
-        stack[top++] = ch.y;
-      }
-    }
-    // A subset whose partitions all cost >= INF (NaN areas) has no valid split; the
-    // reference would index out of bounds there, this leaves the treelet unchanged.
-    {
-      int vm[kTlMax], vh = 0, vt = 0;
-      bool ok = true;
-      vm[vt++] = (int)full;
-      while (vh < vt && ok) {
-        int mask = vm[vh++];
-        int lm = S.part[mask], rm = mask ^ lm;
-        if (lm == 0 || rm == 0 || (lm & ~mask)) { ok = false; break; }
-        if (__popc(lm) > 1) { if (vt >= kTlMax) { ok = false; break; } vm[vt++] = lm; }
-        if (__popc(rm) > 1) { if (vt >= kTlMax) { ok = false; break; } vm[vt++] = rm; }
-      }
-      if (!ok || n_avail != n - 1) S.n = 0;
-    }
-    int qm[kTlMax], qn[kTlMax];
-    int qh = 0, qt = 0, used = 1;
-    if (S.n) {
-      qm[qt] = (int)full;
-      qn[qt++] = avail[0];
-    }
-    while (qh < qt) {
-      int mask = qm[qh], cur = qn[qh];
-      qh++;
-      int lm = S.part[mask], rm = mask ^ lm;
-      int li, ri;
-      if (__popc(lm) == 1) li = S.act[__ffs(lm) - 1];
-      else { li = avail[used++]; qm[qt] = lm; qn[qt++] = li; }
-      if (__popc(rm) == 1) ri = S.act[__ffs(rm) - 1];
-      else { ri = avail[used++]; qm[qt] = rm; qn[qt++] = ri; }
-      Box b = box_empty();
-      for (int i = 0; i < n; ++i)
-        if ((mask >> i) & 1) b = box_union(b, S.leafbox[i]);
-      float4* p = reinterpret_cast<float4*>(nodes + cur);
-      __stcg(p, b.lo);
-      __stcg(p + 1, b.hi);
-      __stcg(reinterpret_cast<int2*>(&nodes[cur].left), make_int2(li, ri));
-      __stcg(&nodes[li].aux0, cur);
-      __stcg(&nodes[ri].aux0, cur);
+}
+
+// 4. Reuse the treelet's internal ids (DFS from the root, right child popped first,
+//    :167-191) and rebuild it breadth-first from the partitions (:194-246).  One lane.
+__device__ void treelet_rebuild(Node* nodes, int32_t root, LaneTreelet& T) {
+  const int n = T.n;
+  if (n < 2) return;
+  const uint32_t full = (1u << n) - 1u;
+  int avail[kTlMax];
+  int n_avail = 0;
+  int stack[kTlMax + 8];
+  int top = 0;
+  stack[top++] = root;
+  while (top > 0) {
+    const int cur = stack[--top];
+    bool in_leaves = false;
+    for (int i = 0; i < n; ++i)
+      if (T.act[i] == cur) { in_leaves = true; break; }
+    if (!in_leaves && n_avail < kTlMax && top + 2 <= kTlMax + 8) {
+      avail[n_avail++] = cur;
+      int2 ch = make_int2(0, 0);
+      bool known = false;
+      for (int e = 0; e < n - 1; ++e)
+        if (T.exp_node[e] == cur) { ch = make_int2(T.exp_l[e], T.exp_r[e]); known = true; break; }
+      if (!known) ch = ldcg_children(nodes, cur);
+      stack[top++] = ch.x;
+      stack[top++] = ch.y;
     }
   }
-  __syncwarp();
+  // A subset whose partitions all cost >= INF (NaN areas) has no valid split; the reference
+  // would index out of bounds there, this leaves the treelet unchanged.
+  {
+    int vm[kTlMax], vh = 0, vt = 0;
+    bool ok = true;
+    vm[vt++] = (int)full;
+    while (vh < vt && ok) {
+      const int mask = vm[vh++];
+      const int lm = T.part[mask], rm = mask ^ lm;
+      if (lm == 0 || rm == 0 || (lm & ~mask)) { ok = false; break; }
+      if (__popc(lm) > 1) { if (vt >= kTlMax) { ok = false; break; } vm[vt++] = lm; }
+      if (__popc(rm) > 1) { if (vt >= kTlMax) { ok = false; break; } vm[vt++] = rm; }
+    }
+    if (!ok || n_avail != n - 1) return;
+  }
+  int qm[kTlMax], qn[kTlMax];
+  int qh = 0, qt = 0, used = 1;
+  qm[qt] = (int)full;
+  qn[qt++] = avail[0];
+  while (qh < qt) {
+    const int mask = qm[qh], cur = qn[qh];
+    qh++;
+    const int lm = T.part[mask], rm = mask ^ lm;
+    int li, ri;
+    if (__popc(lm) == 1) li = T.act[__ffs(lm) - 1];
+    else { li = avail[used++]; qm[qt] = lm; qn[qt++] = li; }
+    if (__popc(rm) == 1) ri = T.act[__ffs(rm) - 1];
+    else { ri = avail[used++]; qm[qt] = rm; qn[qt++] = ri; }
+    Box b = box_empty();
+    for (int i = 0; i < n; ++i)
+      if ((mask >> i) & 1) b = box_union(b, leaf_box(T, i));
+    float4* p = reinterpret_cast<float4*>(nodes + cur);
+    __stcg(p, b.lo);
+    __stcg(p + 1, b.hi);
+    __stcg(reinterpret_cast<int2*>(&nodes[cur].left), make_int2(li, ri));
+    __stcg(&nodes[li].aux0, cur);
+    __stcg(&nodes[ri].aux0, cur);
+  }
 }
 
 // One refit+optimise pass (kRefitAndOptimize(true)).  Warp-synchronous climb: lanes never
-// leave the loop early so that all 32 can serve each lane's treelet.
-__global__ void __launch_bounds__(128) k_treelet_round(Node* __restrict__ nodes, unsigned long long* __restrict__ slots,
-                                                       const uint32_t* epoch_word, uint32_t round, uint32_t n) {
-  __shared__ TreeletSmem S[4];
+// leave the loop early so that all 32 can serve each lane's treelet DP.  The treelets reached
+// in one iteration are disjoint subtrees (none is an ancestor of another: an ancestor's
+// treelet waits for its children), so their growth and rebuild run on their own lanes at once.
+constexpr int kTlThreads = 64;
+__global__ void __launch_bounds__(kTlThreads) k_treelet_round(Node* __restrict__ nodes,
+                                                              unsigned long long* __restrict__ slots,
+                                                              const uint32_t* epoch_word, uint32_t round, uint32_t n) {
+  __shared__ LaneTreelet S[kTlThreads];
+  __shared__ float s_cost[kTlThreads / 32][1 << kTlMax], s_area[kTlThreads / 32][1 << kTlMax];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool active = i < n;
   int32_t idx = (int32_t)(n - 1 + i);
   const unsigned long long tag = (unsigned long long)(__ldcg(epoch_word) + 1u + round) << 32;
+  LaneTreelet& mine = S[threadIdx.x];
   while (__any_sync(0xffffffffu, active)) {
     bool work = false;
     if (active) {
@@ -239,13 +272,16 @@ __global__ void __launch_bounds__(128) k_treelet_round(Node* __restrict__ nodes,
         }
       }
     }
-    uint32_t ballot = __ballot_sync(0xffffffffu, work);
+    if (work) treelet_grow(nodes, idx, mine);
+    __syncwarp();
+    uint32_t ballot = __ballot_sync(0xffffffffu, work && mine.n >= 2);
     while (ballot) {
-      int src = __ffs(ballot) - 1;
+      const int src = __ffs(ballot) - 1;
       ballot &= ballot - 1;
-      int32_t root = __shfl_sync(0xffffffffu, idx, src);
-      treelet_warp(nodes, root, S[w]);
+      treelet_dp(S[w * 32 + src], s_cost[w], s_area[w]);
     }
+    __syncwarp();
+    if (work) treelet_rebuild(nodes, idx, mine);
     __threadfence();
   }
 }
@@ -253,7 +289,7 @@ __global__ void __launch_bounds__(128) k_treelet_round(Node* __restrict__ nodes,
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st) {
   ScratchLayout L = scratch_layout(ws.cap_n);
   for (int r = 0; r < rounds && r + 1 < (int)kEpochStride; ++r)
-    k_treelet_round<<<div_up(n, 128), 128, 0, st>>>(ws.nodes, ws.slots, ws.scratch + L.epoch, (uint32_t)r, n);
+    k_treelet_round<<<div_up(n, (uint32_t)kTlThreads), kTlThreads, 0, st>>>(ws.nodes, ws.slots, ws.scratch + L.epoch, (uint32_t)r, n);
   return cudaGetLastError();
 }
 
