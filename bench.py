@@ -98,13 +98,14 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
 
 def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0) -> int:
     """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
-    fix-up for 64-bit keys, delta + emission + frontier climb; one per treelet pass; PLOC adds
+    fix-up for 64-bit keys, delta + emission + frontier climb; five per treelet pass (heights,
+    offsets, grouping by height, the level kernel, the fallback check); PLOC adds
     cluster init, 3 per clustering iteration (neighbours, merge, loop control) and the root fix
     (its 30-bit prefix stops after the sort)."""
     if algo == "ploc":
         return 2 + 4 + 1 + 3 * ploc_iterations + 1
     n = 2 + 4 + (1 if bits != 30 else 0) + 3
-    return n + (rounds if algo == "lbvh_plus" else 0)
+    return n + (5 * rounds if algo == "lbvh_plus" else 0)
 
 
 STAGE_KERNELS = {

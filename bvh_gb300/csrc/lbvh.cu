@@ -674,7 +674,7 @@ cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, i
   }
   rec(evs, 4, st);
   if (treelet_rounds > 0 && n >= 2) {
-    e = treelet_rounds_run(ws, n, treelet_rounds, st);
+    e = treelet_rounds_run(ws, n, treelet_rounds, st, fb);
     if (e != cudaSuccess) return e;
   }
   rec(evs, 5, st);

@@ -126,8 +126,9 @@ cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cu
 cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
                           uint32_t n, int lbits, cudaStream_t st);
 
-// Treelet restructuring passes (LBVH+) after emission.
-cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st);
+// Treelet restructuring passes (LBVH+) after emission; fb = the sort's final ping-pong buffer
+// (the other one is scratch).
+cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb);
 
 // Stable sort of ws.keys[0] (64-bit) with implicit indices over `passes` 8-bit digits.
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,

@@ -12,6 +12,10 @@
 //
 // Every warp keeps looping while any lane still climbs.  Lanes that reached a node grow and
 // rebuild their own treelets in parallel; the subset DP of each is done by all 32 lanes.
+#include <algorithm>
+
+#include <cooperative_groups.h>
+
 #include "emit.cuh"
 #include "lbvh.cuh"
 
@@ -233,63 +237,401 @@ __device__ void treelet_rebuild(Node* nodes, int32_t root, LaneTreelet& T) {
   }
 }
 
-// One refit+optimise pass (kRefitAndOptimize(true)).  Warp-synchronous climb: lanes never
-// leave the loop early so that all 32 can serve each lane's treelet DP.  The treelets reached
-// in one iteration are disjoint subtrees (none is an ancestor of another: an ancestor's
-// treelet waits for its children), so their growth and rebuild run on their own lanes at once.
-constexpr int kTlThreads = 64;
-__global__ void __launch_bounds__(kTlThreads) k_treelet_round(Node* __restrict__ nodes,
-                                                              unsigned long long* __restrict__ slots,
-                                                              const uint32_t* epoch_word, uint32_t round, uint32_t n) {
-  __shared__ LaneTreelet S[kTlThreads];
-  __shared__ float s_cost[kTlThreads / 32][1 << kTlMax], s_area[kTlThreads / 32][1 << kTlMax];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool active = i < n;
-  int32_t idx = (int32_t)(n - 1 + i);
-  const unsigned long long tag = (unsigned long long)(__ldcg(epoch_word) + 1u + round) << 32;
-  LaneTreelet& mine = S[threadIdx.x];
-  while (__any_sync(0xffffffffu, active)) {
-    bool work = false;
-    if (active) {
-      if (idx == 0) {
-        active = false;
-      } else {
-        int32_t parent = __ldcg(&nodes[idx].aux0);
-        __threadfence();
-        unsigned long long old = atomicExch(slots + parent, tag | 1u);
-        if ((old & 0xffffffff00000000ull) != tag) {
-          active = false;  // first child to arrive
-        } else {
-          __threadfence();
-          int2 ch = ldcg_children(nodes, parent);
-          Box b = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
-          float4* p = reinterpret_cast<float4*>(nodes + parent);
-          __stcg(p, b.lo);
-          __stcg(p + 1, b.hi);
-          idx = parent;
-          work = true;
-        }
+// ---------------------------------------------------------------------------------------
+// Level-synchronous pass.  Any children-before-parent order gives the same tree, and nodes of
+// equal height have disjoint subtrees (neither is an ancestor of the other), so each height
+// is one parallel step: every lane owns one treelet and does its refit, growth, DP and rebuild
+// alone, so the 32 lanes of a warp run the same 7-leaf work in step.  Heights come from a
+// climb that carries them in the rendezvous words; node ids are then grouped by height.
+// Trees higher than kTlMaxHeight (not reachable by a Karras tree: its depth is at most the
+// key bits plus 32) fall back to the climb-ordered kernel above.
+// ---------------------------------------------------------------------------------------
+constexpr int kTlMaxHeight = 254;
+constexpr int kLvThreads = 32;  // one warp per block; its DP tables are 20 KB of shared memory
+
+// A lane's treelet in registers (all indexing below is unrolled to constant indices).
+struct RegTreelet {
+  Box b[kTlMax];
+  int32_t id[kTlMax], cl[kTlMax], cr[kTlMax];
+  float area[kTlMax];
+  int32_t en[kTlMax - 1], el[kTlMax - 1], er[kTlMax - 1];  // expansions: node and its children
+  int n;
+};
+
+__device__ __forceinline__ void reg_set(RegTreelet& T, int i, int32_t id, const Box& b, int2 ch) {
+#pragma unroll
+  for (int k = 0; k < kTlMax; ++k)
+    if (k == i) {
+      T.id[k] = id;
+      T.b[k] = b;
+      T.cl[k] = ch.x;
+      T.cr[k] = ch.y;
+      T.area[k] = box_area(b);
+    }
+}
+__device__ __forceinline__ int32_t reg_id(const RegTreelet& T, int i) {
+  int32_t v = 0;
+#pragma unroll
+  for (int k = 0; k < kTlMax; ++k)
+    if (k == i) v = T.id[k];
+  return v;
+}
+__device__ __forceinline__ Box reg_union(const RegTreelet& T, uint32_t mask) {
+  Box b = box_empty();
+#pragma unroll
+  for (int k = 0; k < kTlMax; ++k)
+    if ((mask >> k) & 1u) b = box_union(b, T.b[k]);
+  return b;
+}
+
+// Growth (lbvh_plus_builder.cu:73-114) with each leaf's children and area cached on entry.
+__device__ __forceinline__ void reg_grow(const Node* nodes, int32_t root, const Box& rootbox, int2 rootch,
+                                         RegTreelet& T) {
+  reg_set(T, 0, root, rootbox, rootch);
+  int cnt = 1;
+#pragma unroll
+  for (int step = 0; step < kTlMax - 1; ++step) {
+    int best = -1;
+    float max_area = -1.0f;
+    int32_t bl = 0, br = 0, bn = 0;
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i) {
+      if (i < cnt && !((uint32_t)T.cl[i] & kLeafBit) && T.area[i] > max_area) {
+        max_area = T.area[i];
+        best = i;
+        bl = T.cl[i];
+        br = T.cr[i];
+        bn = T.id[i];
       }
     }
-    if (work) treelet_grow(nodes, idx, mine);
-    __syncwarp();
-    uint32_t ballot = __ballot_sync(0xffffffffu, work && mine.n >= 2);
-    while (ballot) {
-      const int src = __ffs(ballot) - 1;
-      ballot &= ballot - 1;
-      treelet_dp(S[w * 32 + src], s_cost[w], s_area[w]);
+    if (best < 0) break;
+    T.en[step] = bn;
+    T.el[step] = bl;
+    T.er[step] = br;
+    const Box lb = ldcg_box(nodes, bl), rb = ldcg_box(nodes, br);
+    const int2 lc = ldcg_children(nodes, bl), rc = ldcg_children(nodes, br);
+    reg_set(T, best, bl, lb, lc);
+    reg_set(T, cnt, br, rb, rc);
+    ++cnt;
+  }
+  T.n = cnt;
+}
+
+// Subset DP (:119-165) by one lane.  Subsets in increasing numeric order (every proper subset
+// comes first); the splits of s are the nonempty subsets p of s minus its lowest member, in
+// increasing order, first minimum kept.  The box of s is (its leaves among 3..6) U (among 0..2).
+// C and P are this lane's columns of the warp's tables (stride 32).
+__device__ __forceinline__ void reg_dp(const RegTreelet& T, float* C, uint8_t* P) {
+  const uint32_t full = (1u << T.n) - 1u;
+  Box lo8[8];
+  lo8[0] = box_empty();
+  lo8[1] = box_union(lo8[0], T.b[0]);
+  lo8[2] = box_union(lo8[0], T.b[1]);
+  lo8[3] = box_union(lo8[1], T.b[1]);
+  lo8[4] = box_union(lo8[0], T.b[2]);
+  lo8[5] = box_union(lo8[1], T.b[2]);
+  lo8[6] = box_union(lo8[2], T.b[2]);
+  lo8[7] = box_union(lo8[3], T.b[2]);
+  for (uint32_t hi = 0; hi * 8u <= full; ++hi) {
+    Box bh = box_empty();
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if ((hi >> j) & 1u) bh = box_union(bh, T.b[3 + j]);
+#pragma unroll
+    for (int lo = 0; lo < 8; ++lo) {
+      const uint32_t s = hi * 8u + (uint32_t)lo;
+      if (s == 0u || s > full) continue;
+      if (__popc(s) == 1) {
+        C[s * 32u] = 0.0f;
+        continue;
+      }
+      const float a = box_area(box_union(bh, lo8[lo]));
+      const uint32_t delta = s & (s - 1u);
+      float best = kTlInf;
+      uint32_t bp = 0xffu;
+      for (uint32_t p = delta & (0u - delta); p; p = (p - delta) & delta) {
+        const float c = __fadd_rn(C[p * 32u], C[(s ^ p) * 32u]);
+        if (c < best) {
+          best = c;
+          bp = p;
+        }
+      }
+      // the reference starts from INF with strict <, so an all-INF subset keeps INF / -1
+      C[s * 32u] = __fadd_rn(best, a);
+      P[s * 32u] = (uint8_t)bp;
     }
-    __syncwarp();
-    if (work) treelet_rebuild(nodes, idx, mine);
-    __threadfence();
   }
 }
 
-cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st) {
+// Id reuse and rebuild (:167-246) by one lane, from the cached expansions.
+__device__ __forceinline__ void reg_rebuild(Node* nodes, int32_t root, const RegTreelet& T, const uint8_t* P) {
+  const int n = T.n;
+  const uint32_t full = (1u << n) - 1u;
+  int avail[kTlMax];
+  int n_avail = 0;
+  int stack[kTlMax + 8];
+  int top = 0;
+  stack[top++] = root;
+  while (top > 0) {
+    const int cur = stack[--top];
+    bool in_leaves = false;
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i)
+      if (i < n && T.id[i] == cur) in_leaves = true;
+    if (!in_leaves && n_avail < kTlMax && top + 2 <= kTlMax + 8) {
+      avail[n_avail++] = cur;
+      int2 ch = make_int2(0, 0);
+      bool known = false;
+#pragma unroll
+      for (int e = 0; e < kTlMax - 1; ++e)
+        if (!known && e < n - 1 && T.en[e] == cur) {
+          ch = make_int2(T.el[e], T.er[e]);
+          known = true;
+        }
+      if (!known) ch = ldcg_children(nodes, cur);
+      stack[top++] = ch.x;
+      stack[top++] = ch.y;
+    }
+  }
+  // a subset with no finite split (NaN areas) leaves the treelet unchanged
+  {
+    int vm[kTlMax], vh = 0, vt = 0;
+    vm[vt++] = (int)full;
+    while (vh < vt) {
+      const int mask = vm[vh++];
+      const int lm = P[mask * 32], rm = mask ^ lm;
+      if (lm == 0 || rm == 0 || (lm & ~mask)) return;
+      if (__popc(lm) > 1) { if (vt >= kTlMax) return; vm[vt++] = lm; }
+      if (__popc(rm) > 1) { if (vt >= kTlMax) return; vm[vt++] = rm; }
+    }
+    if (n_avail != n - 1) return;
+  }
+  int qm[kTlMax], qn[kTlMax];
+  int qh = 0, qt = 0, used = 1;
+  qm[qt] = (int)full;
+  qn[qt++] = avail[0];
+  while (qh < qt) {
+    const int mask = qm[qh], cur = qn[qh];
+    qh++;
+    const int lm = P[mask * 32], rm = mask ^ lm;
+    int li, ri;
+    if (__popc(lm) == 1) li = reg_id(T, __ffs(lm) - 1);
+    else { li = avail[used++]; qm[qt] = lm; qn[qt++] = li; }
+    if (__popc(rm) == 1) ri = reg_id(T, __ffs(rm) - 1);
+    else { ri = avail[used++]; qm[qt] = rm; qn[qt++] = ri; }
+    const Box b = reg_union(T, (uint32_t)mask);
+    float4* p = reinterpret_cast<float4*>(nodes + cur);
+    __stcg(p, b.lo);
+    __stcg(p + 1, b.hi);
+    __stcg(reinterpret_cast<int2*>(&nodes[cur].left), make_int2(li, ri));
+    __stcg(&nodes[li].aux0, cur);
+    __stcg(&nodes[ri].aux0, cur);
+  }
+}
+
+// Heights: a climb from every leaf; the first child to reach a parent leaves its height in the
+// rendezvous word, the second computes the parent's and counts it (warp-aggregated).
+__global__ void __launch_bounds__(256) k_tl_heights(const Node* __restrict__ nodes, unsigned long long* __restrict__ slots,
+                                                    const uint32_t* epoch_word, uint32_t round, uint32_t n,
+                                                    uint8_t* __restrict__ hgt, uint32_t* __restrict__ cnt,
+                                                    uint32_t* __restrict__ flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long tag = (unsigned long long)(__ldcg(epoch_word) + 1u + round) << 32;
+  int32_t idx = (int32_t)(n - 1 + i);
+  uint32_t h = 0;
+  while (idx != 0) {
+    const int32_t parent = __ldcg(&nodes[idx].aux0);
+    const unsigned long long old = atomicExch(slots + parent, tag | h);
+    if ((old & 0xffffffff00000000ull) != tag) return;  // first child to arrive
+    h = 1u + max(h, (uint32_t)old);
+    if (h > (uint32_t)kTlMaxHeight) {
+      atomicOr(flags, 1u);
+      h = kTlMaxHeight + 1;
+    }
+    hgt[parent] = (uint8_t)h;
+    const uint32_t peers = __match_any_sync(__activemask(), h);
+    if ((threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(cnt + h, __popc(peers));
+    idx = parent;
+  }
+}
+
+// off[h] = first list position of height h (exclusive scan of cnt over 256 heights), cursor
+// copy for the scatter, off[256] = total, flags[1] = the largest height.  A total other than
+// the m internal nodes (a malformed tree) hands the pass to the fallback.
+__global__ void __launch_bounds__(256) k_tl_offsets(const uint32_t* __restrict__ cnt, uint32_t m,
+                                                    uint32_t* __restrict__ off, uint32_t* __restrict__ cursor,
+                                                    uint32_t* __restrict__ flags) {
+  __shared__ uint32_t s_w[8];
+  __shared__ uint32_t s_maxh;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) s_maxh = 0;
+  const uint32_t v = cnt[t];
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[w] = x;
+  __syncthreads();
+  if (v) atomicMax(&s_maxh, (uint32_t)t);
+  uint32_t before = 0;
+  for (int k = 0; k < w; ++k) before += s_w[k];
+  off[t] = before + x - v;
+  cursor[t] = before + x - v;
+  if (t == 255) {
+    off[256] = before + x;
+    if (before + x != m) atomicOr(flags, 2u);
+  }
+  __syncthreads();
+  if (t == 0) flags[1] = s_maxh;
+}
+
+// Internal node ids grouped by height (order within a height is irrelevant).
+__global__ void __launch_bounds__(256) k_tl_scatter(const uint8_t* __restrict__ hgt, uint32_t m,
+                                                    uint32_t* __restrict__ cursor, uint32_t* __restrict__ list) {
+  __shared__ uint32_t s_cnt[256], s_base[256];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t h = i < m ? hgt[i] : 0u;
+  const uint32_t rank = i < m ? atomicAdd(&s_cnt[h], 1u) : 0u;
+  __syncthreads();
+  const uint32_t c = s_cnt[threadIdx.x];
+  if (c) s_base[threadIdx.x] = atomicAdd(cursor + threadIdx.x, c);
+  __syncthreads();
+  if (i < m) {
+    const uint32_t pos = s_base[h] + rank;
+    if (pos < m) list[pos] = i;
+  }
+}
+
+// All heights, one grid-wide step each (cooperative launch: every block is resident).
+__global__ void __launch_bounds__(kLvThreads) k_tl_levels(Node* __restrict__ nodes, const uint32_t* __restrict__ list,
+                                                          const uint32_t* __restrict__ off,
+                                                          const uint32_t* __restrict__ flags) {
+  __shared__ float s_cost[(1 << kTlMax) * 32];
+  __shared__ uint8_t s_part[(1 << kTlMax) * 32];
+  if (__ldcg(flags) != 0u) return;  // too high: the fallback pass does the work (uniform)
+  const uint32_t maxh = __ldcg(flags + 1);
+  const int lane = threadIdx.x & 31;
+  float* C = s_cost + lane;
+  uint8_t* P = s_part + lane;
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  for (uint32_t h = 1; h <= maxh; ++h) {
+    const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
+    for (uint32_t k = b + blockIdx.x * kLvThreads + lane; k < e; k += gridDim.x * kLvThreads) {
+      const int32_t x = (int32_t)__ldcg(list + k);
+      const int2 ch = ldcg_children(nodes, x);
+      const Box box = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
+      float4* p = reinterpret_cast<float4*>(nodes + x);
+      __stcg(p, box.lo);
+      __stcg(p + 1, box.hi);
+      RegTreelet T;
+      reg_grow(nodes, x, box, ch, T);
+      if (T.n < 2) continue;
+      reg_dp(T, C, P);
+      reg_rebuild(nodes, x, T, P);
+    }
+    grid.sync();
+  }
+}
+
+// The climb-ordered pass as a fallback for trees higher than kTlMaxHeight: persistent warps
+// take groups of 32 leaves.  Launched every pass; returns at once unless flags[0] is set.
+__global__ void __launch_bounds__(64) k_treelet_fallback(Node* __restrict__ nodes, unsigned long long* __restrict__ slots,
+                                                         const uint32_t* epoch_word, uint32_t round, uint32_t n,
+                                                         const uint32_t* __restrict__ flags) {
+  __shared__ LaneTreelet S[64];
+  __shared__ float s_cost[2][1 << kTlMax], s_area[2][1 << kTlMax];
+  if (__ldcg(flags) == 0u) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned long long tag = (unsigned long long)(__ldcg(epoch_word) + 0x20u + round) << 32;
+  LaneTreelet& mine = S[threadIdx.x];
+  for (uint32_t base = (blockIdx.x * 2 + w) * 32u; base < n; base += gridDim.x * 64u) {
+    const uint32_t i = base + lane;
+    bool active = i < n;
+    int32_t idx = (int32_t)(n - 1 + i);
+    while (__any_sync(0xffffffffu, active)) {
+      bool work = false;
+      if (active) {
+        if (idx == 0) {
+          active = false;
+        } else {
+          int32_t parent = __ldcg(&nodes[idx].aux0);
+          __threadfence();
+          unsigned long long old = atomicExch(slots + parent, tag | 1u);
+          if ((old & 0xffffffff00000000ull) != tag) {
+            active = false;
+          } else {
+            __threadfence();
+            int2 ch = ldcg_children(nodes, parent);
+            Box b = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
+            float4* p = reinterpret_cast<float4*>(nodes + parent);
+            __stcg(p, b.lo);
+            __stcg(p + 1, b.hi);
+            idx = parent;
+            work = true;
+          }
+        }
+      }
+      if (work) treelet_grow(nodes, idx, mine);
+      __syncwarp();
+      uint32_t ballot = __ballot_sync(0xffffffffu, work && mine.n >= 2);
+      while (ballot) {
+        const int src = __ffs(ballot) - 1;
+        ballot &= ballot - 1;
+        treelet_dp(S[w * 32 + src], s_cost[w], s_area[w]);
+      }
+      __syncwarp();
+      if (work) treelet_rebuild(nodes, idx, mine);
+      __threadfence();
+    }
+  }
+}
+
+static int g_level_grid[64] = {};  // co-resident blocks of k_tl_levels per device
+
+cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb) {
+  if (n < 2) return cudaSuccess;
   ScratchLayout L = scratch_layout(ws.cap_n);
-  for (int r = 0; r < rounds && r + 1 < (int)kEpochStride; ++r)
-    k_treelet_round<<<div_up(n, (uint32_t)kTlThreads), kTlThreads, 0, st>>>(ws.nodes, ws.slots, ws.scratch + L.epoch, (uint32_t)r, n);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!g_level_grid[dev]) {
+    int per_sm = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_levels, kLvThreads, 0)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return e;
+    g_level_grid[dev] = std::max(1, per_sm * sms);
+  }
+  // scratch: heights in the delta bytes (emission is done with them), the id list in the idle
+  // value buffer, counters / offsets / flags in the sort histogram words
+  uint8_t* hgt = ws.delta;
+  uint32_t* list = ws.vals[fb ^ 1];
+  uint32_t* cnt = ws.scratch + L.hist;       // 256
+  uint32_t* off = cnt + 256;                 // 257
+  uint32_t* cursor = off + 264;              // 256
+  uint32_t* flags = cursor + 256;            // [0] too high, [1] largest height
+  const uint32_t* epoch = ws.scratch + L.epoch;
+  for (int r = 0; r < rounds && r + 1 < 0x20; ++r) {
+    if ((e = cudaMemsetAsync(cnt, 0, 256 * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(flags, 0, 2 * 4, st)) != cudaSuccess) return e;
+    k_tl_heights<<<div_up(n, 256), 256, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, hgt, cnt, flags);
+    k_tl_offsets<<<1, 256, 0, st>>>(cnt, n - 1, off, cursor, flags);
+    k_tl_scatter<<<div_up(n - 1, 256), 256, 0, st>>>(hgt, n - 1, cursor, list);
+    Node* nodes = ws.nodes;
+    const uint32_t* clist = list;
+    const uint32_t* coff = off;
+    const uint32_t* cflags = flags;
+    void* args[] = {(void*)&nodes, (void*)&clist, (void*)&coff, (void*)&cflags};
+    if ((e = cudaLaunchCooperativeKernel((const void*)k_tl_levels, dim3(g_level_grid[dev]), dim3(kLvThreads), args, 0,
+                                         st)) != cudaSuccess)
+      return e;
+    k_treelet_fallback<<<152 * 8, 64, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, flags);
+  }
   return cudaGetLastError();
 }
 
