@@ -236,7 +236,8 @@ def run_ours(args):
     n = mesh.size()
     algo_id = {"lbvh": C.ALGO_LBVH, "lbvh_plus": C.ALGO_LBVH_PLUS, "ploc": C.ALGO_PLOC}[algo]
     ctx = bvh_gb300.Context(local)
-    params = ctx.params(algo_id, morton_bits=bits, ploc_radius=radius or 25)
+    params = ctx.params(algo_id, morton_bits=bits, ploc_radius=radius or 25,
+                        ploc_host_loop=getattr(args, "ploc_host_loop", False))
     d_in = [torch.from_numpy(a).to(dev) for a in mesh.arrays()]
     ptrs = [t.data_ptr() for t in d_in]
     stream = torch.cuda.Stream(device=dev)
@@ -597,6 +598,8 @@ def run_reference(args):
     def once():
         if algo == "ploc":
             nodes, idx, it, ms, rc = R.ploc(arrays, radius)
+            once.ploc_stages = {"init_incl_upload": float(ms[1]), "neighbour_search": float(ms[2]),
+                                "merge": float(ms[3]), "scan_compact": float(ms[4]), "iterations": int(it)}
             return ms[0], ms[5]
         if algo == "lbvh_plus":
             nodes, idx, ms = R.lbvh_plus(arrays)
@@ -637,6 +640,8 @@ def run_reference(args):
                          "sample": f"whole workload on the GPU, {args.steps} builds (the reference path is CUDA)"},
         "clocks": clk.summary(),
     }
+    if getattr(once, "ploc_stages", None):
+        line["stage_ms_last"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in once.ploc_stages.items()}
     if getattr(once, "stages", None):
         line["stage_ms_last"] = dict(zip(["bounds", "morton", "sort", "topology", "refit"],
                                          [round(x, 4) for x in once.stages]))
@@ -652,6 +657,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c1_lbvh63")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default sort variants")
+    ap.add_argument("--ploc-host-loop", action="store_true",
+                    help="PLOC: drive the clustering loop from the host (for profilers; slower)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

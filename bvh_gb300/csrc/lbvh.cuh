@@ -30,6 +30,13 @@ struct Workspace {
   int32_t* nbr = nullptr;
   uint32_t ploc_cap = 0;
   cudaGraphExec_t ploc_exec = nullptr;  // clustering loop graph, valid for the key below
+  uint32_t* ploc_host = nullptr;        // pinned word for the host-driven loop
+  cudaGraphExec_t tl_exec = nullptr;    // LBVH+ loop over heights, valid for the key below
+  uint32_t tl_key_n = 0;
+  const void* tl_key_nodes = nullptr;
+  const void* tl_key_list = nullptr;
+  const void* tl_key_desc = nullptr;
+  const void* tl_key_ctl = nullptr;
   uint32_t ploc_key_n = 0;
   int ploc_key_r = 0;
   const void* ploc_key_nodes = nullptr;
@@ -95,7 +102,7 @@ cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int morton_
 // the PLOC control words (kPlocIterWord, kPlocSumWord) and a loop that cannot finish sets
 // kStatusNoProgress.
 cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter,
-                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices);
+                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices, bool host_loop = false);
 constexpr int kPlocIterWord = 6;
 constexpr int kPlocSumWord = 8;
 

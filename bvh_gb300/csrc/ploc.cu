@@ -25,7 +25,7 @@ constexpr int kPlocTile = kPlocThreads * kPlocIpt;
 // control words (scratch + L.ploc):
 //   [0] live clusters  [1] next node id  [2] merge tile counter  [3] buffer parity
 //   [4] survivors (next iteration)  [5] next node id (next iteration)  [6] iterations  [7] cap
-//   [8..9] sum of live clusters over iterations (64-bit)
+//   [8..9] sum of live clusters over iterations (64-bit)  [10] go on (host-driven loop)
 struct PlocBufs {
   Box* cbox[2];
   int32_t* cid[2];
@@ -62,54 +62,95 @@ __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __rest
   reinterpret_cast<int4*>(np + 2)[0] = make_int4((int32_t)(prim | kLeafBit), -1, 0, 0);
 }
 
-// Nearest neighbour in the +-r window, one 256-cluster tile per block iteration, the window
-// staged in shared memory.  Also clears the merge kernel's look-back words and tile counter.
+// Nearest neighbour in the +-r window (:173-209): the smallest union area, the smallest j on
+// ties; areas that are NaN or infinite never win.  The area of a pair is symmetric (fminf/fmaxf
+// commute), so each pair is evaluated once: the thread of cluster x scans x+1..x+r, keeps x's
+// best in registers and offers (area, x) to cluster j through a 64-bit shared-memory atomicMin
+// on (area bits, index) -- for non-negative floats the bit order is the value order, so the
+// minimum is exactly the reference's choice.  The r clusters before a tile ("halo") only make
+// offers; their rows are spread over all warps.  Tiles of kNnTile clusters (kNnPer per thread)
+// with the window staged in shared memory.  Also clears the merge kernel's look-back words and
+// tile counter.
+constexpr int kNnPer = 4;
+constexpr int kNnTile = kPlocThreads * kNnPer;
+
+__device__ __forceinline__ float pair_area(float4 xa, float4 xb, float4 ja, float4 jb) {
+  return sa_xyz(__fsub_rn(fmaxf(xb.x, jb.x), fminf(xa.x, ja.x)), __fsub_rn(fmaxf(xb.y, jb.y), fminf(xa.y, ja.y)),
+                __fsub_rn(fmaxf(xb.z, jb.z), fminf(xa.z, ja.z)));
+}
+
 __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
-  extern __shared__ float sb[];  // 6 planes of (kPlocThreads + 2r) floats
+  extern __shared__ float4 sw[];  // (kNnTile + 2r) boxes as lo, hi float4 pairs
+  unsigned long long* s_back = reinterpret_cast<unsigned long long*>(sw + 2 * (kNnTile + 2 * r));
   const uint32_t c = __ldcg(B.ctrl + 0);
   const Box* __restrict__ cbox = B.cbox[__ldcg(B.ctrl + 3) & 1u];
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t mtiles = div_up(c, kPlocTile);
   for (uint32_t w = gtid; w < mtiles; w += gridDim.x * blockDim.x) B.desc[w] = 0ull;
   if (gtid == 0) B.ctrl[2] = 0;
-  const int span = kPlocThreads + 2 * r;
-  for (int64_t base = (int64_t)blockIdx.x * kPlocThreads; base < (int64_t)c; base += (int64_t)gridDim.x * kPlocThreads) {
-    const int64_t lo = base - r;
-    __syncthreads();  // previous tile's window no longer read
-    for (int k = threadIdx.x; k < span; k += blockDim.x) {
-      int64_t j = lo + k;
-      if (j >= 0 && j < (int64_t)c) {
+  const int span = kNnTile + 2 * r;
+  const int t = threadIdx.x;
+  const float kInf = __int_as_float(0x7f800000);
+  for (uint32_t base = blockIdx.x * (uint32_t)kNnTile; base < c; base += gridDim.x * (uint32_t)kNnTile) {
+    const int lo = (int)base - r;  // window position 0; may be negative
+    const int tile_n = (int)min((uint32_t)kNnTile, c - base);
+    __syncthreads();  // previous tile's window and offers no longer read
+    for (int k = t; k < span; k += kPlocThreads) {
+      const int j = lo + k;
+      if (j >= 0 && j < (int)c) {
         const float4* bp = reinterpret_cast<const float4*>(cbox + j);
-        float4 a = __ldcg(bp), b = __ldcg(bp + 1);
-        sb[0 * span + k] = a.x; sb[1 * span + k] = a.y; sb[2 * span + k] = a.z;
-        sb[3 * span + k] = b.x; sb[4 * span + k] = b.y; sb[5 * span + k] = b.z;
+        sw[2 * k] = __ldcg(bp);
+        sw[2 * k + 1] = __ldcg(bp + 1);
+      }
+    }
+    for (int k = t; k < kNnTile; k += kPlocThreads) s_back[k] = ~0ull;
+    __syncthreads();
+    float bd[kNnPer];
+    int bj[kNnPer];
+#pragma unroll
+    for (int m = 0; m < kNnPer; ++m) {
+      bd[m] = kInf;  // only finite areas are candidates
+      bj[m] = -1;
+      const int xi = t + m * kPlocThreads;  // tile-relative
+      if (xi < tile_n) {
+        const int xw = xi + r;  // window-relative
+        const float4 xa = sw[2 * xw], xb = sw[2 * xw + 1];
+        const int last = min(r, (int)c - 1 - ((int)base + xi));  // forward offsets 1..last
+        for (int k = 1; k <= last; ++k) {
+          const float d = pair_area(xa, xb, sw[2 * (xw + k)], sw[2 * (xw + k) + 1]);
+          if (d < bd[m]) {  // increasing j: the first of equal areas stays
+            bd[m] = d;
+            bj[m] = (int)base + xi + k;
+          }
+          if (xi + k < tile_n && d < kInf)
+            atomicMin(s_back + xi + k, ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)((int)base + xi));
+        }
+      }
+    }
+    // halo clusters lo + hw (hw < r) offer to the tile's first clusters; row hw goes to thread
+    // hw * 256 / r, spreading the rows over all warps
+    for (int hw = (t * r + kPlocThreads - 1) / kPlocThreads; hw < r && (hw * kPlocThreads) / r == t; ++hw) {
+      const int h = lo + hw;
+      if (h >= 0) {
+        const float4 ha = sw[2 * hw], hb = sw[2 * hw + 1];
+        const int last = min(hw, tile_n - 1);  // tile-relative targets 0..last (offsets r-hw .. r)
+        for (int jj = 0; jj <= last; ++jj) {
+          const float d = pair_area(ha, hb, sw[2 * (jj + r)], sw[2 * (jj + r) + 1]);
+          if (d < kInf) atomicMin(s_back + jj, ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)h);
+        }
       }
     }
     __syncthreads();
-    const int64_t i = base + threadIdx.x;
-    if (i >= (int64_t)c) continue;
-    const int li = (int)(i - lo);
-    const float ax = sb[li], ay = sb[span + li], az = sb[2 * span + li];
-    const float bx = sb[3 * span + li], by = sb[4 * span + li], bz = sb[5 * span + li];
-    const int64_t s = i - r < 0 ? 0 : i - r;
-    const int64_t e = i + r > (int64_t)c - 1 ? (int64_t)c - 1 : i + r;
-    float best = FLT_MAX;
-    int64_t bj = -1;
-    for (int64_t j = s; j <= e; ++j) {
-      if (j == i) continue;
-      const int lj = (int)(j - lo);
-      float x = __fsub_rn(fmaxf(bx, sb[3 * span + lj]), fminf(ax, sb[lj]));
-      float y = __fsub_rn(fmaxf(by, sb[4 * span + lj]), fminf(ay, sb[span + lj]));
-      float z = __fsub_rn(fmaxf(bz, sb[5 * span + lj]), fminf(az, sb[2 * span + lj]));
-      float d = sa_xyz(x, y, z);
-      if (d < best) {
-        best = d;
-        bj = j;
-      } else if (d == best) {
-        if (bj == -1 || j < bj) bj = j;
+#pragma unroll
+    for (int m = 0; m < kNnPer; ++m) {
+      const int xi = t + m * kPlocThreads;
+      if (xi < tile_n) {
+        const unsigned long long o = s_back[xi];
+        int j = bj[m];
+        if (o != ~0ull && __uint_as_float((uint32_t)(o >> 32)) <= bd[m]) j = (int)(uint32_t)o;  // earlier index wins ties
+        B.nbr[base + xi] = j;
       }
     }
-    B.nbr[i] = (int32_t)bj;
   }
 }
 
@@ -229,7 +270,9 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_merge(PlocBufs B) {
   }
 }
 
-// End of one iteration: publish the survivors, swap buffers, decide whether to go on.
+// End of one iteration: publish the survivors, swap buffers, decide whether to go on (the
+// graph's WHILE condition, or ctrl[10] for the host-driven loop).
+template <bool GRAPH>
 __global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const uint32_t c = B.ctrl[0], nc = B.ctrl[4], it = B.ctrl[6] + 1, cap = B.ctrl[7];
@@ -245,7 +288,8 @@ __global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
     atomicOr(B.status, kStatusNoProgress);
     go = false;
   }
-  cudaGraphSetConditional(handle, go ? 1u : 0u);
+  if constexpr (GRAPH) cudaGraphSetConditional(handle, go ? 1u : 0u);
+  else B.ctrl[10] = go ? 1u : 0u;
 }
 
 // Move the root (last node) to index 0 and swap every reference to 0 and the root
@@ -297,7 +341,7 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   return cudaSuccess;
 }
 
-static size_t nn_smem(int radius) { return 6 * sizeof(float) * (kPlocThreads + 2 * (size_t)radius); }
+static size_t nn_smem(int radius) { return 32 * (kNnTile + 2 * (size_t)radius) + 8 * (size_t)kNnTile; }
 
 // The loop as a graph: WHILE(cond) { nn; merge; step }.  Grids are persistent (sized for n), the
 // kernels read the live cluster count from the control words.
@@ -321,11 +365,11 @@ static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n,
     if ((e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
       break;
-    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocThreads), 152 * 8));
-    const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 4));
+    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 4));
+    const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
     k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), cs>>>(B, radius);
     k_ploc_merge<<<mg_grid, kPlocThreads, 0, cs>>>(B);
-    k_ploc_step<<<1, 32, 0, cs>>>(B, handle);
+    k_ploc_step<true><<<1, 32, 0, cs>>>(B, handle);
     cudaGraph_t captured = nullptr;
     cudaError_t e2 = cudaGetLastError();
     e = cudaStreamEndCapture(cs, &captured);
@@ -339,7 +383,7 @@ static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n,
 }
 
 cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter, cudaStream_t st,
-                       StageEvents* evs, uint32_t** out_indices) {
+                       StageEvents* evs, uint32_t** out_indices, bool host_loop) {
   cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   if ((e = workspace_reserve_ploc(ws, n)) != cudaSuccess) return e;
@@ -362,7 +406,8 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   }
   // every iteration that makes progress removes at least one cluster, so n bounds the loop
   const uint32_t cap = max_iter > 0 ? (uint32_t)max_iter : n;
-  if (n > 1) {
+  if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
+  if (n > 1 && !host_loop) {
     const bool same = ws.ploc_exec && ws.ploc_key_n == n && ws.ploc_key_r == radius && ws.ploc_key_nodes == ws.nodes &&
                       ws.ploc_key_scratch == ws.scratch;
     if (!same) {
@@ -381,7 +426,20 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   *out_indices = sidx;
   k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap);
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
-  if (n > 1) {
+  if (n > 1 && host_loop) {
+    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 4));
+    const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
+    for (uint32_t it = 0; it < cap; ++it) {
+      k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), st>>>(B, radius);
+      k_ploc_merge<<<mg_grid, kPlocThreads, 0, st>>>(B);
+      k_ploc_step<false><<<1, 32, 0, st>>>(B, cudaGraphConditionalHandle{});
+      if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+      if (!*ws.ploc_host) break;
+    }
+    k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
+  } else if (n > 1) {
     if ((e = cudaGraphLaunch(ws.ploc_exec, st)) != cudaSuccess) return e;
     k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
   }

@@ -14,8 +14,6 @@
 // rebuild their own treelets in parallel; the subset DP of each is done by all 32 lanes.
 #include <algorithm>
 
-#include <cooperative_groups.h>
-
 #include "emit.cuh"
 #include "lbvh.cuh"
 
@@ -284,9 +282,27 @@ __device__ __forceinline__ Box reg_union(const RegTreelet& T, uint32_t mask) {
   return b;
 }
 
+// Growth state without the leaf boxes (only their areas are compared).
+struct GrowTreelet {
+  int32_t id[kTlMax], cl[kTlMax], cr[kTlMax];
+  float area[kTlMax];
+  int32_t en[kTlMax - 1], el[kTlMax - 1], er[kTlMax - 1];
+  int n;
+};
+__device__ __forceinline__ void reg_set(GrowTreelet& T, int i, int32_t id, const Box& b, int2 ch) {
+#pragma unroll
+  for (int k = 0; k < kTlMax; ++k)
+    if (k == i) {
+      T.id[k] = id;
+      T.cl[k] = ch.x;
+      T.cr[k] = ch.y;
+      T.area[k] = box_area(b);
+    }
+}
+
 // Growth (lbvh_plus_builder.cu:73-114) with each leaf's children and area cached on entry.
-__device__ __forceinline__ void reg_grow(const Node* nodes, int32_t root, const Box& rootbox, int2 rootch,
-                                         RegTreelet& T) {
+template <typename TL>
+__device__ __forceinline__ void reg_grow(const Node* nodes, int32_t root, const Box& rootbox, int2 rootch, TL& T) {
   reg_set(T, 0, root, rootbox, rootch);
   int cnt = 1;
 #pragma unroll
@@ -363,11 +379,11 @@ __device__ __forceinline__ void reg_dp(const RegTreelet& T, float* C, uint8_t* P
   }
 }
 
-// Id reuse and rebuild (:167-246) by one lane, from the cached expansions.
-__device__ __forceinline__ void reg_rebuild(Node* nodes, int32_t root, const RegTreelet& T, const uint8_t* P) {
+// Id reuse (:167-191): the treelet's internal nodes in DFS order from the root, right child
+// popped first, from the cached expansions.  Returns how many were found.
+template <typename TL>
+__device__ __forceinline__ int reg_avail(const Node* nodes, int32_t root, const TL& T, int* avail) {
   const int n = T.n;
-  const uint32_t full = (1u << n) - 1u;
-  int avail[kTlMax];
   int n_avail = 0;
   int stack[kTlMax + 8];
   int top = 0;
@@ -393,7 +409,16 @@ __device__ __forceinline__ void reg_rebuild(Node* nodes, int32_t root, const Reg
       stack[top++] = ch.y;
     }
   }
-  // a subset with no finite split (NaN areas) leaves the treelet unchanged
+  return n_avail;
+}
+
+// Rebuild (:194-246) from the partitions P (this lane's column, stride 32), breadth-first,
+// handing out the reused ids in order.  A subset with no finite split (NaN areas) leaves the
+// treelet unchanged.
+__device__ __forceinline__ void reg_build(Node* nodes, const RegTreelet& T, const uint8_t* P, const int* avail,
+                                          int n_avail) {
+  const int n = T.n;
+  const uint32_t full = (1u << n) - 1u;
   {
     int vm[kTlMax], vh = 0, vt = 0;
     vm[vt++] = (int)full;
@@ -485,7 +510,10 @@ __global__ void __launch_bounds__(256) k_tl_offsets(const uint32_t* __restrict__
     if (before + x != m) atomicOr(flags, 2u);
   }
   __syncthreads();
-  if (t == 0) flags[1] = s_maxh;
+  if (t == 0) {
+    flags[1] = s_maxh;
+    flags[2] = 1;  // the first height processed
+  }
 }
 
 // Internal node ids grouped by height (order within a height is irrelevant).
@@ -507,35 +535,79 @@ __global__ void __launch_bounds__(256) k_tl_scatter(const uint8_t* __restrict__ 
   }
 }
 
-// All heights, one grid-wide step each (cooperative launch: every block is resident).
-__global__ void __launch_bounds__(kLvThreads) k_tl_levels(Node* __restrict__ nodes, const uint32_t* __restrict__ list,
+// Per height, two kernels: k_tl_grow (latency-bound: many warps, few registers) refits each
+// node, grows its treelet and writes a descriptor; k_tl_dp (compute-bound) reloads the leaf
+// boxes, runs the DP and rebuilds.  Descriptors are structure-of-arrays, kTlDescWords words per
+// node at stride `stride` (>= the largest height's node count): [0] n | n_avail << 8,
+// [1..7] leaf ids, [8..13] reused internal ids in order.  ctl: [0] too high, [1] largest
+// height, [2] current height.
+constexpr int kTlDescWords = 14;
+constexpr int kGrowThreads = 128;
+
+__global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ nodes, const uint32_t* __restrict__ list,
                                                           const uint32_t* __restrict__ off,
-                                                          const uint32_t* __restrict__ flags) {
+                                                          const uint32_t* __restrict__ ctl, uint32_t* __restrict__ desc,
+                                                          uint32_t stride) {
+  if (__ldcg(ctl) != 0u) return;  // too high: the fallback pass does the work
+  const uint32_t h = __ldcg(ctl + 2);
+  const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
+  for (uint32_t k = b + blockIdx.x * blockDim.x + threadIdx.x; k < e; k += gridDim.x * blockDim.x) {
+    const int32_t x = (int32_t)__ldcg(list + k);
+    const int2 ch = ldcg_children(nodes, x);
+    const Box box = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
+    float4* p = reinterpret_cast<float4*>(nodes + x);
+    __stcg(p, box.lo);
+    __stcg(p + 1, box.hi);
+    GrowTreelet T;
+    reg_grow(nodes, x, box, ch, T);
+    int avail[kTlMax];
+    const int na = T.n >= 2 ? reg_avail(nodes, x, T, avail) : 0;
+    const uint32_t q = k - b;
+    desc[q] = (uint32_t)T.n | ((uint32_t)na << 8);
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i) desc[(size_t)(1 + i) * stride + q] = (uint32_t)T.id[i];
+#pragma unroll
+    for (int i = 0; i < kTlMax - 1; ++i) desc[(size_t)(8 + i) * stride + q] = i < na ? (uint32_t)avail[i] : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, const uint32_t* __restrict__ off,
+                                                      const uint32_t* __restrict__ ctl,
+                                                      const uint32_t* __restrict__ desc, uint32_t stride) {
   __shared__ float s_cost[(1 << kTlMax) * 32];
   __shared__ uint8_t s_part[(1 << kTlMax) * 32];
-  if (__ldcg(flags) != 0u) return;  // too high: the fallback pass does the work (uniform)
-  const uint32_t maxh = __ldcg(flags + 1);
+  if (__ldcg(ctl) != 0u) return;
+  const uint32_t h = __ldcg(ctl + 2);
+  const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
   const int lane = threadIdx.x & 31;
   float* C = s_cost + lane;
   uint8_t* P = s_part + lane;
-  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
-  for (uint32_t h = 1; h <= maxh; ++h) {
-    const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
-    for (uint32_t k = b + blockIdx.x * kLvThreads + lane; k < e; k += gridDim.x * kLvThreads) {
-      const int32_t x = (int32_t)__ldcg(list + k);
-      const int2 ch = ldcg_children(nodes, x);
-      const Box box = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
-      float4* p = reinterpret_cast<float4*>(nodes + x);
-      __stcg(p, box.lo);
-      __stcg(p + 1, box.hi);
-      RegTreelet T;
-      reg_grow(nodes, x, box, ch, T);
-      if (T.n < 2) continue;
-      reg_dp(T, C, P);
-      reg_rebuild(nodes, x, T, P);
+  for (uint32_t k = b + blockIdx.x * kLvThreads + lane; k < e; k += gridDim.x * kLvThreads) {
+    const uint32_t q = k - b;
+    const uint32_t w0 = __ldcg(desc + q);
+    RegTreelet T;
+    T.n = (int)(w0 & 255u);
+    if (T.n < 2) continue;
+    const int na = (int)(w0 >> 8);
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i) {
+      T.id[i] = (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q);
+      T.b[i] = i < T.n ? ldcg_box(nodes, T.id[i]) : box_empty();
     }
-    grid.sync();
+    int avail[kTlMax];
+#pragma unroll
+    for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
+    reg_dp(T, C, P);
+    reg_build(nodes, T, P, avail, na);
   }
+}
+
+// End of a height: the next one, and whether the loop goes on.
+__global__ void k_tl_step(uint32_t* __restrict__ ctl, cudaGraphConditionalHandle handle) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t h = ctl[2] + 1;
+  ctl[2] = h;
+  cudaGraphSetConditional(handle, (ctl[0] == 0u && h <= ctl[1]) ? 1u : 0u);
 }
 
 // The climb-ordered pass as a fallback for trees higher than kTlMaxHeight: persistent warps
@@ -591,7 +663,45 @@ __global__ void __launch_bounds__(64) k_treelet_fallback(Node* __restrict__ node
   }
 }
 
-static int g_level_grid[64] = {};  // co-resident blocks of k_tl_levels per device
+static int g_dp_grid[64] = {};  // resident blocks of k_tl_dp per device
+
+// The loop over heights as a graph: WHILE(cond) { grow; dp; step }.
+static cudaError_t make_height_graph(Node* nodes, const uint32_t* list, const uint32_t* off, uint32_t* ctl,
+                                     uint32_t* desc, uint32_t stride, uint32_t grow_grid, uint32_t dp_grid,
+                                     cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaStream_t cs = nullptr;
+  do {
+    cudaGraphConditionalHandle handle;
+    if ((e = cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp)) != cudaSuccess) break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+      break;
+    k_tl_grow<<<grow_grid, kGrowThreads, 0, cs>>>(nodes, list, off, ctl, desc, stride);
+    k_tl_dp<<<dp_grid, kLvThreads, 0, cs>>>(nodes, off, ctl, desc, stride);
+    k_tl_step<<<1, 32, 0, cs>>>(ctl, handle);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t e2 = cudaGetLastError();
+    e = cudaStreamEndCapture(cs, &captured);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) break;
+    e = cudaGraphInstantiate(out, g, 0);
+  } while (false);
+  if (cs) cudaStreamDestroy(cs);
+  cudaGraphDestroy(g);
+  return e;
+}
 
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb) {
   if (n < 2) return cudaSuccess;
@@ -600,37 +710,48 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!g_level_grid[dev]) {
-    int per_sm = 0, sms = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_levels, kLvThreads, 0)) != cudaSuccess ||
-        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-      return e;
-    g_level_grid[dev] = std::max(1, per_sm * sms);
+  int sms = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if (!g_dp_grid[dev]) {
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_dp, kLvThreads, 0)) != cudaSuccess) return e;
+    g_dp_grid[dev] = std::max(1, per_sm * sms);
   }
   // scratch: heights in the delta bytes (emission is done with them), the id list in the idle
-  // value buffer, counters / offsets / flags in the sort histogram words
+  // value buffer, descriptors in the triangle boxes (32 B per triangle; a height has at most
+  // n/2 nodes), counters / offsets / control words in the sort histogram words
   uint8_t* hgt = ws.delta;
   uint32_t* list = ws.vals[fb ^ 1];
+  uint32_t* desc = reinterpret_cast<uint32_t*>(ws.boxes);
+  const uint32_t stride = std::max<uint32_t>(n / 2, 1);
   uint32_t* cnt = ws.scratch + L.hist;       // 256
   uint32_t* off = cnt + 256;                 // 257
   uint32_t* cursor = off + 264;              // 256
-  uint32_t* flags = cursor + 256;            // [0] too high, [1] largest height
+  uint32_t* ctl = cursor + 256;              // [0] too high, [1] largest height, [2] current height
   const uint32_t* epoch = ws.scratch + L.epoch;
+  const bool same = ws.tl_exec && ws.tl_key_n == n && ws.tl_key_nodes == ws.nodes && ws.tl_key_list == list &&
+                    ws.tl_key_desc == desc && ws.tl_key_ctl == ctl;
+  if (!same) {
+    if (ws.tl_exec) cudaGraphExecDestroy(ws.tl_exec);
+    ws.tl_exec = nullptr;
+    const uint32_t grow_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(stride, kGrowThreads), sms * 16));
+    if ((e = make_height_graph(ws.nodes, list, off, ctl, desc, stride, grow_grid, (uint32_t)g_dp_grid[dev],
+                               &ws.tl_exec)) != cudaSuccess)
+      return e;
+    ws.tl_key_n = n;
+    ws.tl_key_nodes = ws.nodes;
+    ws.tl_key_list = list;
+    ws.tl_key_desc = desc;
+    ws.tl_key_ctl = ctl;
+  }
   for (int r = 0; r < rounds && r + 1 < 0x20; ++r) {
     if ((e = cudaMemsetAsync(cnt, 0, 256 * 4, st)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(flags, 0, 2 * 4, st)) != cudaSuccess) return e;
-    k_tl_heights<<<div_up(n, 256), 256, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, hgt, cnt, flags);
-    k_tl_offsets<<<1, 256, 0, st>>>(cnt, n - 1, off, cursor, flags);
+    if ((e = cudaMemsetAsync(ctl, 0, 4 * 4, st)) != cudaSuccess) return e;
+    k_tl_heights<<<div_up(n, 256), 256, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, hgt, cnt, ctl);
+    k_tl_offsets<<<1, 256, 0, st>>>(cnt, n - 1, off, cursor, ctl);
     k_tl_scatter<<<div_up(n - 1, 256), 256, 0, st>>>(hgt, n - 1, cursor, list);
-    Node* nodes = ws.nodes;
-    const uint32_t* clist = list;
-    const uint32_t* coff = off;
-    const uint32_t* cflags = flags;
-    void* args[] = {(void*)&nodes, (void*)&clist, (void*)&coff, (void*)&cflags};
-    if ((e = cudaLaunchCooperativeKernel((const void*)k_tl_levels, dim3(g_level_grid[dev]), dim3(kLvThreads), args, 0,
-                                         st)) != cudaSuccess)
-      return e;
-    k_treelet_fallback<<<152 * 8, 64, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, flags);
+    if ((e = cudaGraphLaunch(ws.tl_exec, st)) != cudaSuccess) return e;
+    k_treelet_fallback<<<sms * 8, 64, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, ctl);
   }
   return cudaGetLastError();
 }

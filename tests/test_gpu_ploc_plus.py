@@ -53,13 +53,27 @@ def test_ploc_canonical_vs_reference_kernels(ctx, gpu, name):
     assert ctx.last_timing().ploc_iterations == rit
 
 
+@pytest.mark.parametrize("radius", [1, 25, 100])
+@pytest.mark.parametrize("name", ["uniform3", "uniform4097", "clumped5000", "clustered20000"])
+def test_ploc_host_driven_loop_equals_graph_loop(ctx, gpu, oracle_lib, name, radius):
+    m = CASES[name]
+    g_nodes, g_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_PLOC, ploc_radius=radius))
+    g_it = ctx.last_timing().ploc_iterations
+    h_nodes, h_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_PLOC, ploc_radius=radius, ploc_host_loop=True))
+    t = ctx.last_timing()
+    assert np.array_equal(g_idx, h_idx)
+    assert oracle_lib.node_fields_equal(g_nodes, h_nodes)
+    assert t.ploc_iterations == g_it
+
+
 def test_ploc_nan_mesh_reports_no_progress(ctx, gpu):
     m = meshgen.uniform_small(64, seed=1)
     for a in m.arrays():
         a[:] = np.nan
-    with pytest.raises(C.BVHError) as e:
-        ctx.build_host(m, ctx.params(C.ALGO_PLOC, ploc_radius=4))
-    assert e.value.status == C.BVH_ERR_NO_PROGRESS
+    for host_loop in (False, True):
+        with pytest.raises(C.BVHError) as e:
+            ctx.build_host(m, ctx.params(C.ALGO_PLOC, ploc_radius=4, ploc_host_loop=host_loop))
+        assert e.value.status == C.BVH_ERR_NO_PROGRESS
 
 
 @pytest.mark.parametrize("rounds", [1, 3])
