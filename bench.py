@@ -237,7 +237,7 @@ def run_ours(args):
     algo_id = {"lbvh": C.ALGO_LBVH, "lbvh_plus": C.ALGO_LBVH_PLUS, "ploc": C.ALGO_PLOC}[algo]
     ctx = bvh_gb300.Context(local)
     params = ctx.params(algo_id, morton_bits=bits, ploc_radius=radius or 25,
-                        ploc_host_loop=getattr(args, "ploc_host_loop", False))
+                        host_loops=getattr(args, "host_loops", False))
     d_in = [torch.from_numpy(a).to(dev) for a in mesh.arrays()]
     ptrs = [t.data_ptr() for t in d_in]
     stream = torch.cuda.Stream(device=dev)
@@ -657,8 +657,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c1_lbvh63")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default sort variants")
-    ap.add_argument("--ploc-host-loop", action="store_true",
-                    help="PLOC: drive the clustering loop from the host (for profilers; slower)")
+    ap.add_argument("--host-loops", action="store_true",
+                    help="drive the PLOC / LBVH+ device loops from the host (for profilers; slower)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -70,7 +70,7 @@ class Batch(ctypes.Structure):
 
 
 BATCH_USE_GRAPH = 1
-PLOC_HOST_LOOP = 1  # bvh_params.reserved[1]: host-driven PLOC loop
+HOST_DRIVEN_LOOPS = 1  # bvh_params.reserved[1]: PLOC / LBVH+ loops driven from the host
 
 
 class Camera(ctypes.Structure):

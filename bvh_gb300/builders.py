@@ -87,10 +87,10 @@ class Context:
 
     def params(self, algo: int, morton_bits: Optional[int] = None, treelet_rounds: Optional[int] = None,
                ploc_radius: Optional[int] = None, max_iterations: Optional[int] = None,
-               ploc_host_loop: bool = False) -> C.Params:
+               host_loops: bool = False) -> C.Params:
         p = self.lib.bvh_default_params(algo)
-        if ploc_host_loop:
-            p.reserved[1] = C.PLOC_HOST_LOOP
+        if host_loops:
+            p.reserved[1] = C.HOST_DRIVEN_LOOPS
         if morton_bits is not None:
             p.morton_bits = morton_bits
         if treelet_rounds is not None:

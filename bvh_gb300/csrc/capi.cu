@@ -173,11 +173,12 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   cudaError_t e;
   if (params->algo == BVH_ALGO_PLOC) {
     e = ploc_build(ctx->ws, m, n, params->ploc_radius, params->max_iterations, st, &ctx->evs, &idx,
-                   params->reserved[1] == BVH_PLOC_HOST_LOOP);
+                   params->reserved[1] == BVH_HOST_DRIVEN_LOOPS);
     if (e != cudaSuccess) return from_cuda(e);
   } else {
     int rounds = params->algo == BVH_ALGO_LBVH_PLUS ? params->treelet_rounds : 0;
-    e = lbvh_build(ctx->ws, m, n, params->morton_bits, rounds, st, &ctx->evs, &idx);
+    e = lbvh_build(ctx->ws, m, n, params->morton_bits, rounds, st, &ctx->evs, &idx,
+                   params->reserved[1] == BVH_HOST_DRIVEN_LOOPS);
     if (e != cudaSuccess) return from_cuda(e);
   }
   ScratchLayout L = scratch_layout(ctx->ws.cap_n);

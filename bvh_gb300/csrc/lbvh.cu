@@ -655,7 +655,7 @@ cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st,
 }
 
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,
-                       StageEvents* evs, uint32_t** out_indices) {
+                       StageEvents* evs, uint32_t** out_indices, bool host_loops) {
   cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(ws.cap_n);
@@ -676,7 +676,7 @@ cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, i
   }
   rec(evs, 4, st);
   if (treelet_rounds > 0 && n >= 2) {
-    e = treelet_rounds_run(ws, n, treelet_rounds, st, fb);
+    e = treelet_rounds_run(ws, n, treelet_rounds, st, fb, host_loops);
     if (e != cudaSuccess) return e;
   }
   rec(evs, 5, st);

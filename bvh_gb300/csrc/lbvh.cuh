@@ -30,7 +30,7 @@ struct Workspace {
   int32_t* nbr = nullptr;
   uint32_t ploc_cap = 0;
   cudaGraphExec_t ploc_exec = nullptr;  // clustering loop graph, valid for the key below
-  uint32_t* ploc_host = nullptr;        // pinned word for the host-driven loop
+  uint32_t* ploc_host = nullptr;        // pinned words for the host-driven loops
   cudaGraphExec_t tl_exec = nullptr;    // LBVH+ loop over heights, valid for the key below
   uint32_t tl_key_n = 0;
   const void* tl_key_nodes = nullptr;
@@ -95,7 +95,7 @@ struct StageEvents {
 // LBVH over device-resident SoA input; result in ws.nodes / ws.vals[final].
 // morton_bits: 30, 60 or 63.  treelet_rounds > 0 selects LBVH+.
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int morton_bits, int treelet_rounds,
-                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices);
+                       cudaStream_t st, StageEvents* evs, uint32_t** out_indices, bool host_loops = false);
 
 // PLOC (radius r) over device-resident SoA input, fully asynchronous (the clustering loop is a
 // CUDA graph WHILE node).  Node count is 2n-1; iterations and the live-cluster sum are left in
@@ -135,7 +135,8 @@ cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned lon
 
 // Treelet restructuring passes (LBVH+) after emission; fb = the sort's final ping-pong buffer
 // (the other one is scratch).
-cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb);
+cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb,
+                               bool host_loop = false);
 
 // Stable sort of ws.keys[0] (64-bit) with implicit indices over `passes` 8-bit digits.
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,

@@ -64,15 +64,17 @@ __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __rest
 
 // Nearest neighbour in the +-r window (:173-209): the smallest union area, the smallest j on
 // ties; areas that are NaN or infinite never win.  The area of a pair is symmetric (fminf/fmaxf
-// commute), so each pair is evaluated once: the thread of cluster x scans x+1..x+r, keeps x's
-// best in registers and offers (area, x) to cluster j through a 64-bit shared-memory atomicMin
-// on (area bits, index) -- for non-negative floats the bit order is the value order, so the
-// minimum is exactly the reference's choice.  The r clusters before a tile ("halo") only make
-// offers; their rows are spread over all warps.  Tiles of kNnTile clusters (kNnPer per thread)
-// with the window staged in shared memory.  Also clears the merge kernel's look-back words and
-// tile counter.
+// commute), so each pair is evaluated once, by the thread of its earlier cluster x: it keeps x's
+// forward best in registers and writes the area into a per-offset table D[k][j] for the later
+// cluster j = x + k, which after a barrier reads its backward candidates from its column (the
+// later offset, i.e. the smaller index, wins ties).  Offsets go in chunks of kNnKc to bound the
+// table.  The r clusters before a tile ("halo") only fill the table; their pairs are spread over
+// all warps.  Tiles of kNnTile clusters (kNnPer per thread, strided so lanes are consecutive),
+// the window staged in shared memory.  Also clears the merge kernel's look-back words and tile
+// counter.
 constexpr int kNnPer = 4;
 constexpr int kNnTile = kPlocThreads * kNnPer;
+constexpr int kNnKc = 5;
 
 __device__ __forceinline__ float pair_area(float4 xa, float4 xb, float4 ja, float4 jb) {
   return sa_xyz(__fsub_rn(fmaxf(xb.x, jb.x), fminf(xa.x, ja.x)), __fsub_rn(fmaxf(xb.y, jb.y), fminf(xa.y, ja.y)),
@@ -81,7 +83,7 @@ __device__ __forceinline__ float pair_area(float4 xa, float4 xb, float4 ja, floa
 
 __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   extern __shared__ float4 sw[];  // (kNnTile + 2r) boxes as lo, hi float4 pairs
-  unsigned long long* s_back = reinterpret_cast<unsigned long long*>(sw + 2 * (kNnTile + 2 * r));
+  float* sD = reinterpret_cast<float*>(sw + 2 * (kNnTile + 2 * r));  // [kNnKc][kNnTile]
   const uint32_t c = __ldcg(B.ctrl + 0);
   const Box* __restrict__ cbox = B.cbox[__ldcg(B.ctrl + 3) & 1u];
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   for (uint32_t base = blockIdx.x * (uint32_t)kNnTile; base < c; base += gridDim.x * (uint32_t)kNnTile) {
     const int lo = (int)base - r;  // window position 0; may be negative
     const int tile_n = (int)min((uint32_t)kNnTile, c - base);
-    __syncthreads();  // previous tile's window and offers no longer read
+    __syncthreads();  // previous tile's window no longer read
     for (int k = t; k < span; k += kPlocThreads) {
       const int j = lo + k;
       if (j >= 0 && j < (int)c) {
@@ -103,53 +105,72 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
         sw[2 * k + 1] = __ldcg(bp + 1);
       }
     }
-    for (int k = t; k < kNnTile; k += kPlocThreads) s_back[k] = ~0ull;
     __syncthreads();
-    float bd[kNnPer];
-    int bj[kNnPer];
+    float fd[kNnPer], ed[kNnPer];  // forward / backward best areas (+inf: none yet)
+    int fj[kNnPer], ej[kNnPer];
+    float4 xa[kNnPer], xb[kNnPer];
 #pragma unroll
     for (int m = 0; m < kNnPer; ++m) {
-      bd[m] = kInf;  // only finite areas are candidates
-      bj[m] = -1;
-      const int xi = t + m * kPlocThreads;  // tile-relative
-      if (xi < tile_n) {
-        const int xw = xi + r;  // window-relative
-        const float4 xa = sw[2 * xw], xb = sw[2 * xw + 1];
-        const int last = min(r, (int)c - 1 - ((int)base + xi));  // forward offsets 1..last
-        for (int k = 1; k <= last; ++k) {
-          const float d = pair_area(xa, xb, sw[2 * (xw + k)], sw[2 * (xw + k) + 1]);
-          if (d < bd[m]) {  // increasing j: the first of equal areas stays
-            bd[m] = d;
-            bj[m] = (int)base + xi + k;
+      fd[m] = ed[m] = kInf;
+      fj[m] = ej[m] = -1;
+      const int xi = t + m * kPlocThreads;
+      xa[m] = sw[2 * min(xi + r, span - 1)];
+      xb[m] = sw[2 * min(xi + r, span - 1) + 1];
+    }
+    for (int k0 = 1; k0 <= r; k0 += kNnKc) {
+      const int kc = min(kNnKc, r - k0 + 1);
+      // pairs (x, x + k), k in [k0, k0 + kc): forward candidates of x, table entries for x + k
+#pragma unroll
+      for (int m = 0; m < kNnPer; ++m) {
+        const int xi = t + m * kPlocThreads;
+        if (xi < tile_n) {
+          const int kmax = min(kc, (int)c - 1 - ((int)base + xi) - k0 + 1);  // j = base + xi + k < c
+          for (int kk = 0; kk < kmax; ++kk) {
+            const int jw = xi + r + k0 + kk;
+            const float d = pair_area(xa[m], xb[m], sw[2 * jw], sw[2 * jw + 1]);
+            if (d < fd[m]) {  // increasing j: the first of equal areas stays
+              fd[m] = d;
+              fj[m] = (int)base + xi + k0 + kk;
+            }
+            if (xi + k0 + kk < tile_n) sD[kk * kNnTile + xi + k0 + kk] = d;
           }
-          if (xi + k < tile_n && d < kInf)
-            atomicMin(s_back + xi + k, ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)((int)base + xi));
         }
       }
-    }
-    // halo clusters lo + hw (hw < r) offer to the tile's first clusters; row hw goes to thread
-    // hw * 256 / r, spreading the rows over all warps
-    for (int hw = (t * r + kPlocThreads - 1) / kPlocThreads; hw < r && (hw * kPlocThreads) / r == t; ++hw) {
-      const int h = lo + hw;
-      if (h >= 0) {
-        const float4 ha = sw[2 * hw], hb = sw[2 * hw + 1];
-        const int last = min(hw, tile_n - 1);  // tile-relative targets 0..last (offsets r-hw .. r)
-        for (int jj = 0; jj <= last; ++jj) {
-          const float d = pair_area(ha, hb, sw[2 * (jj + r)], sw[2 * (jj + r) + 1]);
-          if (d < kInf) atomicMin(s_back + jj, ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)h);
+      // halo pairs (h, jj) with jj < k: the table entries of the tile's first clusters
+      for (int kk = 0; kk < kc; ++kk) {
+        const int k = k0 + kk;
+        const int rot = (k * 37) & (kPlocThreads - 1);  // spread each offset's pairs over the block
+        for (int p = (t - rot) & (kPlocThreads - 1); p < k && p < tile_n; p += kPlocThreads) {
+          const int h = (int)base + p - k;  // the halo cluster; p is the tile-relative target
+          if (h >= 0) {
+            const int hw = p - k + r;
+            sD[kk * kNnTile + p] = pair_area(sw[2 * hw], sw[2 * hw + 1], sw[2 * (p + r)], sw[2 * (p + r) + 1]);
+          }
         }
       }
+      __syncthreads();
+      // backward candidates j - k of this thread's clusters
+#pragma unroll
+      for (int m = 0; m < kNnPer; ++m) {
+        const int xi = t + m * kPlocThreads;
+        if (xi < tile_n) {
+          for (int kk = 0; kk < kc; ++kk) {
+            const int src = (int)base + xi - k0 - kk;
+            if (src < 0) break;
+            const float d = sD[kk * kNnTile + xi];
+            if (d < kInf && d <= ed[m]) {  // later offset = smaller index: wins ties
+              ed[m] = d;
+              ej[m] = src;
+            }
+          }
+        }
+      }
+      __syncthreads();  // the table is refilled by the next chunk
     }
-    __syncthreads();
 #pragma unroll
     for (int m = 0; m < kNnPer; ++m) {
       const int xi = t + m * kPlocThreads;
-      if (xi < tile_n) {
-        const unsigned long long o = s_back[xi];
-        int j = bj[m];
-        if (o != ~0ull && __uint_as_float((uint32_t)(o >> 32)) <= bd[m]) j = (int)(uint32_t)o;  // earlier index wins ties
-        B.nbr[base + xi] = j;
-      }
+      if (xi < tile_n) B.nbr[base + xi] = (ej[m] >= 0 && ed[m] <= fd[m]) ? ej[m] : fj[m];  // earlier index wins ties
     }
   }
 }
@@ -341,7 +362,7 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   return cudaSuccess;
 }
 
-static size_t nn_smem(int radius) { return 32 * (kNnTile + 2 * (size_t)radius) + 8 * (size_t)kNnTile; }
+static size_t nn_smem(int radius) { return 32 * (kNnTile + 2 * (size_t)radius) + 4 * (size_t)kNnKc * kNnTile; }
 
 // The loop as a graph: WHILE(cond) { nn; merge; step }.  Grids are persistent (sized for n), the
 // kernels read the live cluster count from the control words.
@@ -365,7 +386,7 @@ static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n,
     if ((e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
       break;
-    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 4));
+    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3));
     const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
     k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), cs>>>(B, radius);
     k_ploc_merge<<<mg_grid, kPlocThreads, 0, cs>>>(B);
@@ -427,7 +448,7 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap);
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
   if (n > 1 && host_loop) {
-    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 4));
+    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3));
     const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
     for (uint32_t it = 0; it < cap; ++it) {
       k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), st>>>(B, radius);

@@ -415,6 +415,7 @@ __device__ __forceinline__ int reg_avail(const Node* nodes, int32_t root, const 
 // Rebuild (:194-246) from the partitions P (this lane's column, stride 32), breadth-first,
 // handing out the reused ids in order.  A subset with no finite split (NaN areas) leaves the
 // treelet unchanged.
+template <int PSTRIDE>
 __device__ __forceinline__ void reg_build(Node* nodes, const RegTreelet& T, const uint8_t* P, const int* avail,
                                           int n_avail) {
   const int n = T.n;
@@ -424,7 +425,7 @@ __device__ __forceinline__ void reg_build(Node* nodes, const RegTreelet& T, cons
     vm[vt++] = (int)full;
     while (vh < vt) {
       const int mask = vm[vh++];
-      const int lm = P[mask * 32], rm = mask ^ lm;
+      const int lm = P[mask * PSTRIDE], rm = mask ^ lm;
       if (lm == 0 || rm == 0 || (lm & ~mask)) return;
       if (__popc(lm) > 1) { if (vt >= kTlMax) return; vm[vt++] = lm; }
       if (__popc(rm) > 1) { if (vt >= kTlMax) return; vm[vt++] = rm; }
@@ -438,7 +439,7 @@ __device__ __forceinline__ void reg_build(Node* nodes, const RegTreelet& T, cons
   while (qh < qt) {
     const int mask = qm[qh], cur = qn[qh];
     qh++;
-    const int lm = P[mask * 32], rm = mask ^ lm;
+    const int lm = P[mask * PSTRIDE], rm = mask ^ lm;
     int li, ri;
     if (__popc(lm) == 1) li = reg_id(T, __ffs(lm) - 1);
     else { li = avail[used++]; qm[qt] = lm; qn[qt++] = li; }
@@ -455,11 +456,10 @@ __device__ __forceinline__ void reg_build(Node* nodes, const RegTreelet& T, cons
 }
 
 // Heights: a climb from every leaf; the first child to reach a parent leaves its height in the
-// rendezvous word, the second computes the parent's and counts it (warp-aggregated).
+// rendezvous word, the second computes the parent's.
 __global__ void __launch_bounds__(256) k_tl_heights(const Node* __restrict__ nodes, unsigned long long* __restrict__ slots,
                                                     const uint32_t* epoch_word, uint32_t round, uint32_t n,
-                                                    uint8_t* __restrict__ hgt, uint32_t* __restrict__ cnt,
-                                                    uint32_t* __restrict__ flags) {
+                                                    uint8_t* __restrict__ hgt, uint32_t* __restrict__ flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const unsigned long long tag = (unsigned long long)(__ldcg(epoch_word) + 1u + round) << 32;
@@ -475,10 +475,20 @@ __global__ void __launch_bounds__(256) k_tl_heights(const Node* __restrict__ nod
       h = kTlMaxHeight + 1;
     }
     hgt[parent] = (uint8_t)h;
-    const uint32_t peers = __match_any_sync(__activemask(), h);
-    if ((threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(cnt + h, __popc(peers));
     idx = parent;
   }
+}
+
+// Nodes per height (block histograms in shared memory, one global add per nonzero bin).
+__global__ void __launch_bounds__(256) k_tl_count(const uint8_t* __restrict__ hgt, uint32_t m, uint32_t* __restrict__ cnt) {
+  __shared__ uint32_t s_cnt[256];
+  s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    atomicAdd(&s_cnt[hgt[i]], 1u);
+  __syncthreads();
+  const uint32_t c = s_cnt[threadIdx.x];
+  if (c) atomicAdd(cnt + threadIdx.x, c);
 }
 
 // off[h] = first list position of height h (exclusive scan of cnt over 256 heights), cursor
@@ -541,7 +551,6 @@ __global__ void __launch_bounds__(256) k_tl_scatter(const uint8_t* __restrict__ 
 // node at stride `stride` (>= the largest height's node count): [0] n | n_avail << 8,
 // [1..7] leaf ids, [8..13] reused internal ids in order.  ctl: [0] too high, [1] largest
 // height, [2] current height.
-constexpr int kTlDescWords = 14;
 constexpr int kGrowThreads = 128;
 
 __global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ nodes, const uint32_t* __restrict__ list,
@@ -580,6 +589,43 @@ __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, 
   const uint32_t h = __ldcg(ctl + 2);
   const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
   const int lane = threadIdx.x & 31;
+  if (e - b <= 8u * gridDim.x) {
+    // a narrow height: one treelet per warp with the warp-cooperative DP (shorter critical path)
+    LaneTreelet& S = *reinterpret_cast<LaneTreelet*>(s_cost);
+    float* cost = s_cost + 512;
+    float* area = s_cost + 640;
+    for (uint32_t k = b + blockIdx.x; k < e; k += gridDim.x) {
+      const uint32_t q = k - b;
+      const uint32_t w0 = __ldcg(desc + q);
+      const int n = (int)(w0 & 255u);
+      if (n < 2) continue;  // uniform over the warp
+      if (lane < kTlMax) {
+        const int32_t id = (int32_t)__ldcg(desc + (size_t)(1 + lane) * stride + q);
+        S.act[lane] = id;
+        const Box bx = lane < n ? ldcg_box(nodes, id) : box_empty();
+        S.box[0][lane] = bx.lo.x; S.box[1][lane] = bx.lo.y; S.box[2][lane] = bx.lo.z;
+        S.box[3][lane] = bx.hi.x; S.box[4][lane] = bx.hi.y; S.box[5][lane] = bx.hi.z;
+      }
+      if (lane == 0) S.n = n;
+      __syncwarp();
+      treelet_dp(S, cost, area);
+      if (lane == 0) {
+        RegTreelet T;
+        T.n = n;
+#pragma unroll
+        for (int i = 0; i < kTlMax; ++i) {
+          T.id[i] = S.act[i];
+          T.b[i] = leaf_box(S, i);
+        }
+        int avail[kTlMax];
+#pragma unroll
+        for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
+        reg_build<1>(nodes, T, S.part, avail, (int)(w0 >> 8));
+      }
+      __syncwarp();
+    }
+    return;
+  }
   float* C = s_cost + lane;
   uint8_t* P = s_part + lane;
   for (uint32_t k = b + blockIdx.x * kLvThreads + lane; k < e; k += gridDim.x * kLvThreads) {
@@ -598,16 +644,18 @@ __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, 
 #pragma unroll
     for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
     reg_dp(T, C, P);
-    reg_build(nodes, T, P, avail, na);
+    reg_build<32>(nodes, T, P, avail, na);
   }
 }
 
-// End of a height: the next one, and whether the loop goes on.
+// End of a height: the next one, and whether the loop goes on (the graph's WHILE condition;
+// the host-driven loop only advances the height).
+template <bool GRAPH>
 __global__ void k_tl_step(uint32_t* __restrict__ ctl, cudaGraphConditionalHandle handle) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const uint32_t h = ctl[2] + 1;
   ctl[2] = h;
-  cudaGraphSetConditional(handle, (ctl[0] == 0u && h <= ctl[1]) ? 1u : 0u);
+  if constexpr (GRAPH) cudaGraphSetConditional(handle, (ctl[0] == 0u && h <= ctl[1]) ? 1u : 0u);
 }
 
 // The climb-ordered pass as a fallback for trees higher than kTlMaxHeight: persistent warps
@@ -690,7 +738,7 @@ static cudaError_t make_height_graph(Node* nodes, const uint32_t* list, const ui
       break;
     k_tl_grow<<<grow_grid, kGrowThreads, 0, cs>>>(nodes, list, off, ctl, desc, stride);
     k_tl_dp<<<dp_grid, kLvThreads, 0, cs>>>(nodes, off, ctl, desc, stride);
-    k_tl_step<<<1, 32, 0, cs>>>(ctl, handle);
+    k_tl_step<true><<<1, 32, 0, cs>>>(ctl, handle);
     cudaGraph_t captured = nullptr;
     const cudaError_t e2 = cudaGetLastError();
     e = cudaStreamEndCapture(cs, &captured);
@@ -703,7 +751,7 @@ static cudaError_t make_height_graph(Node* nodes, const uint32_t* list, const ui
   return e;
 }
 
-cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb) {
+cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb, bool host_loop) {
   if (n < 2) return cudaSuccess;
   ScratchLayout L = scratch_layout(ws.cap_n);
   int dev = 0;
@@ -729,12 +777,13 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   uint32_t* cursor = off + 264;              // 256
   uint32_t* ctl = cursor + 256;              // [0] too high, [1] largest height, [2] current height
   const uint32_t* epoch = ws.scratch + L.epoch;
-  const bool same = ws.tl_exec && ws.tl_key_n == n && ws.tl_key_nodes == ws.nodes && ws.tl_key_list == list &&
+  const uint32_t grow_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(stride, kGrowThreads), sms * 16));
+  if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
+  const bool same = host_loop || ws.tl_exec && ws.tl_key_n == n && ws.tl_key_nodes == ws.nodes && ws.tl_key_list == list &&
                     ws.tl_key_desc == desc && ws.tl_key_ctl == ctl;
   if (!same) {
     if (ws.tl_exec) cudaGraphExecDestroy(ws.tl_exec);
     ws.tl_exec = nullptr;
-    const uint32_t grow_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(stride, kGrowThreads), sms * 16));
     if ((e = make_height_graph(ws.nodes, list, off, ctl, desc, stride, grow_grid, (uint32_t)g_dp_grid[dev],
                                &ws.tl_exec)) != cudaSuccess)
       return e;
@@ -747,10 +796,24 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   for (int r = 0; r < rounds && r + 1 < 0x20; ++r) {
     if ((e = cudaMemsetAsync(cnt, 0, 256 * 4, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ctl, 0, 4 * 4, st)) != cudaSuccess) return e;
-    k_tl_heights<<<div_up(n, 256), 256, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, hgt, cnt, ctl);
+    k_tl_heights<<<div_up(n, 256), 256, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, hgt, ctl);
+    k_tl_count<<<std::max<uint32_t>(1, std::min<uint32_t>(div_up(n - 1, 256), sms * 8)), 256, 0, st>>>(hgt, n - 1, cnt);
     k_tl_offsets<<<1, 256, 0, st>>>(cnt, n - 1, off, cursor, ctl);
     k_tl_scatter<<<div_up(n - 1, 256), 256, 0, st>>>(hgt, n - 1, cursor, list);
-    if ((e = cudaGraphLaunch(ws.tl_exec, st)) != cudaSuccess) return e;
+    if (host_loop) {
+      // read the largest height (and the too-high flag) once, then one grow + dp per height
+      if ((e = cudaMemcpyAsync(ws.ploc_host, ctl, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+      const uint32_t maxh = ws.ploc_host[0] ? 0u : ws.ploc_host[1];
+      for (uint32_t h = 1; h <= maxh; ++h) {
+        k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
+        k_tl_dp<<<g_dp_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+        k_tl_step<false><<<1, 32, 0, st>>>(ctl, cudaGraphConditionalHandle{});
+      }
+    } else if ((e = cudaGraphLaunch(ws.tl_exec, st)) != cudaSuccess) {
+      return e;
+    }
     k_treelet_fallback<<<sms * 8, 64, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, ctl);
   }
   return cudaGetLastError();

@@ -136,11 +136,12 @@ typedef struct bvh_batch {
  * graph on first use and replay it while the batch layout (pointers, offsets) is unchanged. */
 #define BVH_BATCH_USE_GRAPH 1
 
-/* bvh_params.reserved[1] for PLOC: 1 = drive the clustering loop from the host (one launch of
- * each loop kernel per iteration, the live cluster count read back after each) instead of the
- * CUDA graph with a conditional WHILE node.  Same tree; slower; for tools that cannot follow
+/* bvh_params.reserved[1]: 1 = drive the device loops from the host instead of CUDA graphs with
+ * a conditional WHILE node: PLOC's clustering loop (one launch of each loop kernel per
+ * iteration, the live cluster count read back after each) and LBVH+'s loop over tree heights
+ * (the height read back once per pass).  Same tree; slower; for tools that cannot follow
  * conditional graph nodes (profilers) and drivers without them. */
-#define BVH_PLOC_HOST_LOOP 1
+#define BVH_HOST_DRIVEN_LOOPS 1
 
 typedef struct bvh_ctx bvh_ctx;
 

@@ -59,11 +59,22 @@ def test_ploc_host_driven_loop_equals_graph_loop(ctx, gpu, oracle_lib, name, rad
     m = CASES[name]
     g_nodes, g_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_PLOC, ploc_radius=radius))
     g_it = ctx.last_timing().ploc_iterations
-    h_nodes, h_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_PLOC, ploc_radius=radius, ploc_host_loop=True))
+    h_nodes, h_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_PLOC, ploc_radius=radius, host_loops=True))
     t = ctx.last_timing()
     assert np.array_equal(g_idx, h_idx)
     assert oracle_lib.node_fields_equal(g_nodes, h_nodes)
     assert t.ploc_iterations == g_it
+
+
+@pytest.mark.parametrize("rounds", [1, 3])
+@pytest.mark.parametrize("name", ["uniform17", "uniform4097", "clustered20000"])
+def test_lbvh_plus_host_driven_loop_equals_graph_loop(ctx, gpu, oracle_lib, name, rounds):
+    m = CASES[name]
+    p = dict(morton_bits=60, treelet_rounds=rounds)
+    g_nodes, g_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH_PLUS, **p))
+    h_nodes, h_idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH_PLUS, host_loops=True, **p))
+    assert np.array_equal(g_idx, h_idx)
+    assert oracle_lib.node_fields_equal(g_nodes, h_nodes)
 
 
 def test_ploc_nan_mesh_reports_no_progress(ctx, gpu):
@@ -72,7 +83,7 @@ def test_ploc_nan_mesh_reports_no_progress(ctx, gpu):
         a[:] = np.nan
     for host_loop in (False, True):
         with pytest.raises(C.BVHError) as e:
-            ctx.build_host(m, ctx.params(C.ALGO_PLOC, ploc_radius=4, ploc_host_loop=host_loop))
+            ctx.build_host(m, ctx.params(C.ALGO_PLOC, ploc_radius=4, host_loops=host_loop))
         assert e.value.status == C.BVH_ERR_NO_PROGRESS
 
 
