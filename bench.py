@@ -96,16 +96,18 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
     return 144.0 * rounds
 
 
-def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0) -> int:
+def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0, tree_height: int = 0) -> int:
     """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
-    fix-up for 64-bit keys, delta + emission + frontier climb; five per treelet pass (heights,
-    offsets, grouping by height, the level kernel, the fallback check); PLOC adds
-    cluster init, 3 per clustering iteration (neighbours, merge, loop control) and the root fix
+    fix-up for 64-bit keys, delta + emission + frontier climb; per treelet pass five (heights,
+    counts, offsets, grouping by height, the fallback check) plus growth, DP and loop control per
+    tree level; PLOC adds
+    cluster init, 4 per clustering iteration (neighbours, tile counts + scan, merge + compaction,
+    loop control) and the root fix
     (its 30-bit prefix stops after the sort)."""
     if algo == "ploc":
-        return 2 + 4 + 1 + 3 * ploc_iterations + 1
+        return 2 + 4 + 1 + 4 * ploc_iterations + 1
     n = 2 + 4 + (1 if bits != 30 else 0) + 3
-    return n + (5 * rounds if algo == "lbvh_plus" else 0)
+    return n + (rounds * (5 + 3 * tree_height) if algo == "lbvh_plus" else 0)
 
 
 STAGE_KERNELS = {
@@ -113,8 +115,9 @@ STAGE_KERNELS = {
     "morton_boxes_hist": "k_morton",
     "onesweep_sort": "k_onesweep x4 (+ k_fixrun for 60/63-bit keys)",
     "emit_refit": "k_delta + k_emit + k_emit_climb",
-    "treelet_or_ploc_loop": "k_treelet_round (LBVH+) / k_ploc_nn + k_ploc_merge + k_ploc_step per iteration"
-                            " + k_ploc_root (PLOC)",
+    "treelet_or_ploc_loop": "LBVH+: k_tl_heights, k_tl_count, k_tl_offsets, k_tl_scatter, then k_tl_grow +"
+                            " k_tl_dp per tree height; PLOC: k_ploc_nn, k_ploc_count, k_ploc_scatter, k_ploc_step"
+                            " per iteration + k_ploc_root",
 }
 
 
@@ -271,6 +274,7 @@ def run_ours(args):
             t = ctx.last_timing()
             stages.append((t.bounds_ms, t.morton_ms, t.sort_ms, t.emit_ms, t.optimize_ms, t.total_ms))
             ploc_iters, ploc_csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
+            tree_height = int(t.tree_height)
     elapsed_ms = ev0.elapsed_time(ev1)
     if ws > 1:
         tt = torch.tensor([elapsed_ms], device=dev)
@@ -341,7 +345,7 @@ def run_ours(args):
         "stage_ms_median": stage_ms,
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": args.steps * kernels_per_build(algo, bits, rounds, ploc_iters),
+        "gpu_launches": args.steps * kernels_per_build(algo, bits, rounds, ploc_iters, tree_height),
         "clocks": clk.summary(),
         "autotune": tuning,
     }

@@ -185,6 +185,8 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   cudaMemcpyAsync(ctx->h_status, ctx->ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
   if (params->algo == BVH_ALGO_PLOC)  // iterations and live-cluster sum, read at bvh_sync
     cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.ploc, 16 * 4, cudaMemcpyDeviceToHost, st);
+  if (params->algo == BVH_ALGO_LBVH_PLUS && params->treelet_rounds > 0 && n > 1)  // tree height, read at bvh_sync
+    cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.hist + kTlCtlWord, 2 * 4, cudaMemcpyDeviceToHost, st);
   cudaEventRecord(ctx->evs.ev[6], st);
   out->nodes = reinterpret_cast<const bvh_node*>(ctx->ws.nodes);
   out->indices = idx;
@@ -216,6 +218,8 @@ extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
     const uint32_t* w = ctx->h_status + 4;
     ctx->last.ploc_iterations = (int32_t)w[kPlocIterWord];
     ctx->last.ploc_cluster_sum = (uint64_t)w[kPlocSumWord + 1] << 32 | w[kPlocSumWord];
+  } else if (ctx->last_algo == BVH_ALGO_LBVH_PLUS) {
+    ctx->last.tree_height = (int32_t)ctx->h_status[5];
   }
   return check_status_word(ctx);
 }

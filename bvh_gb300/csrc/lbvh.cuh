@@ -137,6 +137,8 @@ cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned lon
 // (the other one is scratch).
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb,
                                bool host_loop = false);
+// Treelet control words (scratch + L.hist + kTlCtlWord): [0] too high, [1] tree height.
+constexpr size_t kTlCtlWord = 256 + 264 + 256;
 
 // Stable sort of ws.keys[0] (64-bit) with implicit indices over `passes` 8-bit digits.
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,

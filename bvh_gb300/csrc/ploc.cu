@@ -6,8 +6,8 @@
 // order-preserving compaction (:267-293), same root move to index 0 (:563-582).
 //
 // Differences by design: new node ids are handed out in ascending cluster order through a
-// scan (the reference uses atomicAdd, so its ids vary run to run); merge and compaction are one
-// kernel with a decoupled look-back scan; and the iteration loop runs on the device as a CUDA
+// scan (the reference uses atomicAdd, so its ids vary run to run); merge and compaction share
+// one reduce-then-scan over 2048-cluster tiles; and the iteration loop runs on the device as a CUDA
 // graph WHILE node (the reference synchronises with the host five times per iteration,
 // :489-548): a one-thread step kernel swaps the cluster buffers, stops on convergence, on an
 // iteration that merges nothing (NaN/Inf areas, where the reference loops forever) or at the
@@ -23,7 +23,7 @@ constexpr int kPlocIpt = 8;
 constexpr int kPlocTile = kPlocThreads * kPlocIpt;
 
 // control words (scratch + L.ploc):
-//   [0] live clusters  [1] next node id  [2] merge tile counter  [3] buffer parity
+//   [0] live clusters  [1] next node id  [2] count ticket  [3] buffer parity
 //   [4] survivors (next iteration)  [5] next node id (next iteration)  [6] iterations  [7] cap
 //   [8..9] sum of live clusters over iterations (64-bit)  [10] go on (host-driven loop)
 struct PlocBufs {
@@ -70,8 +70,7 @@ __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __rest
 // later offset, i.e. the smaller index, wins ties).  Offsets go in chunks of kNnKc to bound the
 // table.  The r clusters before a tile ("halo") only fill the table; their pairs are spread over
 // all warps.  Tiles of kNnTile clusters (kNnPer per thread, strided so lanes are consecutive),
-// the window staged in shared memory.  Also clears the merge kernel's look-back words and tile
-// counter.
+// the window staged in shared memory.
 constexpr int kNnPer = 4;
 constexpr int kNnTile = kPlocThreads * kNnPer;
 constexpr int kNnKc = 5;
@@ -86,10 +85,6 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   float* sD = reinterpret_cast<float*>(sw + 2 * (kNnTile + 2 * r));  // [kNnKc][kNnTile]
   const uint32_t c = __ldcg(B.ctrl + 0);
   const Box* __restrict__ cbox = B.cbox[__ldcg(B.ctrl + 3) & 1u];
-  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t mtiles = div_up(c, kPlocTile);
-  for (uint32_t w = gtid; w < mtiles; w += gridDim.x * blockDim.x) B.desc[w] = 0ull;
-  if (gtid == 0) B.ctrl[2] = 0;
   const int span = kNnTile + 2 * r;
   const int t = threadIdx.x;
   const float kInf = __int_as_float(0x7f800000);
@@ -175,127 +170,28 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   }
 }
 
-constexpr unsigned long long kPFlagAgg = 1ull << 62;
-constexpr unsigned long long kPFlagInc = 2ull << 62;
-constexpr unsigned long long kPValMask = (1ull << 62) - 1;
+// Merge mutual pairs (i < j keeps position i, :211-264) and compact the survivors (:267-293),
+// as reduce-then-scan: k_ploc_count totals each 2048-cluster tile and its last block scans the
+// tile totals, k_ploc_scatter recomputes its tile's flags and writes, k_ploc_step ends the
+// iteration.  Warp w of a tile
+// takes its items w*256 + r*32 + lane in 8 rounds r of 32 consecutive clusters, so positions
+// within the warp come from ballots.  Counts are packed as merges << 31 | survivors; new node
+// ids follow the cluster order.
+constexpr int kPlocRounds = kPlocTile / kPlocThreads;  // 8
 
-// Merge mutual pairs (i < j keeps position i) and compact the survivors; counts are packed as
-// merges << 31 | survivors.  Persistent blocks take tiles in order from a counter.
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_merge(PlocBufs B) {
-  __shared__ uint32_t s_tile;
-  __shared__ unsigned long long s_warp[kPlocThreads / 32];
-  __shared__ unsigned long long s_prefix;
-  const uint32_t c = __ldcg(B.ctrl + 0);
-  const uint32_t next = __ldcg(B.ctrl + 1);
-  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
-  const Box* __restrict__ cin = B.cbox[par];
-  const int32_t* __restrict__ idin = B.cid[par];
-  Box* __restrict__ cout = B.cbox[par ^ 1u];
-  int32_t* __restrict__ idout = B.cid[par ^ 1u];
-  const int32_t* __restrict__ nbr = B.nbr;
-  const uint32_t tiles = div_up(c, kPlocTile);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  while (true) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_tile = atomicAdd(B.ctrl + 2, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    if (tile >= tiles) return;
-    // blocked arrangement: thread t owns items base + t*IPT .. + IPT-1 (keeps order for the scan)
-    const uint32_t first = tile * kPlocTile + threadIdx.x * kPlocIpt;
-    uint32_t mflags = 0, vflags = 0;
-    int32_t nj[kPlocIpt];
-#pragma unroll
-    for (int k = 0; k < kPlocIpt; ++k) {
-      uint32_t i = first + k;
-      nj[k] = -1;
-      if (i < c) {
-        int32_t j = __ldcg(nbr + i);
-        nj[k] = j;
-        bool mutual = j >= 0 && (uint32_t)j < c && __ldcg(nbr + j) == (int32_t)i;
-        if (mutual && (int32_t)i < j) mflags |= 1u << k;
-        if (!(mutual && j < (int32_t)i)) vflags |= 1u << k;
-      }
-    }
-    unsigned long long mine = ((unsigned long long)__popc(mflags) << 31) | (unsigned long long)__popc(vflags);
-    unsigned long long x = mine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[w] = x;
-    __syncthreads();
-    if (w == 0) {
-      unsigned long long t = lane < kPlocThreads / 32 ? s_warp[lane] : 0ull;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
-        if (lane >= o) t += y;
-      }
-      if (lane < kPlocThreads / 32) s_warp[lane] = t;
-    }
-    __syncthreads();
-    const unsigned long long tile_total = s_warp[kPlocThreads / 32 - 1];
-    const unsigned long long excl_in_tile = (w ? s_warp[w - 1] : 0ull) + x - mine;
-    if (threadIdx.x == 0) {
-      unsigned long long pre = 0;
-      if (tile == 0) {
-        st_relaxed(B.desc, kPFlagInc | tile_total);
-      } else {
-        st_relaxed(B.desc + tile, kPFlagAgg | tile_total);
-        pre = lookback<16, unsigned long long>(B.desc, 1, (int64_t)tile, ~kPValMask, kPFlagInc, B.status,
-                                               kStatusSortTimeout);
-        st_relaxed(B.desc + tile, kPFlagInc | (pre + tile_total));
-      }
-      s_prefix = pre;
-      if (tile == tiles - 1) {
-        const unsigned long long tot = pre + tile_total;
-        B.ctrl[4] = (uint32_t)(tot & 0x7fffffffull);  // survivors
-        B.ctrl[5] = next + (uint32_t)(tot >> 31);      // next node id
-      }
-    }
-    __syncthreads();
-    const unsigned long long ex = s_prefix + excl_in_tile;
-    uint32_t mpos = (uint32_t)(ex >> 31), vpos = (uint32_t)(ex & 0x7fffffffull);
-#pragma unroll
-    for (int k = 0; k < kPlocIpt; ++k) {
-      uint32_t i = first + k;
-      if (i >= c) break;
-      const float4* ip = reinterpret_cast<const float4*>(cin + i);
-      float4 lo = __ldcg(ip), hi = __ldcg(ip + 1);
-      int32_t id = __ldcg(idin + i);
-      if ((mflags >> k) & 1u) {
-        int32_t j = nj[k];
-        const float4* jp = reinterpret_cast<const float4*>(cin + j);
-        float4 jlo = __ldcg(jp), jhi = __ldcg(jp + 1);
-        lo = make_float4(fminf(lo.x, jlo.x), fminf(lo.y, jlo.y), fminf(lo.z, jlo.z), 0.f);
-        hi = make_float4(fmaxf(hi.x, jhi.x), fmaxf(hi.y, jhi.y), fmaxf(hi.z, jhi.z), 0.f);
-        int32_t nid = (int32_t)(next + mpos);
-        if ((uint32_t)nid >= 2 * next) break;  // counts inconsistent only after a timed-out wait
-        float4* np = reinterpret_cast<float4*>(B.nodes + nid);
-        np[0] = lo;
-        np[1] = hi;
-        reinterpret_cast<int4*>(np + 2)[0] = make_int4(id, __ldcg(idin + j), 0, 0);
-        id = nid;
-        mpos++;
-      }
-      if (((vflags >> k) & 1u) && vpos < c) {
-        float4* op = reinterpret_cast<float4*>(cout + vpos);
-        op[0] = lo;
-        op[1] = hi;
-        idout[vpos] = id;
-        vpos++;
-      }
-    }
-  }
+// Item i merges here (as the smaller index of a mutual pair) / survives.
+__device__ __forceinline__ void item_flags(const int32_t* __restrict__ nbr, uint32_t c, uint32_t i, int32_t& j,
+                                           bool& m, bool& v) {
+  j = i < c ? __ldcg(nbr + i) : -1;
+  const bool mutual = i < c && j >= 0 && (uint32_t)j < c && __ldcg(nbr + j) == (int32_t)i;
+  m = mutual && (int32_t)i < j;
+  v = i < c && !(mutual && j < (int32_t)i);
 }
 
 // End of one iteration: publish the survivors, swap buffers, decide whether to go on (the
 // graph's WHILE condition, or ctrl[10] for the host-driven loop).
 template <bool GRAPH>
-__global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
   const uint32_t c = B.ctrl[0], nc = B.ctrl[4], it = B.ctrl[6] + 1, cap = B.ctrl[7];
   unsigned long long sum = ((unsigned long long)B.ctrl[9] << 32 | B.ctrl[8]) + c;
   B.ctrl[8] = (uint32_t)sum;
@@ -311,6 +207,152 @@ __global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
   }
   if constexpr (GRAPH) cudaGraphSetConditional(handle, go ? 1u : 0u);
   else B.ctrl[10] = go ? 1u : 0u;
+}
+
+// Exclusive prefix of the tile totals (in place), the survivors and the next node id; run by
+// the last block of k_ploc_count.
+__device__ __forceinline__ void ploc_scan_tiles(PlocBufs B, uint32_t tiles, unsigned long long* s_w) {
+  const uint32_t per = div_up(tiles, (uint32_t)kPlocThreads);
+  const uint32_t t0 = threadIdx.x * per, t1 = min(t0 + per, tiles);
+  unsigned long long sum = 0;
+  for (uint32_t t = t0; t < t1; ++t) sum += __ldcg(B.desc + t);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[w] = x;
+  __syncthreads();
+  unsigned long long run = x - sum, total = 0;
+#pragma unroll
+  for (int k = 0; k < kPlocThreads / 32; ++k) {
+    if (k < w) run += s_w[k];
+    total += s_w[k];
+  }
+  for (uint32_t t = t0; t < t1; ++t) {
+    const unsigned long long v = __ldcg(B.desc + t);
+    B.desc[t] = run;
+    run += v;
+  }
+  if (threadIdx.x == 0) {
+    B.ctrl[4] = (uint32_t)(total & 0x7fffffffull);             // survivors
+    B.ctrl[5] = __ldcg(B.ctrl + 1) + (uint32_t)(total >> 31);  // next node id
+  }
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
+  __shared__ unsigned long long s_w[kPlocThreads / 32];
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const uint32_t tiles = div_up(c, kPlocTile);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t base = tile * kPlocTile + w * (32 * kPlocRounds);
+    uint32_t tm = 0, tv = 0;
+#pragma unroll
+    for (int r = 0; r < kPlocRounds; ++r) {
+      int32_t j;
+      bool m, v;
+      item_flags(B.nbr, c, base + r * 32 + lane, j, m, v);
+      tm += __popc(__ballot_sync(0xffffffffu, m));
+      tv += __popc(__ballot_sync(0xffffffffu, v));
+    }
+    if (lane == 0) s_w[w] = ((unsigned long long)tm << 31) | tv;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long t = 0;
+#pragma unroll
+      for (int k = 0; k < kPlocThreads / 32; ++k) t += s_w[k];
+      B.desc[tile] = t;
+    }
+    __syncthreads();
+  }
+  // the last block to finish scans the tile totals (ticket in ctrl[2])
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(B.ctrl + 2, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  ploc_scan_tiles(B, tiles, s_w);
+  if (threadIdx.x == 0) B.ctrl[2] = 0;
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_scatter(PlocBufs B) {
+  __shared__ unsigned long long s_w[kPlocThreads / 32];
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const uint32_t next = __ldcg(B.ctrl + 1);
+  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
+  const Box* __restrict__ cin = B.cbox[par];
+  const int32_t* __restrict__ idin = B.cid[par];
+  Box* __restrict__ cout = B.cbox[par ^ 1u];
+  int32_t* __restrict__ idout = B.cid[par ^ 1u];
+  const uint32_t tiles = div_up(c, kPlocTile);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t base = tile * kPlocTile + w * (32 * kPlocRounds);
+    uint32_t mb[kPlocRounds], vb[kPlocRounds];
+    int32_t nj[kPlocRounds];
+    uint32_t tm = 0, tv = 0;
+#pragma unroll
+    for (int r = 0; r < kPlocRounds; ++r) {
+      bool m, v;
+      item_flags(B.nbr, c, base + r * 32 + lane, nj[r], m, v);
+      mb[r] = __ballot_sync(0xffffffffu, m);
+      vb[r] = __ballot_sync(0xffffffffu, v);
+      tm += __popc(mb[r]);
+      tv += __popc(vb[r]);
+    }
+    if (lane == 0) s_w[w] = ((unsigned long long)tm << 31) | tv;
+    __syncthreads();
+    unsigned long long before = __ldcg(B.desc + tile);
+#pragma unroll
+    for (int k = 0; k < kPlocThreads / 32; ++k)
+      if (k < w) before += s_w[k];
+    __syncthreads();  // s_w is rewritten by the next tile
+    uint32_t mpos = (uint32_t)(before >> 31), vpos = (uint32_t)(before & 0x7fffffffull);
+#pragma unroll
+    for (int r = 0; r < kPlocRounds; ++r) {
+      const uint32_t i = base + r * 32 + lane;
+      const bool m = (mb[r] >> lane) & 1u, v = (vb[r] >> lane) & 1u;
+      if (m || v) {
+        const float4* ip = reinterpret_cast<const float4*>(cin + i);
+        float4 lo = __ldcg(ip), hi = __ldcg(ip + 1);
+        int32_t id = __ldcg(idin + i);
+        if (m) {
+          const int32_t j = nj[r];
+          const float4* jp = reinterpret_cast<const float4*>(cin + j);
+          const float4 jlo = __ldcg(jp), jhi = __ldcg(jp + 1);
+          lo = make_float4(fminf(lo.x, jlo.x), fminf(lo.y, jlo.y), fminf(lo.z, jlo.z), 0.f);
+          hi = make_float4(fmaxf(hi.x, jhi.x), fmaxf(hi.y, jhi.y), fmaxf(hi.z, jhi.z), 0.f);
+          const int32_t nid = (int32_t)(next + mpos + __popc(mb[r] & lt));
+          float4* np = reinterpret_cast<float4*>(B.nodes + nid);
+          np[0] = lo;
+          np[1] = hi;
+          reinterpret_cast<int4*>(np + 2)[0] = make_int4(id, __ldcg(idin + j), 0, 0);
+          id = nid;
+        }
+        if (v) {
+          const uint32_t o = vpos + __popc(vb[r] & lt);
+          float4* op = reinterpret_cast<float4*>(cout + o);
+          op[0] = lo;
+          op[1] = hi;
+          idout[o] = id;
+        }
+      }
+      mpos += __popc(mb[r]);
+      vpos += __popc(vb[r]);
+    }
+  }
+}
+
+// End of an iteration, one thread.
+template <bool GRAPH>
+__global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) ploc_step<GRAPH>(B, handle);
 }
 
 // Move the root (last node) to index 0 and swap every reference to 0 and the root
@@ -355,7 +397,7 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   if ((e = cudaMalloc(&ws.cbox[1], (size_t)cap * sizeof(Box))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&ws.cid[0], (size_t)cap * 4)) != cudaSuccess) return e;
   if ((e = cudaMalloc(&ws.cid[1], (size_t)cap * 4)) != cudaSuccess) return e;
-  // neighbours (cap) + look-back descriptors (tiles, 64-bit) share one allocation
+  // neighbours (cap) + per-tile merge totals / prefixes (64-bit) share one allocation
   size_t desc_words = div_up(cap, kPlocTile) + 8;
   if ((e = cudaMalloc(&ws.nbr, (size_t)cap * 4 + desc_words * 8 + 64)) != cudaSuccess) return e;
   ws.ploc_cap = cap;
@@ -389,7 +431,8 @@ static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n,
     const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3));
     const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
     k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), cs>>>(B, radius);
-    k_ploc_merge<<<mg_grid, kPlocThreads, 0, cs>>>(B);
+    k_ploc_count<<<mg_grid, kPlocThreads, 0, cs>>>(B);
+    k_ploc_scatter<<<mg_grid, kPlocThreads, 0, cs>>>(B);
     k_ploc_step<true><<<1, 32, 0, cs>>>(B, handle);
     cudaGraph_t captured = nullptr;
     cudaError_t e2 = cudaGetLastError();
@@ -452,7 +495,8 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
     const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
     for (uint32_t it = 0; it < cap; ++it) {
       k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), st>>>(B, radius);
-      k_ploc_merge<<<mg_grid, kPlocThreads, 0, st>>>(B);
+      k_ploc_count<<<mg_grid, kPlocThreads, 0, st>>>(B);
+      k_ploc_scatter<<<mg_grid, kPlocThreads, 0, st>>>(B);
       k_ploc_step<false><<<1, 32, 0, st>>>(B, cudaGraphConditionalHandle{});
       if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
           (e = cudaStreamSynchronize(st)) != cudaSuccess)

@@ -95,7 +95,7 @@ typedef struct bvh_timing {
   float emit_ms;     /* hierarchy + refit (LBVH) / cluster init (PLOC) */
   float optimize_ms; /* treelet passes (LBVH+) / clustering loop (PLOC) */
   int32_t ploc_iterations;
-  int32_t reserved;
+  int32_t tree_height;       /* LBVH+: tree height in the last treelet pass (one kernel pair per level) */
   uint64_t ploc_cluster_sum; /* sum of live clusters over PLOC iterations */
 } bvh_timing;
 
