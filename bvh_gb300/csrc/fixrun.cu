@@ -8,7 +8,7 @@
 // ordering each run by (L = code & (2^lbits - 1), position) completes the sort.  On real meshes
 // almost every run has length 1, so this costs one read of the keys instead of four more passes.
 //
-// k_fixrun: one block per tile of 2048 positions.  The block owns the runs that START in its
+// k_fixrun: one block per tile of 1024 positions.  The block owns the runs that START in its
 // tile.  Runs of up to kHalo items are ranked from shared memory (each item's rank is the count
 // of smaller (L, position) pairs in its run) and permuted in place; longer runs are sorted by the
 // owning block with a block-wide stable LSD over L, through the same positions of the other
@@ -20,7 +20,7 @@ namespace bvhgb {
 namespace {
 
 constexpr int kFixThreads = 256;
-constexpr int kFixTile = 2048;
+constexpr int kFixTile = 1024;
 constexpr int kHalo = 64;  // runs up to this length are ranked in shared memory
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kSpan = kFixTile + kHalo + 1;  // positions a-1 .. a+T+kHalo-1
@@ -117,14 +117,13 @@ __device__ void block_sort_run(unsigned long long* keys, uint32_t* vals, unsigne
   }
 }
 
-__global__ void __launch_bounds__(kFixThreads) k_fixrun(unsigned long long* __restrict__ keys,
+__global__ void __launch_bounds__(kFixThreads, 5) k_fixrun(unsigned long long* __restrict__ keys,
                                                         uint32_t* __restrict__ vals,
                                                         unsigned long long* __restrict__ tkeys,
                                                         uint32_t* __restrict__ tvals, uint32_t n, int lbits) {
+  constexpr int kPer = (kSpan + kFixThreads - 1) / kFixThreads;  // positions per thread
   __shared__ uint32_t s_h[kSpan];    // H of position q at q - a + 1
   __shared__ uint32_t s_l[kSpan];    // L
-  __shared__ uint32_t s_dst[kSpan];  // new position of a moved item, or kNone
-  __shared__ uint32_t s_v[kSpan];    // its value
   __shared__ uint32_t s_wh[8 * 256];
   __shared__ uint32_t s_off[256];
   __shared__ uint32_t s_w[8];
@@ -139,8 +138,7 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun(unsigned long long* __re
   const unsigned long long lmask = (1ull << lbits) - 1ull;
   if (t == 0) s_nlong = 0;
   {
-    // all of this thread's loads first (kSpan / 256 + 1 per thread), then the stores
-    constexpr int kPer = (kSpan + kFixThreads - 1) / kFixThreads;
+    // all of this thread's loads first, then the stores
     unsigned long long k[kPer];
 #pragma unroll
     for (int r = 0; r < kPer; ++r) {
@@ -153,14 +151,20 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun(unsigned long long* __re
       if (q < hi) {
         s_h[q - a + 1] = (uint32_t)(k[r] >> lbits);
         s_l[q - a + 1] = (uint32_t)(k[r] & lmask);
-        s_dst[q - a + 1] = kNone;
       }
     }
   }
   __syncthreads();
 #define H(q) s_h[(q) - a + 1]
 #define L(q) s_l[(q) - a + 1]
-  for (uint32_t q = a + t; q < hi; q += kFixThreads) {
+  // this thread's positions a + t + 256 r: new position of a moved item (or kNone) and its value
+  uint32_t dst[kPer], mv[kPer];
+#pragma unroll
+  for (int r = 0; r < kPer; ++r) {
+    dst[r] = kNone;
+    mv[r] = 0;
+    const uint32_t q = a + t + (uint32_t)r * kFixThreads;
+    if (q >= hi) continue;
     const uint32_t h = H(q);
     const bool prev_same = q > 0 && H(q - 1) == h;
     const bool next_same = q + 1 < hi && H(q + 1) == h;
@@ -181,22 +185,23 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun(unsigned long long* __re
     while (e < hi && H(e) == h) ++e;
     // rank by (L, position) within [s, e)
     const uint32_t l = L(q);
-    uint32_t r = 0;
+    uint32_t rank = 0;
     for (uint32_t j = s; j < e; ++j) {
       const uint32_t lj = L(j);
-      r += (lj < l) || (lj == l && j < q);
+      rank += (lj < l) || (lj == l && j < q);
     }
-    if (s + r != q) {
-      s_dst[q - a + 1] = s + r;
-      s_v[q - a + 1] = vals[q];
+    if (s + rank != q) {
+      dst[r] = s + rank;
+      mv[r] = vals[q];
     }
   }
-  __syncthreads();
-  for (uint32_t q = a + t; q < hi; q += kFixThreads) {
-    const uint32_t d = s_dst[q - a + 1];
-    if (d != kNone) {
-      keys[d] = ((unsigned long long)H(q) << lbits) | L(q);
-      vals[d] = s_v[q - a + 1];
+  __syncthreads();  // every item of the block's runs has been read
+#pragma unroll
+  for (int r = 0; r < kPer; ++r) {
+    if (dst[r] != kNone) {
+      const uint32_t q = a + t + (uint32_t)r * kFixThreads;
+      keys[dst[r]] = ((unsigned long long)H(q) << lbits) | L(q);
+      vals[dst[r]] = mv[r];
     }
   }
   __syncthreads();
