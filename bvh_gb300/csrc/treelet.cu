@@ -21,6 +21,9 @@ namespace bvhgb {
 
 constexpr int kTlMax = 7;
 constexpr float kTlInf = 1e30f;
+}  // namespace bvhgb
+#include "treelet_dp_unrolled.cuh"
+namespace bvhgb {
 
 __device__ __forceinline__ Box ldcg_box(const Node* nodes, int32_t idx) {
   const float4* p = reinterpret_cast<const float4*>(nodes + idx);
@@ -333,12 +336,10 @@ __device__ __forceinline__ void reg_grow(const Node* nodes, int32_t root, const 
   T.n = cnt;
 }
 
-// Subset DP (:119-165) by one lane.  Subsets in increasing numeric order (every proper subset
-// comes first); the splits of s are the nonempty subsets p of s minus its lowest member, in
-// increasing order, first minimum kept.  The box of s is (its leaves among 3..6) U (among 0..2).
-// C and P are this lane's columns of the warp's tables (stride 32).
-__device__ __forceinline__ void reg_dp(const RegTreelet& T, float* C, uint8_t* P) {
-  const uint32_t full = (1u << T.n) - 1u;
+// Areas of the subsets s < 2^nv with two or more leaves into this lane's column A (stride 32):
+// the box of s is (its leaves among 3..6) U (its leaves among 0..2).
+__device__ __forceinline__ void reg_areas(const RegTreelet& T, int nv, float* A) {
+  const uint32_t full = (1u << nv) - 1u;
   Box lo8[8];
   lo8[0] = box_empty();
   lo8[1] = box_union(lo8[0], T.b[0]);
@@ -356,27 +357,18 @@ __device__ __forceinline__ void reg_dp(const RegTreelet& T, float* C, uint8_t* P
 #pragma unroll
     for (int lo = 0; lo < 8; ++lo) {
       const uint32_t s = hi * 8u + (uint32_t)lo;
-      if (s == 0u || s > full) continue;
-      if (__popc(s) == 1) {
-        C[s * 32u] = 0.0f;
-        continue;
-      }
-      const float a = box_area(box_union(bh, lo8[lo]));
-      const uint32_t delta = s & (s - 1u);
-      float best = kTlInf;
-      uint32_t bp = 0xffu;
-      for (uint32_t p = delta & (0u - delta); p; p = (p - delta) & delta) {
-        const float c = __fadd_rn(C[p * 32u], C[(s ^ p) * 32u]);
-        if (c < best) {
-          best = c;
-          bp = p;
-        }
-      }
-      // the reference starts from INF with strict <, so an all-INF subset keeps INF / -1
-      C[s * 32u] = __fadd_rn(best, a);
-      P[s * 32u] = (uint8_t)bp;
+      if (s <= full && __popc(s) > 1) A[s * 32u] = box_area(box_union(bh, lo8[lo]));
     }
   }
+}
+
+// Subset DP (:119-165) by one lane for up to nv leaves, straight-line code with the costs in
+// registers (treelet_dp_unrolled.cuh); best splits into this lane's column P.
+__device__ __forceinline__ void reg_dp(int nv, const float* A, uint8_t* P) {
+  if (nv <= 4) dp_unrolled_4(A, P);
+  else if (nv == 5) dp_unrolled_5(A, P);
+  else if (nv == 6) dp_unrolled_6(A, P);
+  else dp_unrolled_7(A, P);
 }
 
 // Id reuse (:167-191): the treelet's internal nodes in DFS order from the root, right child
@@ -628,23 +620,30 @@ __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, 
   }
   float* C = s_cost + lane;
   uint8_t* P = s_part + lane;
-  for (uint32_t k = b + blockIdx.x * kLvThreads + lane; k < e; k += gridDim.x * kLvThreads) {
+  // warp-uniform loop: the warp runs the DP variant of its largest treelet
+  for (uint32_t kb = b + blockIdx.x * kLvThreads; kb < e; kb += gridDim.x * kLvThreads) {
+    const uint32_t k = kb + lane;
+    const bool act = k < e;
     const uint32_t q = k - b;
-    const uint32_t w0 = __ldcg(desc + q);
+    const uint32_t w0 = act ? __ldcg(desc + q) : 0u;
     RegTreelet T;
     T.n = (int)(w0 & 255u);
-    if (T.n < 2) continue;
     const int na = (int)(w0 >> 8);
 #pragma unroll
     for (int i = 0; i < kTlMax; ++i) {
-      T.id[i] = (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q);
+      T.id[i] = i < T.n ? (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q) : 0;
       T.b[i] = i < T.n ? ldcg_box(nodes, T.id[i]) : box_empty();
     }
-    int avail[kTlMax];
+    const int nv = (int)__reduce_max_sync(0xffffffffu, (uint32_t)T.n);
+    if (nv < 2) continue;
+    reg_areas(T, nv, C);
+    reg_dp(nv, C, P);
+    if (T.n >= 2) {
+      int avail[kTlMax];
 #pragma unroll
-    for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
-    reg_dp(T, C, P);
-    reg_build<32>(nodes, T, P, avail, na);
+      for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
+      reg_build<32>(nodes, T, P, avail, na);
+    }
   }
 }
 
