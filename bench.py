@@ -270,7 +270,7 @@ def run_ours(args):
         ctx.sync()
         # per-stage device times from the library's stage events, one build at a time
         for _ in range(min(args.steps, 10)):
-            ctx.build_device(ptrs, n, params, s)
+            tree = ctx.build_device(ptrs, n, params, s)
             t = ctx.last_timing()
             stages.append((t.bounds_ms, t.morton_ms, t.sort_ms, t.emit_ms, t.optimize_ms, t.total_ms))
             ploc_iters, ploc_csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
@@ -305,6 +305,34 @@ def run_ours(args):
     if algo == "ploc":
         roofline["ploc"] = {"iterations": ploc_iters, "cluster_sum": ploc_csum}
     stage_ms = {k: round(v, 4) for k, v in shares.items()}
+
+    # --- tree quality: evaluator statistics on the GPU, 1920x1080 pinhole primary rays -----
+    quality = None
+    with torch.cuda.stream(stream):
+        quality = ctx.evaluate(tree.nodes, tree.n_nodes, s)
+        root = np.zeros(1, C.NODE_DTYPE)
+        xs, ys, zs = mesh.arrays()[0::3], mesh.arrays()[1::3], mesh.arrays()[2::3]
+        root["min"][0] = [min(a.min() for a in xs), min(a.min() for a in ys), min(a.min() for a in zs)]
+        root["max"][0] = [max(a.max() for a in xs), max(a.max() for a in ys), max(a.max() for a in zs)]
+        cam = bvh_gb300.auto_camera(root[0])
+        W, Hh = 1920, 1080
+        hits = [torch.empty(W * Hh, dtype=torch.float32, device=dev)] + \
+               [torch.empty(W * Hh, dtype=torch.int32, device=dev) for _ in range(4)]
+        hp = [h.data_ptr() for h in hits]
+        ctx.trace_pinhole(tree.nodes, tree.n_nodes, ptrs, n, cam, W, Hh, hp, s)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            ctx.trace_pinhole(tree.nodes, tree.n_nodes, ptrs, n, cam, W, Hh, hp, s)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        tr_ms = e0.elapsed_time(e1) / 3
+        quality.update({"pinhole_rays": W * Hh, "avg_nodes_visited": round(float(hits[2].double().mean()), 3),
+                        "hit_fraction": round(float((hits[1] >= 0).double().mean()), 4),
+                        "trace_ms": round(tr_ms, 3), "trace_mrays_per_s": round(W * Hh / (tr_ms / 1e3) / 1e6, 1)})
+        quality["sah"] = round(quality["sah"], 3)
+        quality["avg_leaf_depth"] = round(quality["avg_leaf_depth"], 3)
 
     # --- end to end through the C ABI with pinned host buffers ----------------------------
     h_in = [torch.from_numpy(a).pin_memory() for a in mesh.arrays()]
@@ -343,6 +371,7 @@ def run_ours(args):
                    "morton_bits": bits, "ploc_radius": radius or None, "parallelism": f"replicas x{ws}",
                    "l2": "inputs (360 MB) and per-build writes exceed the 129 MB L2; no flush"},
         "stage_ms_median": stage_ms,
+        "quality": quality,
         "roofline": roofline,
         "e2e": e2e,
         "gpu_launches": args.steps * kernels_per_build(algo, bits, rounds, ploc_iters, tree_height),
@@ -585,6 +614,53 @@ def run_serve(args):
         print(json.dumps(line), flush=True)
 
 
+def run_reference_batched(args, ref, sample_meshes: int = 256):
+    """Config 3 on the reference: it has no batched builder, so its LBVH builder runs once per
+    mesh (the loop a BLAS build would need), on a bounded sample of the batch's meshes."""
+    from bvh_gb300 import meshgen
+    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    counts = meshgen.batch_counts(kw["meshes"], kw["lo"], kw["hi"], seed=4)
+    mesh, offsets = meshgen.batch(counts, seed=5)
+    arrays = mesh.arrays()
+    k = min(sample_meshes, counts.shape[0])
+    parts = [[a[offsets[m]:offsets[m + 1]] for a in arrays] for m in range(k)]
+    R = ref.RefRunner(fast=True)
+    for m in range(min(8, k)):
+        R.lbvh(parts[m])
+    tris = int(offsets[k])
+    builds, walls = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            b = w = 0.0
+            for m in range(k):
+                _, _, ms = R.lbvh(parts[m])
+                b += float(ms[0])
+                w += float(ms[6])
+            builds.append(b)
+            walls.append(w)
+    b = float(np.mean(builds))
+    w = float(np.mean(walls))
+    value = tris / (b / 1e3) / 1e6
+    print(json.dumps({
+        "impl": "reference", "metric": "batched build Mtris/s (device-resident) vs per-mesh loop",
+        "value": round(value, 2), "unit": "Mtris/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(b, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+u32", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
+        "config": {"workload": args.workload, "description": desc, "meshes_sampled": k, "triangles_sampled": tris,
+                   "reference_builder": "LBVHBuilderCUDA (30-bit) once per mesh: the reference has no batched "
+                                        "builder",
+                   "how": "the reference's own kernels (its .cu files compiled unmodified, Release flags) "
+                          "replayed in its host order; value from the sum of its getLastBuildTimeMS"},
+        "e2e": {"value": round(tris / (w / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * tris,
+                "d2h_bytes_per_step": 48 * (2 * tris - k) + 4 * tris, "ms_per_step": round(w, 3),
+                "note": "wall time of the per-mesh build() calls: upload, kernels, download, AoS conversion"},
+        "cpu_baseline": {"value": round(value, 2), "unit": "Mtris/s", "cores": 1, "kind": "reference",
+                         "sample": f"first {k} of {counts.shape[0]} meshes ({tris:,} triangles) on the GPU "
+                                   "(the reference path is CUDA)"},
+        "clocks": clk.summary(),
+    }), flush=True)
+
+
 def run_reference(args):
     ws, rank, local = dist_info()
     if rank != 0:
@@ -594,6 +670,13 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref fatbins) not built"}))
         return
     gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    if algo == "serve":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving path (no request "
+                          "queue, admission or overlapped builds); nothing of it can run this workload"}))
+        return
+    if algo == "lbvh_batched":
+        run_reference_batched(args, ref)
+        return
     mesh = make_mesh(args.workload)
     n = mesh.size()
     R = ref.RefRunner(fast=True)

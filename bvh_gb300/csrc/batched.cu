@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) k_seg_bounds(MeshPtrs m, const SegItem* _
 }
 
 __global__ void __launch_bounds__(256) k_seg_morton(MeshPtrs m, const SegItem* __restrict__ items, uint32_t n_items,
-                                                    const float* __restrict__ mbox, int passes,
+                                                    const float* __restrict__ mbox, int passes, int shift0,
                                                     unsigned long long* __restrict__ keys, Box* __restrict__ boxes,
                                                     uint32_t* __restrict__ scratch, ScratchLayout L) {
   __shared__ uint32_t s_hist[kMaxPasses][256];
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_seg_morton(MeshPtrs m, const SegItem* _
       float4* bp = reinterpret_cast<float4*>(boxes + i);
       bp[0] = make_float4(lo[0], lo[1], lo[2], 0.f);
       bp[1] = make_float4(hi[0], hi[1], hi[2], 0.f);
-      for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(uint32_t)(key >> (8 * p)) & 255u], 1u);
+      for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(uint32_t)(key >> (shift0 + 8 * p)) & 255u], 1u);
     }
   }
   __syncthreads();
@@ -148,19 +148,28 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   ScratchLayout L = scratch_layout(ws.cap_n);
   int mbits = 1;
   while (mbits < 34 && (1ull << mbits) < count) ++mbits;
-  const int passes = (30 + mbits + 7) / 8;
+  // keys have 30 + mbits bits: up to 32 are sorted whole; longer keys are sorted by their high
+  // 32 bits and the runs of equal high bits are then ordered by the rest (sort_fix_runs)
+  const int kbits = 30 + mbits;
+  const int shift0 = kbits > 32 ? kbits - 32 : 0;
+  const int passes = kbits > 32 ? 4 : (kbits + 7) / 8;
   L.zero_end = L.desc + (size_t)passes * div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_variant_tile(8, ws.sort_variant[1])) * 256;
   if (evs && evs->use) cudaEventRecord(evs->ev[0], st);
   k_seg_init<<<152 * 4, 256, 0, st>>>(d_mbox, count, ws.scratch, L);
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(n_items, 152 * 8));
   k_seg_bounds<<<grid, 256, 0, st>>>(m, d_items, n_items, d_mbox);
   if (evs && evs->use) cudaEventRecord(evs->ev[1], st);
-  k_seg_morton<<<grid, 256, 0, st>>>(m, d_items, n_items, d_mbox, passes,
+  k_seg_morton<<<grid, 256, 0, st>>>(m, d_items, n_items, d_mbox, passes, shift0,
                                                 reinterpret_cast<unsigned long long*>(ws.keys[0]), ws.boxes,
                                                 ws.scratch, L);
   if (evs && evs->use) cudaEventRecord(evs->ev[2], st);
   int fb = 0;
-  if ((e = run_sort_u64(ws, n, passes, st, L, &fb)) != cudaSuccess) return e;
+  if ((e = run_sort_u64(ws, n, passes, st, L, &fb, shift0)) != cudaSuccess) return e;
+  if (shift0 > 0 &&
+      (e = sort_fix_runs(reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb],
+                         reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, shift0, st)) !=
+          cudaSuccess)
+    return e;
   if (evs && evs->use) cudaEventRecord(evs->ev[3], st);
   const unsigned long long* keys = reinterpret_cast<const unsigned long long*>(ws.keys[fb]);
   k_delta<unsigned long long, true><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], d_offsets, ws.delta, n);

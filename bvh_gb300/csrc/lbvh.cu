@@ -650,8 +650,8 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
 }
 
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
-                         int* final_buf) {
-  return run_sort<unsigned long long>(ws, n, passes, st, L, final_buf);
+                         int* final_buf, int shift0) {
+  return run_sort<unsigned long long>(ws, n, passes, st, L, final_buf, shift0);
 }
 
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,

@@ -141,8 +141,9 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
 constexpr size_t kTlCtlWord = 256 + 264 + 256;
 
 // Stable sort of ws.keys[0] (64-bit) with implicit indices over `passes` 8-bit digits.
+// `passes` stable 8-bit LSD passes over 64-bit keys, starting at bit shift0.
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
-                         int* final_buf);
+                         int* final_buf, int shift0 = 0);
 
 // A slice of one mesh handled by one block of the batched per-mesh kernels.
 struct SegItem {

@@ -57,6 +57,24 @@ def test_batched_log_uniform(ctx, gpu, oracle_lib):
     _check_batch(ctx, gpu, mesh, offsets, oracle=oracle_lib)
 
 
+def test_batched_few_meshes_whole_key_sort(ctx, gpu, oracle_lib):
+    """At most 4 meshes: 32-bit keys, sorted whole (no run fix-up)."""
+    mesh, offsets = meshgen.batch([3000, 17, 4097, 1], seed=16)
+    _check_batch(ctx, gpu, mesh, offsets, oracle=oracle_lib)
+
+
+def test_batched_long_runs(ctx, gpu, oracle_lib):
+    """Meshes of identical triangles: runs of equal high key bits longer than 64 (the fix-up's
+    block-wide path) inside a batch of 10 meshes."""
+    from tests import meshes as M
+    parts = [M.identical(3000), meshgen.uniform_small(2000, seed=3), M.identical(70), M.dense_cell(5000)]
+    parts += [meshgen.uniform_small(100 + 37 * k, seed=20 + k) for k in range(6)]
+    arrays = [np.concatenate([p.arrays()[k] for p in parts]) for k in range(9)]
+    mesh = TriangleMesh(*arrays)
+    offsets = np.concatenate([[0], np.cumsum([p.size() for p in parts])]).astype(np.int64)
+    _check_batch(ctx, gpu, mesh, offsets, oracle=oracle_lib)
+
+
 def test_batched_graph_replay(ctx, gpu):
     counts = meshgen.batch_counts(100, 64, 8000, seed=14)
     mesh, offsets = meshgen.batch(counts, seed=15)
