@@ -6,7 +6,8 @@ interface.
 """
 from ._capi import (ALGO_LBVH, ALGO_LBVH_PLUS, ALGO_PLOC, NODE_DTYPE, BVHError, load_library)  # noqa: F401
 from .builders import (BVHBuilder, Context, LBVHBuilder, LBVHPlusBuilder, PLOCBuilder, TriangleMesh,  # noqa: F401
-                       auto_camera)
+                       auto_camera, load_obj)
 
 __all__ = ["ALGO_LBVH", "ALGO_LBVH_PLUS", "ALGO_PLOC", "NODE_DTYPE", "BVHError", "BVHBuilder", "Context",
-           "LBVHBuilder", "LBVHPlusBuilder", "PLOCBuilder", "TriangleMesh", "auto_camera", "load_library"]
+           "LBVHBuilder", "LBVHPlusBuilder", "PLOCBuilder", "TriangleMesh", "auto_camera", "load_library",
+           "load_obj"]

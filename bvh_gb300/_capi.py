@@ -82,6 +82,10 @@ class EvalStats(ctypes.Structure):
                 ("leaf_count", c_uint64), ("max_depth", c_uint32), ("reserved", c_uint32)]
 
 
+class ObjMesh(ctypes.Structure):
+    _fields_ = [("v", POINTER(ctypes.c_float) * 9), ("n", c_uint32), ("pinned", c_uint32), ("vertices", c_uint64)]
+
+
 class ServeConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", c_uint64), ("slots", c_int32), ("morton_bits", c_int32), ("device", c_int32),
                 ("max_triangles", c_uint32), ("max_rays", c_uint32), ("reserved", c_int32 * 3)]
@@ -127,6 +131,8 @@ SIGNATURES = {
     "bvh_tuning_set": (c_int, [c_void_p, c_int32, c_int32]),
     "bvh_build_lbvh_static": (c_int, [POINTER(MeshSoA), c_int32, c_void_p, c_void_p, c_void_p]),
     "bvh_evaluate": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p, POINTER(EvalStats)]),
+    "bvh_load_obj": (c_int, [ctypes.c_char_p, c_int32, c_int32, POINTER(ObjMesh)]),
+    "bvh_obj_free": (None, [POINTER(ObjMesh)]),
     "bvh_serve_default_config": (ServeConfig, []),
     "bvh_serve_open": (c_int, [POINTER(ServeConfig), POINTER(c_void_p)]),
     "bvh_serve_submit": (c_int, [c_void_p, POINTER(ServeRequest)]),

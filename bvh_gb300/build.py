@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libbvh_gb300.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 
-SOURCES = ["lbvh.cu", "treelet.cu", "ploc.cu", "trace.cu", "batched.cu", "capi.cu", "noalloc.cu", "serve.cu", "evaluate.cu", "fixrun.cu"]
+SOURCES = ["lbvh.cu", "treelet.cu", "ploc.cu", "trace.cu", "batched.cu", "capi.cu", "noalloc.cu", "serve.cu", "evaluate.cu", "fixrun.cu", "objload.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
               "--expt-relaxed-constexpr"]

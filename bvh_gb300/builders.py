@@ -199,6 +199,18 @@ class Context:
                                            ctypes.c_void_p(stream)), "bvh_trace_pinhole")
 
 
+def load_obj(path: str, threads: int = 0) -> "TriangleMesh":
+    """loadOBJ (src/loader.cpp:10-74) as a multi-threaded parse straight to SoA (bvh_load_obj)."""
+    lib = C.load_library()
+    m = C.ObjMesh()
+    C.check(lib.bvh_load_obj(str(path).encode(), int(threads), 0, ctypes.byref(m)), "bvh_load_obj")
+    try:
+        arrays = [np.ctypeslib.as_array(m.v[k], shape=(max(m.n, 1),))[: m.n].copy() for k in range(9)]
+    finally:
+        lib.bvh_obj_free(ctypes.byref(m))
+    return TriangleMesh(*arrays)
+
+
 def auto_camera(root_node) -> C.Camera:
     """autoCamera (src/render_engine.cu:601-637) from a host root node (NODE_DTYPE record) or None."""
     lib = C.load_library()

@@ -261,6 +261,23 @@ bvh_status bvh_serve_stats_get(bvh_server* sv, bvh_serve_stats* out);
 /* Finish every queued request, then release the server. */
 bvh_status bvh_serve_close(bvh_server* sv);
 
+/* ---------------------------------------------------------------------------------------
+ * OBJ input: loadOBJ (src/loader.cpp:10-74) as a multi-threaded parse straight to SoA.
+ * ------------------------------------------------------------------------------------- */
+typedef struct bvh_obj_mesh {
+  float* v[9];       /* v0x v0y v0z v1x v1y v1z v2x v2y v2z, n floats each (library-owned) */
+  uint32_t n;        /* triangles */
+  uint32_t pinned;   /* arrays are page-locked (cudaMallocHost) */
+  uint64_t vertices; /* 'v' lines read */
+} bvh_obj_mesh;
+/* Same rules as loadOBJ: '#' and empty lines skipped; "v x y z"; "f" with v, v/vt, v//vn or
+ * v/vt/vn tokens, negative indices counting back from the vertices read so far; fan
+ * triangulation; a triangle with an index outside the vertices read so far is skipped.
+ * threads <= 0: all hardware threads.  pinned != 0: page-locked arrays (fast upload).
+ * BVH_ERR_INVALID_ARG for an unreadable file or an index loadOBJ's std::stoi would reject. */
+bvh_status bvh_load_obj(const char* path, int32_t threads, int32_t pinned, bvh_obj_mesh* out);
+void bvh_obj_free(bvh_obj_mesh* m);
+
 /* Tree statistics (BVHEvaluator::evaluate, src/evaluator.cpp:7-113) computed on the GPU for a
  * device node array: SAH with the reference's costs (3 per internal node, 2 per leaf, areas
  * relative to the root), reachable node and leaf counts, maximum and average leaf depth.  The

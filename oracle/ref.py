@@ -18,6 +18,22 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 
 
+def loader_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libref_loader.so"))
+
+
+def ref_load_obj(path: str):
+    """The reference's loadOBJ on `path`: nine float32 arrays, or None when it throws."""
+    lib = ctypes.CDLL(os.path.join(REF_DIR, "libref_loader.so"))
+    out = (ctypes.POINTER(ctypes.c_float) * 9)()
+    n = ctypes.c_uint32(0)
+    if lib.ref_load_obj(path.encode(), out, ctypes.byref(n)):
+        return None
+    arrays = [np.ctypeslib.as_array(out[k], shape=(max(n.value, 1),))[: n.value].copy() for k in range(9)]
+    lib.ref_free(out)
+    return arrays
+
+
 def eval_available() -> bool:
     return os.path.exists(os.path.join(REF_DIR, "libref_eval.so"))
 

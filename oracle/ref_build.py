@@ -5,6 +5,7 @@
     to sm_103a device code with the reference's default (non-Release) flags; *_fast.fatbin with
     its Release flags (-O3 --use_fast_math, CMakeLists.txt:41-45).
   - libref_eval.so: the reference's src/evaluator.cpp with ref_eval_shim.cpp (host only).
+  - libref_loader.so: the reference's src/loader.cpp with ref_loader_shim.cpp (host only).
 * Anywhere (GPU machine included): libref_runner.so from ref_runner.cu (our host code that loads the
   fatbins and replays the reference builders with CUB/Thrust).
 """
@@ -61,6 +62,13 @@ def build_eval():
           "-o", os.path.join(OUT, "libref_eval.so")])
 
 
+def build_loader():
+    _run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC",
+          "-I" + os.path.join(REF_ROOT, "include"), "-I/usr/local/cuda/include",
+          os.path.join(HERE, "ref_loader_shim.cpp"), os.path.join(REF_ROOT, "src", "loader.cpp"),
+          "-o", os.path.join(OUT, "libref_loader.so")])
+
+
 def build_runner():
     _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
                              os.path.join(HERE, "ref_runner.cu"), "-o", os.path.join(OUT, "libref_runner.so"),
@@ -76,6 +84,7 @@ def build(runner: bool = True):
     if have_reference():
         build_fatbins()
         build_eval()
+        build_loader()
     if runner and fatbins_present():
         build_runner()
 
