@@ -109,12 +109,13 @@ struct Climb {
   bool internal;
 };
 
-template <typename Seg, bool PARENTS>
-__global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
-                                              const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
-                                              uint32_t n, Seg seg, uint32_t* __restrict__ out_idx,
-                                              uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count) {
-  constexpr uint32_t T = 256;
+// T sorted positions per block, one thread each (a larger block leaves fewer nodes whose sibling
+// lies in another block to the frontier pass).
+template <typename Seg, bool PARENTS, uint32_t T = 256>
+__global__ void __launch_bounds__(T) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
+                                            const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
+                                            uint32_t n, Seg seg, uint32_t* __restrict__ out_idx,
+                                            uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count) {
   // D of positions bbase-1 .. bbase+T-1 (0 outside [0, n-1) : a segment boundary)
   __shared__ uint8_t s_D[T + 1];
   // rendezvous slot k <-> split gamma = bbase + k: one side per child (0 left, 1 right)
