@@ -120,6 +120,15 @@ STAGE_KERNELS = {
                             " per iteration + k_ploc_root",
 }
 
+# DRAM bytes per triangle (dram__bytes_read.sum + dram__bytes_write.sum over the stage's kernels)
+# from one ncu capture of a smaller case of the same distribution, whose buffers exceed the L2;
+# the stage's traffic grows with the triangle count, so a launch over n triangles moves about
+# n times this.  Keyed by (algorithm, Morton bits, stage).
+MEASURED_TRAFFIC_PER_TRI = {
+    ("lbvh", 63, "emit_refit"): (194.8, "profiles/emit_fixrun_c1_4m.md: k_delta + k_emit + k_emit_climb at 4M, "
+                                        "779 MB / 4M triangles, scaled by the triangle count"),
+}
+
 
 def hbm_peak():
     try:
@@ -297,8 +306,11 @@ def run_ours(args):
     whole = bytes_per_tri(algo, bits, rounds, csum)
     build_gbs = whole * n / (med[5] / 1e3) / 1e9
     kernels = "k_ploc_init" if (algo == "ploc" and dom == "emit_refit") else STAGE_KERNELS[dom]
+    measured = MEASURED_TRAFFIC_PER_TRI.get((algo, bits, dom))
+    traffic = round(measured[0] * n) if measured else None
     roofline = {"bound": "hbm", "kernel": dom, "kernels": kernels, "achieved": round(achieved, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "traffic_source": measured[1] if measured else "no capture of this stage at this workload",
                 "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": round(per_unit, 2),
                 "whole_build": {"bytes_per_tri": round(whole, 2), "achieved": round(build_gbs, 1),
                                 "frac": round(build_gbs / peak, 4), "median_build_ms": round(med[5], 4)}}
