@@ -138,6 +138,20 @@ __device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long 
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Lanes of the (full) warp whose low NB bits of d equal this lane's: one ballot per bit, a cost
+// independent of how many distinct values the warp holds (match.any's grows with it).
+template <int NB>
+__device__ __forceinline__ uint32_t warp_match_bits(uint32_t d) {
+  uint32_t m = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? bal : ~bal;
+  }
+  return m;
+}
+
 // Decoupled look-back over tiles (Merrill & Garland): descriptor words hold a 2-bit flag and the
 // value in one word, so relaxed loads suffice.  Predecessors are read W at a time to shorten the
 // dependent chain; an unpublished word (flag 0) is polled again, at most kSpinLimit times.

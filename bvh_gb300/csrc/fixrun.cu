@@ -45,7 +45,8 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_w
 // Stable LSD sort of keys[s, s+m) / vals[s, s+m) by the low `lbits` bits of the key, by the
 // calling block alone, ping-ponging through tkeys/tvals at the same positions; an even number
 // of 8-bit passes leaves the result in keys/vals.  Items are ranked in chunks of 2048 in their
-// current order (warp w takes chunk items w*256 .. w*256+255), so equal digits keep their order.
+// current order (warp w takes chunk items w*256 .. w*256+255), so equal digits keep their order
+// (a warp's shared atomics execute in issue order).
 __device__ void block_sort_run(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys,
                                uint32_t* tvals, uint32_t s, uint32_t m, int lbits, uint32_t* s_wh,
                                uint32_t* s_off, uint32_t* s_w) {
@@ -81,16 +82,11 @@ __device__ void block_sort_run(unsigned long long* keys, uint32_t* vals, unsigne
         key[k] = ok ? sk[s + i] : 0ull;
         val[k] = ok ? sv[s + i] : 0u;
         dig[k] = ok ? (uint32_t)(key[k] >> sh) & 255u : 256u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, dig[k]);
-        const uint32_t leader = __ffs(peers) - 1;
+        const uint32_t peers = warp_match_bits<9>(dig[k]);
+        const uint32_t leader = 31u - __clz(peers);
         uint32_t old = 0;
-        if (lane == leader && dig[k] < 256u) {
-          old = wh[dig[k]];
-          wh[dig[k]] = old + __popc(peers);
-        }
-        old = __shfl_sync(0xffffffffu, old, leader);
-        rnk[k] = old + __popc(peers & lt);
-        __syncwarp();
+        if (lane == leader && dig[k] < 256u) old = atomicAdd(wh + dig[k], (uint32_t)__popc(peers));
+        rnk[k] = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt);
       }
       __syncthreads();
       // per bin: exclusive prefix over the warps, chunk count

@@ -285,6 +285,27 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan_u64(unsigned 
   return before + x - v;
 }
 
+// Stable warp-local ranking of the warp's 32 x IPT items (item k of lane l is the warp's item
+// 32k + l, so (k, lane) order is input order).  NB = 8 for a full tile; NB = 9 gives the items
+// past n the digit 256, which is matched but never counted.  The leader of each group of equal
+// digits reserves the group's slots with one shared atomic; the atomics of one warp execute in
+// issue order, so earlier items of a digit always get the lower ranks.
+template <int NB, typename K, int IPT>
+__device__ __forceinline__ void warp_rank(const K (&key)[IPT], uint32_t (&rnk)[IPT], int shift, uint32_t wbase,
+                                          uint32_t n, uint32_t* wh, uint32_t lane) {
+  const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    uint32_t d = (uint32_t)(key[k] >> shift) & 255u;
+    if (NB > 8 && wbase + (uint32_t)k * 32u + lane >= n) d = 256u;
+    const uint32_t peers = warp_match_bits<NB>(d);
+    const uint32_t leader = 31u - __clz(peers);
+    uint32_t old = 0;
+    if (lane == leader && d < 256u) old = atomicAdd(wh + d, (uint32_t)__popc(peers));
+    rnk[k] = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt);
+  }
+}
+
 template <typename K, int THREADS, int IPT, int W, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                       K* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
@@ -295,10 +316,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict_
   extern __shared__ __align__(16) unsigned char smem[];
   K* s_keys = reinterpret_cast<K*>(smem);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
-  uint32_t* s_whist = s_vals + TILE;          // NW x BINS
-  uint32_t* s_binstart = s_whist + NW * BINS; // BINS
-  uint32_t* s_gstart = s_binstart + BINS;     // BINS
-  unsigned long long* s_scan = reinterpret_cast<unsigned long long*>(s_gstart + BINS);  // 32
+  uint32_t* s_whist = s_vals + TILE;          // NW x BINS: warp counts, then each warp's tile offset per bin
+  uint32_t* s_gdelta = s_whist + NW * BINS;   // BINS: output position of tile item i is s_gdelta[digit] + i
+  unsigned long long* s_scan = reinterpret_cast<unsigned long long*>(s_gdelta + 2 * BINS);  // 32
   uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_scan + 32);
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -317,71 +337,64 @@ __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict_
   for (int k = 0; k < IPT; ++k) {
     uint32_t idx = wbase + (uint32_t)k * 32u + lane;
     bool ok = idx < n;
-    key[k] = ok ? kin[idx] : K(0);
-    val[k] = ok ? (vin ? vin[idx] : idx) : 0u;
+    key[k] = ok ? __ldcs(kin + idx) : K(0);
+    val[k] = ok ? (vin ? __ldcs(vin + idx) : idx) : 0u;
   }
-  // stable warp-local ranking: items in (k, lane) order == original order within the warp
   uint32_t* wh = s_whist + w * BINS;
-  const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    uint32_t idx = wbase + (uint32_t)k * 32u + lane;
-    uint32_t d = idx < n ? (uint32_t)(key[k] >> shift) & 255u : 256u;
-    uint32_t peers = __match_any_sync(0xffffffffu, d);
-    uint32_t leader = __ffs(peers) - 1;
-    uint32_t old = 0;
-    if (lane == leader && d < 256u) {
-      old = wh[d];
-      wh[d] = old + __popc(peers);
-    }
-    old = __shfl_sync(0xffffffffu, old, leader);
-    rnk[k] = old + __popc(peers & lt);
-    __syncwarp();
-  }
+  if (base + (uint32_t)TILE <= n) warp_rank<8>(key, rnk, shift, wbase, n, wh, (uint32_t)lane);
+  else warp_rank<9>(key, rnk, shift, wbase, n, wh, (uint32_t)lane);
   __syncthreads();
-  // per bin: exclusive prefix over warps, tile count
+  // per bin: the tile count, its exclusive scan over bins, and each warp's offset in tile order
   const int b = tid;
+  uint32_t wc[NW];
   uint32_t cnt = 0;
 #pragma unroll
   for (int ww = 0; ww < NW; ++ww) {
-    uint32_t c = s_whist[ww * BINS + b];
-    s_whist[ww * BINS + b] = cnt;
-    cnt += c;
+    wc[ww] = s_whist[ww * BINS + b];
+    cnt += wc[ww];
   }
   const uint32_t ghist = __ldcg(scratch + L.hist + pass * BINS + b);
   unsigned long long packed = ((unsigned long long)ghist << 32) | cnt;
   unsigned long long ex = block_exclusive_scan_u64<THREADS>(packed, s_scan);
-  s_binstart[b] = (uint32_t)ex;                 // tile-local start of bin b
+  const uint32_t binstart = (uint32_t)ex;         // tile-local start of bin b
   const uint32_t binbase = (uint32_t)(ex >> 32);  // global start of bin b
   // publish this tile's count first so that successors can proceed
   uint32_t* desc = scratch + L.desc + ((size_t)pass * tiles) * BINS;
   st_relaxed(desc + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | cnt);
-  __syncthreads();  // s_binstart complete
+  {
+    uint32_t run = binstart;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) {
+      s_whist[ww * BINS + b] = run;
+      run += wc[ww];
+    }
+  }
+  __syncthreads();  // warp offsets complete
   // local scatter into tile order (independent of the global offsets); frees the key registers
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
     uint32_t idx = wbase + (uint32_t)k * 32u + lane;
     if (idx < n) {
       uint32_t d = (uint32_t)(key[k] >> shift) & 255u;
-      uint32_t pos = s_binstart[d] + s_whist[w * BINS + d] + rnk[k];
+      uint32_t pos = wh[d] + rnk[k];
       s_keys[pos] = key[k];
       s_vals[pos] = val[k];
     }
   }
-  // decoupled look-back on bin b, 32 predecessors per round
+  // decoupled look-back on bin b, W predecessors per round
   uint32_t excl = 0;
   if (tile != 0) {
     excl = lookback<W, uint32_t>(desc + b, BINS, (int64_t)tile, ~kValMask, kFlagInc, scratch + L.status,
                                  kStatusSortTimeout);
     st_relaxed(desc + (size_t)tile * BINS + b, kFlagInc | (excl + cnt));
   }
-  s_gstart[b] = binbase + excl;
+  s_gdelta[b] = binbase + excl - binstart;
   __syncthreads();
   const uint32_t len = min((uint32_t)TILE, n - base);
   for (uint32_t i = tid; i < len; i += THREADS) {
     K kk = s_keys[i];
     uint32_t d = (uint32_t)(kk >> shift) & 255u;
-    uint32_t dst = s_gstart[d] + (i - s_binstart[d]);
+    uint32_t dst = s_gdelta[d] + i;
     if (dst < n) {  // always true unless a look-back wait gave up (status already set)
       kout[dst] = kk;
       vout[dst] = s_vals[i];
