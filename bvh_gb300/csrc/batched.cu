@@ -175,8 +175,9 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   k_delta<unsigned long long, true><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], d_offsets, ws.delta, n);
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer
-  k_emit<SegBatch, false, 512><<<div_up(n, 512), 512, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n,
-                                                          SegBatch{keys, d_offsets}, d_indices, frontier, fcount);
+  k_emit<SegBatch, false, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
+      ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, SegBatch{keys, d_offsets}, d_indices, frontier, fcount,
+      kEmitMaxSteps);
   k_emit_climb<SegBatch, false><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
       ws.delta, ws.nodes, ws.slots, ws.scratch + L.epoch, n, SegBatch{keys, d_offsets}, frontier, fcount);
   if (evs && evs->use) {

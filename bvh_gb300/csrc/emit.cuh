@@ -7,8 +7,9 @@
 // (delta_nt, lbvh_builder.cu:33-43: common-prefix length of the codes, or 32/64 +
 // clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0 marks a segment boundary).
 // Step 2 (k_emit): one thread per sorted position climbs; merges whose two children belong to
-// threads of one block happen in shared memory.  Nodes whose sibling is built by another block
-// are listed as a frontier, from which k_emit_climb continues through global rendezvous words.  A node with range [f, l] has its
+// threads of one block happen in shared memory.  Nodes whose sibling is built by another block,
+// and nodes still climbing after kEmitMaxSteps levels, are listed as a frontier, from which
+// k_emit_climb continues through global rendezvous words.  A node with range [f, l] has its
 // parent's split on the side whose adjacent delta is larger (Apetrei 2014): gamma = l when
 // D[l] > D[f-1], else gamma = f-1.  The second child to reach gamma's rendezvous word completes
 // the parent.  Karras ids: leaf i -> n-1+i, a left child's id is its last index, a right
@@ -43,6 +44,11 @@ struct SegBatch {
   }
 };
 
+// In-tile climbs stop after this many levels and continue in k_emit_climb (k_emit's max_steps):
+// the longest chain of a block no longer holds its 512 threads.
+constexpr uint32_t kEmitMaxSteps = 8;
+constexpr uint32_t kEmitTile = 512;  // sorted positions (threads) per k_emit block
+
 __device__ __forceinline__ void store_node(Node* nodes, uint32_t idx, const Box& b, int32_t l, int32_t r, int32_t aux0) {
   float4* p = reinterpret_cast<float4*>(nodes + idx);
   __stcg(p, b.lo);
@@ -55,6 +61,15 @@ __device__ __forceinline__ Box load_node_box(const Node* nodes, uint32_t idx) {
   b.lo = __ldcg(p);
   b.hi = __ldcg(p + 1);
   return b;
+}
+
+__device__ __forceinline__ uint32_t atom_or_acq_rel_cta(uint32_t* p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.cta.shared::cta.or.b32 %0, [%1], %2;"
+               : "=r"(old)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(v)
+               : "memory");
+  return old;
 }
 
 __device__ __forceinline__ unsigned long long atom_exch_acq_rel(unsigned long long* p, unsigned long long v) {
@@ -112,17 +127,18 @@ struct Climb {
 // T sorted positions per block, one thread each (a larger block leaves fewer nodes whose sibling
 // lies in another block to the frontier pass).
 template <typename Seg, bool PARENTS, uint32_t T = 256>
-__global__ void __launch_bounds__(T) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
+__global__ void __launch_bounds__(T, 2048 / T) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
                                             const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
                                             uint32_t n, Seg seg, uint32_t* __restrict__ out_idx,
-                                            uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count) {
+                                            uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count,
+                                            uint32_t max_steps) {
   // D of positions bbase-1 .. bbase+T-1 (0 outside [0, n-1) : a segment boundary)
   __shared__ uint8_t s_D[T + 1];
-  // rendezvous slot k <-> split gamma = bbase + k: one side per child (0 left, 1 right)
+  // rendezvous slot k <-> split gamma = bbase + k: one side per child (0 left, 1 right); the
+  // child's box with its id in lo.w and its far end (f of a left child, l of a right child) in hi.w
   __shared__ uint32_t s_flag[T];
-  __shared__ float s_bx[2][6][T];
-  __shared__ int32_t s_id[2][T];
-  __shared__ uint32_t s_end[2][T];  // the child's far end: f of a left child, l of a right child
+  __shared__ float4 s_lo[2][T];
+  __shared__ float4 s_hi[2][T];
   const uint32_t tid = threadIdx.x;
   const uint32_t i = blockIdx.x * T + tid;
   const uint32_t bbase = blockIdx.x * T;  // sorted position of thread 0
@@ -159,7 +175,7 @@ __global__ void __launch_bounds__(T) k_emit(const uint8_t* __restrict__ D, const
   // A node [f, l] with both ends in this block reads D[f-1] and D[l] from s_D; its parent's
   // split is gamma = l (it is the left child) when D[l] > D[f-1], else gamma = f-1.
   bool to_frontier = false;
-  while (active) {
+  for (uint32_t step = 0; active; ++step) {
     const int dl = (int)s_D[c.f - bbase] - 1;
     const int dr = (int)s_D[c.l - bbase + 1] - 1;
     if (dl < 0 && dr < 0) {  // segment root
@@ -168,37 +184,39 @@ __global__ void __launch_bounds__(T) k_emit(const uint8_t* __restrict__ D, const
     }
     const bool is_left = dr > dl;
     const uint32_t gamma = is_left ? c.l : c.f - 1;
-    if (c.internal) {  // its id is known now: a left child is named by its last index
-      c.my = (int32_t)((is_left ? c.l : c.f) - off);
-      write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
-      c.internal = false;
-    }
-    if (is_left ? gamma + 1 >= bbase + T : gamma < bbase) {  // sibling starts outside the block
+    const bool pending = c.internal;  // complete; its id is known now: a left child is named by its last index
+    if (pending) c.my = (int32_t)((is_left ? c.l : c.f) - off);
+    // sibling starts outside the block, or the climb has gone max_steps levels: the node
+    // continues in k_emit_climb, so that one long chain does not hold the block
+    if (step >= max_steps || (is_left ? gamma + 1 >= bbase + T : gamma < bbase)) {
+      if (pending) write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
       to_frontier = true;
       break;
     }
+    // with parent links the node is written before the rendezvous, so that the parent's later
+    // write of its aux0 lands last
+    if (PARENTS && pending) write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
     const uint32_t k = gamma - bbase;
     const int side = is_left ? 0 : 1;
-    s_bx[side][0][k] = c.box.lo.x; s_bx[side][1][k] = c.box.lo.y; s_bx[side][2][k] = c.box.lo.z;
-    s_bx[side][3][k] = c.box.hi.x; s_bx[side][4][k] = c.box.hi.y; s_bx[side][5][k] = c.box.hi.z;
-    s_id[side][k] = c.my;
-    s_end[side][k] = is_left ? c.f : c.l;
-    __threadfence_block();
-    if (atomicOr(&s_flag[k], 1u << side) == 0u) break;  // first to arrive
-    __threadfence_block();
-    const int o = side ^ 1;
+    s_lo[side][k] = make_float4(c.box.lo.x, c.box.lo.y, c.box.lo.z, __int_as_float(c.my));
+    s_hi[side][k] = make_float4(c.box.hi.x, c.box.hi.y, c.box.hi.z, __uint_as_float(is_left ? c.f : c.l));
+    // release: the slot is visible before the flag bit; acquire: the sibling's slot is read after
+    const uint32_t prev = atom_or_acq_rel_cta(&s_flag[k], 1u << side);
+    if (!PARENTS && pending) write_internal<PARENTS>(nodes, nb, c.my, c.box, c.lc, c.rc);
+    if (prev == 0u) break;  // first to arrive
+    const float4 a = s_lo[side ^ 1][k], b = s_hi[side ^ 1][k];
     Box sb;
-    sb.lo = make_float4(s_bx[o][0][k], s_bx[o][1][k], s_bx[o][2][k], 0.f);
-    sb.hi = make_float4(s_bx[o][3][k], s_bx[o][4][k], s_bx[o][5][k], 0.f);
+    sb.lo = make_float4(a.x, a.y, a.z, 0.f);
+    sb.hi = make_float4(b.x, b.y, b.z, 0.f);
     if (is_left) {
       c.lc = c.my;
-      c.rc = s_id[o][k];
-      c.l = s_end[o][k];
+      c.rc = __float_as_int(a.w);
+      c.l = __float_as_uint(b.w);
       c.box = box_union(c.box, sb);
     } else {
-      c.lc = s_id[o][k];
+      c.lc = __float_as_int(a.w);
       c.rc = c.my;
-      c.f = s_end[o][k];
+      c.f = __float_as_uint(b.w);
       c.box = box_union(sb, c.box);
     }
     c.internal = true;
@@ -211,7 +229,8 @@ __global__ void __launch_bounds__(T) k_emit(const uint8_t* __restrict__ D, const
   if (tid < T - 1) {
     const uint32_t fl = s_flag[tid];
     const uint32_t g = bbase + tid;
-    uint2 e = fl == 1u ? make_uint2(s_end[0][tid], g) : make_uint2(g + 1, s_end[1][tid]);
+    uint2 e = fl == 1u ? make_uint2(__float_as_uint(s_hi[0][tid].w), g)
+                       : make_uint2(g + 1, __float_as_uint(s_hi[1][tid].w));
     if (fl == 1u || fl == 2u) {
       if (nf) fr1 = e;
       else fr0 = e;

@@ -656,8 +656,8 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer, 8 B per position
   k_delta<K, false><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], nullptr, ws.delta, n);
-  k_emit<SegSingle, PARENTS, 512><<<div_up(n, 512), 512, 0, st>>>(ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n,
-                                                             SegSingle{n}, nullptr, frontier, fcount);
+  k_emit<SegSingle, PARENTS, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
+      ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, SegSingle{n}, nullptr, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegSingle, PARENTS><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
       ws.delta, ws.nodes, ws.slots, epoch, n, SegSingle{n}, frontier, fcount);
 }
