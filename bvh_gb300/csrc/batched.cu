@@ -167,7 +167,8 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   if ((e = run_sort_u64(ws, n, passes, st, L, &fb, shift0)) != cudaSuccess) return e;
   if (shift0 > 0 &&
       (e = sort_fix_runs(reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb],
-                         reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, shift0, st)) !=
+                         reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, shift0,
+                         reinterpret_cast<uint32_t*>(ws.delta), ws.scratch + L.counters + kLongRunCounter, st)) !=
           cudaSuccess)
     return e;
   if (evs && evs->use) cudaEventRecord(evs->ev[3], st);

@@ -8,22 +8,20 @@
 // ordering each run by (L = code & (2^lbits - 1), position) completes the sort.  On real meshes
 // almost every run has length 1, so this costs one read of the keys instead of four more passes.
 //
-// k_fixrun: one block per tile of 1024 positions.  The block owns the runs that START in its
-// tile.  Runs of up to kHalo items are ranked from shared memory (each item's rank is the count
-// of smaller (L, position) pairs in its run) and permuted in place; longer runs are sorted by the
-// owning block with a block-wide stable LSD over L, through the same positions of the other
-// key/value buffer.  Blocks read positions owned by neighbours only for H, which a permutation
-// within a run does not change, so the in-place writes cannot disturb them.
+// k_fixrun_short: one thread per 4 consecutive positions.  A thread owns the runs that START
+// in its 4 positions (a run's first position differs from its predecessor); neighbours come from
+// the adjacent lanes.  A run of at most kMaxShort items is ranked in registers (rank = count of
+// smaller (L, position) pairs) and written back in place; a longer one is appended to a list,
+// which k_fixrun_long sorts, one run per block, with a block-wide stable LSD over L through the
+// same positions of the other key/value buffer.  Other threads read positions of a run only
+// for H, which a permutation within the run does not change.
 #include "lbvh.cuh"
 
 namespace bvhgb {
 namespace {
 
 constexpr int kFixThreads = 256;
-constexpr int kFixTile = 1024;
-constexpr int kHalo = 64;  // runs up to this length are ranked in shared memory
-constexpr uint32_t kNone = 0xffffffffu;
-constexpr int kSpan = kFixTile + kHalo + 1;  // positions a-1 .. a+T+kHalo-1
+constexpr int kMaxShort = 8;  // runs up to this length are ranked in registers
 
 // Exclusive prefix over the 256 threads' values (thread t = bin t); s_w holds 8 warp totals.
 __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_w) {
@@ -113,104 +111,91 @@ __device__ void block_sort_run(unsigned long long* keys, uint32_t* vals, unsigne
   }
 }
 
-__global__ void __launch_bounds__(kFixThreads, 5) k_fixrun(unsigned long long* __restrict__ keys,
-                                                        uint32_t* __restrict__ vals,
-                                                        unsigned long long* __restrict__ tkeys,
-                                                        uint32_t* __restrict__ tvals, uint32_t n, int lbits) {
-  constexpr int kPer = (kSpan + kFixThreads - 1) / kFixThreads;  // positions per thread
-  __shared__ uint32_t s_h[kSpan];    // H of position q at q - a + 1
-  __shared__ uint32_t s_l[kSpan];    // L
-  __shared__ uint32_t s_wh[8 * 256];
-  __shared__ uint32_t s_off[256];
-  __shared__ uint32_t s_w[8];
-  __shared__ uint32_t s_long[kFixTile / kHalo];
-  __shared__ uint32_t s_nlong, s_e;
-
-  const int t = threadIdx.x;
-  const uint32_t a = blockIdx.x * kFixTile;
-  const uint32_t lo = a == 0 ? 0 : a - 1;
-  const uint32_t hi = min(n, a + (uint32_t)kFixTile + (uint32_t)kHalo);
-  const uint32_t tile_end = min(n, a + (uint32_t)kFixTile);
-  const unsigned long long lmask = (1ull << lbits) - 1ull;
-  if (t == 0) s_nlong = 0;
-  {
-    // all of this thread's loads first, then the stores
-    unsigned long long k[kPer];
+__global__ void __launch_bounds__(256) k_fixrun_short(unsigned long long* __restrict__ keys,
+                                                      uint32_t* __restrict__ vals, uint32_t n, int lbits,
+                                                      uint32_t* __restrict__ long_list,
+                                                      uint32_t* __restrict__ long_count) {
+  constexpr unsigned long long kNoH = ~0ull;  // "no position": H is below 2^32
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+  // H of this thread's 4 positions (kNoH past n)
+  unsigned long long h[4];
+  if (p0 + 4 <= n) {
+    const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(keys + p0);
+    const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(keys + p0 + 2);
+    h[0] = a.x >> lbits;
+    h[1] = a.y >> lbits;
+    h[2] = b.x >> lbits;
+    h[3] = b.y >> lbits;
+  } else {
 #pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-      const uint32_t q = lo + t + (uint32_t)r * kFixThreads;
-      k[r] = q < hi ? keys[q] : 0ull;
+    for (int j = 0; j < 4; ++j) h[j] = p0 + j < n ? keys[p0 + j] >> lbits : kNoH;
+  }
+  unsigned long long hprev = __shfl_up_sync(0xffffffffu, h[3], 1);
+  unsigned long long hnext = __shfl_down_sync(0xffffffffu, h[0], 1);
+  if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? keys[p0 - 1] >> lbits : kNoH;
+  if (lane == 31) hnext = p0 + 4 < n ? keys[p0 + 4] >> lbits : kNoH;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const unsigned long long hp = j == 0 ? hprev : h[j - 1];
+    const unsigned long long hn = j == 3 ? hnext : h[j + 1];
+    if (h[j] == kNoH || h[j] == hp || h[j] != hn) continue;  // not the start of a run of 2 or more
+    const uint32_t s = p0 + j;
+    uint32_t m = 2;  // run length, counted up to kMaxShort + 1
+    while (m <= (uint32_t)kMaxShort && s + m < n && (keys[s + m] >> lbits) == h[j]) ++m;
+    if (m > (uint32_t)kMaxShort) {
+      long_list[atomicAdd(long_count, 1u)] = s;
+      continue;
+    }
+    const unsigned long long lmask = (1ull << lbits) - 1ull;
+    unsigned long long k[kMaxShort];
+    uint32_t v[kMaxShort];
+#pragma unroll
+    for (int i = 0; i < kMaxShort; ++i) {
+      k[i] = i < (int)m ? keys[s + i] : ~0ull;
+      v[i] = i < (int)m ? vals[s + i] : 0u;
     }
 #pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-      const uint32_t q = lo + t + (uint32_t)r * kFixThreads;
-      if (q < hi) {
-        s_h[q - a + 1] = (uint32_t)(k[r] >> lbits);
-        s_l[q - a + 1] = (uint32_t)(k[r] & lmask);
+    for (int i = 0; i < kMaxShort; ++i) {
+      if (i >= (int)m) break;
+      const unsigned long long li = k[i] & lmask;
+      uint32_t r = 0;
+#pragma unroll
+      for (int q = 0; q < kMaxShort; ++q) {
+        if (q < (int)m) {
+          const unsigned long long lq = k[q] & lmask;
+          r += (lq < li) || (lq == li && q < i);
+        }
+      }
+      if (r != (uint32_t)i) {
+        keys[s + r] = k[i];
+        vals[s + r] = v[i];
       }
     }
   }
-  __syncthreads();
-#define H(q) s_h[(q) - a + 1]
-#define L(q) s_l[(q) - a + 1]
-  // this thread's positions a + t + 256 r: new position of a moved item (or kNone) and its value
-  uint32_t dst[kPer], mv[kPer];
-#pragma unroll
-  for (int r = 0; r < kPer; ++r) {
-    dst[r] = kNone;
-    mv[r] = 0;
-    const uint32_t q = a + t + (uint32_t)r * kFixThreads;
-    if (q >= hi) continue;
-    const uint32_t h = H(q);
-    const bool prev_same = q > 0 && H(q - 1) == h;
-    const bool next_same = q + 1 < hi && H(q + 1) == h;
-    // a run of more than kHalo items that starts in this tile goes to the block-wide path
-    if (!prev_same && q < tile_end && q + kHalo < n && H(q + kHalo) == h) {
-      const uint32_t slot = atomicAdd(&s_nlong, 1u);
-      s_long[slot] = q;
-      continue;
-    }
-    if (!prev_same && !next_same) continue;  // a run of one
-    // start of q's run, within kHalo steps
-    uint32_t s = q;
-    while (s > lo && q - s < (uint32_t)kHalo && H(s - 1) == h) --s;
-    if (q - s == (uint32_t)kHalo) continue;  // more than kHalo equal items: a long run
-    if (s < a || s >= tile_end) continue;    // started in another tile: not ours
-    if (s + kHalo < n && H(s + kHalo) == h) continue;  // long run (sorted by the block-wide path)
-    uint32_t e = q + 1;
-    while (e < hi && H(e) == h) ++e;
-    // rank by (L, position) within [s, e)
-    const uint32_t l = L(q);
-    uint32_t rank = 0;
-    for (uint32_t j = s; j < e; ++j) {
-      const uint32_t lj = L(j);
-      rank += (lj < l) || (lj == l && j < q);
-    }
-    if (s + rank != q) {
-      dst[r] = s + rank;
-      mv[r] = vals[q];
-    }
-  }
-  __syncthreads();  // every item of the block's runs has been read
-#pragma unroll
-  for (int r = 0; r < kPer; ++r) {
-    if (dst[r] != kNone) {
-      const uint32_t q = a + t + (uint32_t)r * kFixThreads;
-      keys[dst[r]] = ((unsigned long long)H(q) << lbits) | L(q);
-      vals[dst[r]] = mv[r];
-    }
-  }
-  __syncthreads();
-  // long runs starting in this tile, one at a time by the whole block
-  const uint32_t nlong = s_nlong;
-  for (uint32_t li = 0; li < nlong; ++li) {
-    const uint32_t s = s_long[li];
-    const uint32_t h = H(s);
+}
+
+// One block per listed run (longer than kMaxShort): find its end, then sort it by its low bits.
+__global__ void __launch_bounds__(kFixThreads) k_fixrun_long(unsigned long long* __restrict__ keys,
+                                                         uint32_t* __restrict__ vals,
+                                                         unsigned long long* __restrict__ tkeys,
+                                                         uint32_t* __restrict__ tvals, uint32_t n, int lbits,
+                                                         const uint32_t* __restrict__ long_list,
+                                                         const uint32_t* __restrict__ long_count) {
+  __shared__ uint32_t s_wh[8 * 256];
+  __shared__ uint32_t s_off[256];
+  __shared__ uint32_t s_w[8];
+  __shared__ uint32_t s_e;
+  const uint32_t count = __ldcg(long_count);
+  const int t = threadIdx.x;
+  for (uint32_t li = blockIdx.x; li < count; li += gridDim.x) {
+    const uint32_t s = __ldcg(long_list + li);
+    const unsigned long long h = keys[s] >> lbits;
     if (t == 0) s_e = n;
     __syncthreads();
-    for (uint32_t base = s + kHalo + 1; base < n; base += kFixThreads) {
+    for (uint32_t base = s + kMaxShort + 1; base < n; base += kFixThreads) {
       const uint32_t q = base + t;
-      if (q < n && (uint32_t)(keys[q] >> lbits) != h) atomicMin(&s_e, q);
+      if (q < n && (keys[q] >> lbits) != h) atomicMin(&s_e, q);
       __syncthreads();
       const bool found = s_e != n;
       __syncthreads();
@@ -219,16 +204,15 @@ __global__ void __launch_bounds__(kFixThreads, 5) k_fixrun(unsigned long long* _
     block_sort_run(keys, vals, tkeys, tvals, s, s_e - s, lbits, s_wh, s_off, s_w);
     __syncthreads();
   }
-#undef H
-#undef L
 }
 
 }  // namespace
 
 cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
-                          uint32_t n, int lbits, cudaStream_t st) {
+                          uint32_t n, int lbits, uint32_t* long_list, uint32_t* long_count, cudaStream_t st) {
   if (n < 2) return cudaSuccess;
-  k_fixrun<<<div_up(n, (uint32_t)kFixTile), kFixThreads, 0, st>>>(keys, vals, tkeys, tvals, n, lbits);
+  k_fixrun_short<<<div_up(div_up(n, 4u), 256u), 256, 0, st>>>(keys, vals, n, lbits, long_list, long_count);
+  k_fixrun_long<<<152, kFixThreads, 0, st>>>(keys, vals, tkeys, tvals, n, lbits, long_list, long_count);
   return cudaGetLastError();
 }
 

@@ -633,8 +633,10 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   cudaError_t e = run_sort<K>(ws, n, 4, st, L, final_buf, S0);
   if (e == cudaSuccess && sizeof(K) == 8) {
     const int fb = *final_buf;
+    // the long-run list lives in the delta bytes, which emission has not written yet
     e = sort_fix_runs(reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb],
-                      reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, S0, st);
+                      reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, S0,
+                      reinterpret_cast<uint32_t*>(ws.delta), ws.scratch + L.counters + kLongRunCounter, st);
   }
   rec(evs, 3, st);
   return e;

@@ -77,6 +77,7 @@ constexpr int kBoundsBlocks = 152 * 4;
 constexpr int kSortThreads = 256;
 constexpr int kMaxPasses = 8;
 constexpr int kFrontierCounter = 15;  // counters[15]: emission frontier length (passes use 0..7)
+constexpr int kLongRunCounter = 14;   // counters[14]: runs listed for the block-wide fix-up
 
 ScratchLayout scratch_layout(uint32_t n);
 int sort_tile(int key_bytes);  // smallest tile over all variants (sizes the look-back scratch)
@@ -129,9 +130,10 @@ cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cu
 
 // Completes a sort of 64-bit keys whose radix passes covered only bits lbits..lbits+31: orders
 // every run of equal key >> lbits by (key low bits, position), in place; tkeys/tvals (the other
-// ping-pong buffers) are scratch for runs longer than 64.
+// ping-pong buffers) are scratch for runs longer than 8, whose starts are listed in long_list
+// (room for n / 4 words) behind the zeroed counter long_count.
 cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
-                          uint32_t n, int lbits, cudaStream_t st);
+                          uint32_t n, int lbits, uint32_t* long_list, uint32_t* long_count, cudaStream_t st);
 
 // Treelet restructuring passes (LBVH+) after emission; fb = the sort's final ping-pong buffer
 // (the other one is scratch).
