@@ -8,10 +8,11 @@
 // ordering each run by (L = code & (2^lbits - 1), position) completes the sort.  On real meshes
 // almost every run has length 1, so this costs one read of the keys instead of four more passes.
 //
-// k_fixrun_short: one thread per 4 consecutive positions.  A thread owns the runs that START
-// in its 4 positions (a run's first position differs from its predecessor); neighbours come from
-// the adjacent lanes.  A run of at most kMaxShort items is ranked in registers (rank = count of
-// smaller (L, position) pairs) and written back in place; a longer one is appended to a list,
+// k_fixrun_short: one thread per 4 consecutive positions, with the next thread's 4 keys (from
+// the adjacent lane) as an 8-key window.  A thread owns the runs that START in its 4 positions
+// (a run's first position differs from its predecessor).  A run that ends inside the window is
+// ranked in registers (rank = count of smaller (L, position) pairs) and written back in place;
+// a longer one is appended to a list,
 // which k_fixrun_long sorts, one run per block, with a block-wide stable LSD over L through the
 // same positions of the other key/value buffer.  Other threads read positions of a run only
 // for H, which a permutation within the run does not change.
@@ -21,7 +22,7 @@ namespace bvhgb {
 namespace {
 
 constexpr int kFixThreads = 256;
-constexpr int kMaxShort = 8;  // runs up to this length are ranked in registers
+constexpr int kRankMax = 1024;  // listed runs up to this length are ranked by counting
 
 // Exclusive prefix over the 256 threads' values (thread t = bin t); s_w holds 8 warp totals.
 __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_w) {
@@ -111,71 +112,109 @@ __device__ void block_sort_run(unsigned long long* keys, uint32_t* vals, unsigne
   }
 }
 
-__global__ void __launch_bounds__(256) k_fixrun_short(unsigned long long* __restrict__ keys,
+// Stable rank of window item i among the window items [j, j + m) by (L, window position).
+__device__ __forceinline__ uint32_t window_rank(const unsigned long long (&w)[8], int j, int m, int i,
+                                                unsigned long long lmask) {
+  const unsigned long long li = w[i] & lmask;
+  uint32_t r = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (q >= j && q < j + m) {
+      const unsigned long long lq = w[q] & lmask;
+      r += (lq < li) || (lq == li && q < i);
+    }
+  }
+  return r;
+}
+
+__global__ void __launch_bounds__(256, 4) k_fixrun_short(unsigned long long* __restrict__ keys,
                                                       uint32_t* __restrict__ vals, uint32_t n, int lbits,
                                                       uint32_t* __restrict__ long_list,
                                                       uint32_t* __restrict__ long_count) {
   constexpr unsigned long long kNoH = ~0ull;  // "no position": H is below 2^32
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
-  // H of this thread's 4 positions (kNoH past n)
-  unsigned long long h[4];
+  // window: this thread's 4 keys, then the next thread's 4 (kNoH-keyed past n)
+  // (values alongside, so that a reorder needs no second round trip)
+  unsigned long long w[8];
+  uint32_t v[8];
   if (p0 + 4 <= n) {
     const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(keys + p0);
     const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(keys + p0 + 2);
-    h[0] = a.x >> lbits;
-    h[1] = a.y >> lbits;
-    h[2] = b.x >> lbits;
-    h[3] = b.y >> lbits;
+    const uint4 c = *reinterpret_cast<const uint4*>(vals + p0);
+    w[0] = a.x;
+    w[1] = a.y;
+    w[2] = b.x;
+    w[3] = b.y;
+    v[0] = c.x;
+    v[1] = c.y;
+    v[2] = c.z;
+    v[3] = c.w;
   } else {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) h[j] = p0 + j < n ? keys[p0 + j] >> lbits : kNoH;
+    for (int j = 0; j < 4; ++j) {
+      w[j] = p0 + j < n ? keys[p0 + j] : kNoH;
+      v[j] = p0 + j < n ? vals[p0 + j] : 0u;
+    }
   }
-  unsigned long long hprev = __shfl_up_sync(0xffffffffu, h[3], 1);
-  unsigned long long hnext = __shfl_down_sync(0xffffffffu, h[0], 1);
-  if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? keys[p0 - 1] >> lbits : kNoH;
-  if (lane == 31) hnext = p0 + 4 < n ? keys[p0 + 4] >> lbits : kNoH;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const unsigned long long hp = j == 0 ? hprev : h[j - 1];
-    const unsigned long long hn = j == 3 ? hnext : h[j + 1];
-    if (h[j] == kNoH || h[j] == hp || h[j] != hn) continue;  // not the start of a run of 2 or more
+    w[4 + j] = __shfl_down_sync(0xffffffffu, w[j], 1);
+    v[4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
+  }
+  if (lane == 31) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      w[4 + j] = p0 + 4 + j < n ? keys[p0 + 4 + j] : kNoH;
+      v[4 + j] = p0 + 4 + j < n ? vals[p0 + 4 + j] : 0u;
+    }
+  }
+  unsigned long long hw[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) hw[q] = w[q] == kNoH ? kNoH : w[q] >> lbits;
+  unsigned long long hprev = __shfl_up_sync(0xffffffffu, hw[3], 1);
+  if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? keys[p0 - 1] >> lbits : kNoH;
+  const unsigned long long lmask = (1ull << lbits) - 1ull;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const unsigned long long hp = j == 0 ? hprev : hw[j - 1];
+    if (hw[j] == kNoH || hw[j] == hp || hw[j] != hw[j + 1]) continue;  // not the start of a run of 2+
     const uint32_t s = p0 + j;
-    uint32_t m = 2;  // run length, counted up to kMaxShort + 1
-    while (m <= (uint32_t)kMaxShort && s + m < n && (keys[s + m] >> lbits) == h[j]) ++m;
-    if (m > (uint32_t)kMaxShort) {
+    // run length inside the window
+    int m = 2;
+#pragma unroll
+    for (int q = j + 2; q < 8; ++q) m += (m == q - j && hw[q] == hw[j]) ? 1 : 0;
+    // a run that reaches the end of the window and goes on (at least 6 items) takes the
+    // block-wide path
+    if (j + m == 8 && p0 + 8 < n && (keys[p0 + 8] >> lbits) == hw[j]) {
       long_list[atomicAdd(long_count, 1u)] = s;
       continue;
     }
-    const unsigned long long lmask = (1ull << lbits) - 1ull;
-    unsigned long long k[kMaxShort];
-    uint32_t v[kMaxShort];
-#pragma unroll
-    for (int i = 0; i < kMaxShort; ++i) {
-      k[i] = i < (int)m ? keys[s + i] : ~0ull;
-      v[i] = i < (int)m ? vals[s + i] : 0u;
-    }
-#pragma unroll
-    for (int i = 0; i < kMaxShort; ++i) {
-      if (i >= (int)m) break;
-      const unsigned long long li = k[i] & lmask;
-      uint32_t r = 0;
-#pragma unroll
-      for (int q = 0; q < kMaxShort; ++q) {
-        if (q < (int)m) {
-          const unsigned long long lq = k[q] & lmask;
-          r += (lq < li) || (lq == li && q < i);
-        }
+    if (m == 2) {  // the common case: swap when out of order
+      if ((w[j] & lmask) > (w[j + 1] & lmask)) {
+        keys[s] = w[j + 1];
+        keys[s + 1] = w[j];
+        vals[s] = v[j + 1];
+        vals[s + 1] = v[j];
       }
-      if (r != (uint32_t)i) {
-        keys[s + r] = k[i];
-        vals[s + r] = v[i];
+      continue;
+    }
+    uint32_t rk[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      rk[i] = (i >= j && i < j + m) ? window_rank(w, j, m, i, lmask) + (uint32_t)j : (uint32_t)i;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (i >= j && i < j + m && rk[i] != (uint32_t)i) {
+        keys[p0 + rk[i]] = w[i];
+        vals[p0 + rk[i]] = v[i];
       }
     }
   }
 }
 
-// One block per listed run (longer than kMaxShort): find its end, then sort it by its low bits.
+// One block per listed run (one that outgrew its thread's window): find its end, then sort it
+// by its low bits.
 __global__ void __launch_bounds__(kFixThreads) k_fixrun_long(unsigned long long* __restrict__ keys,
                                                          uint32_t* __restrict__ vals,
                                                          unsigned long long* __restrict__ tkeys,
@@ -193,7 +232,7 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun_long(unsigned long long*
     const unsigned long long h = keys[s] >> lbits;
     if (t == 0) s_e = n;
     __syncthreads();
-    for (uint32_t base = s + kMaxShort + 1; base < n; base += kFixThreads) {
+    for (uint32_t base = s + 1; base < n; base += kFixThreads) {
       const uint32_t q = base + t;
       if (q < n && (keys[q] >> lbits) != h) atomicMin(&s_e, q);
       __syncthreads();
@@ -201,7 +240,42 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun_long(unsigned long long*
       __syncthreads();
       if (found) break;
     }
-    block_sort_run(keys, vals, tkeys, tvals, s, s_e - s, lbits, s_wh, s_off, s_w);
+    const uint32_t m = s_e - s;
+    if (m <= kRankMax) {
+      // rank by counting: each thread takes items t, t + 256, ...; the low bits of the run's
+      // keys sit in s_wh (kRankMax words)
+      const unsigned long long lmask = (1ull << lbits) - 1ull;
+      for (uint32_t q = t; q < m; q += kFixThreads) s_wh[q] = (uint32_t)(keys[s + q] & lmask);
+      __syncthreads();
+      unsigned long long kq[kRankMax / kFixThreads];
+      uint32_t vq[kRankMax / kFixThreads], rq[kRankMax / kFixThreads];
+#pragma unroll
+      for (int r = 0; r < kRankMax / kFixThreads; ++r) {
+        const uint32_t q = t + (uint32_t)r * kFixThreads;
+        if (q < m) {
+          const uint32_t lq = s_wh[q];
+          uint32_t rank = 0;
+          for (uint32_t x = 0; x < m; ++x) {
+            const uint32_t lx = s_wh[x];
+            rank += (lx < lq) || (lx == lq && x < q);
+          }
+          kq[r] = keys[s + q];
+          vq[r] = vals[s + q];
+          rq[r] = rank;
+        }
+      }
+      __syncthreads();  // every item of the run is read before any is written
+#pragma unroll
+      for (int r = 0; r < kRankMax / kFixThreads; ++r) {
+        const uint32_t q = t + (uint32_t)r * kFixThreads;
+        if (q < m && rq[r] != q) {
+          keys[s + rq[r]] = kq[r];
+          vals[s + rq[r]] = vq[r];
+        }
+      }
+    } else {
+      block_sort_run(keys, vals, tkeys, tvals, s, m, lbits, s_wh, s_off, s_w);
+    }
     __syncthreads();
   }
 }

@@ -130,8 +130,8 @@ cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cu
 
 // Completes a sort of 64-bit keys whose radix passes covered only bits lbits..lbits+31: orders
 // every run of equal key >> lbits by (key low bits, position), in place; tkeys/tvals (the other
-// ping-pong buffers) are scratch for runs longer than 8, whose starts are listed in long_list
-// (room for n / 4 words) behind the zeroed counter long_count.
+// ping-pong buffers) are scratch for runs longer than a few items, whose starts are listed in
+// long_list (room for n / 6 words) behind the zeroed counter long_count.
 cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
                           uint32_t n, int lbits, uint32_t* long_list, uint32_t* long_count, cudaStream_t st);
 
