@@ -106,6 +106,26 @@ __global__ void __launch_bounds__(256) k_delta(const K* __restrict__ keys, const
   D[k] = (uint8_t)(d + 1);
 }
 
+// delta(k, k+1) + 1 of 60/63-bit codes held split: hk = code >> lbits (sorted), lows = the low
+// lbits bits by original index.  The same values as k_delta on the whole codes (clz of the
+// 64-bit XOR, or 64 + clz of the 64-bit XOR of the indices for equal codes).
+static __global__ void __launch_bounds__(256)
+    k_delta_split(const uint32_t* __restrict__ hk, const uint32_t* __restrict__ vals,
+                  const uint32_t* __restrict__ lows, int lbits, uint8_t* __restrict__ D, uint32_t n) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k + 1 >= n) return;
+  const uint32_t a = __ldg(hk + k), b = __ldg(hk + k + 1);
+  int d;
+  if (a != b) {
+    d = __clz(a ^ b) + 32 - lbits;
+  } else {
+    const uint32_t va = __ldg(vals + k), vb = __ldg(vals + k + 1);
+    const uint32_t la = __ldg(lows + va), lb = __ldg(lows + vb);
+    d = la != lb ? 32 + __clz(la ^ lb) : 96 + __clz(va ^ vb);
+  }
+  D[k] = (uint8_t)(d + 1);
+}
+
 template <bool PARENTS>
 __device__ __forceinline__ void write_internal(Node* nodes, uint32_t nb, int32_t my, const Box& box, int32_t lc,
                                                int32_t rc) {

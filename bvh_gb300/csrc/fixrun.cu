@@ -280,6 +280,144 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun_long(unsigned long long*
   }
 }
 
+// Split codes: H = hkeys[position] (sorted), L = lows[original index].  Same ownership rules as
+// k_fixrun_short; only the values of a run move.
+__global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __restrict__ hkeys,
+                                                            uint32_t* __restrict__ vals,
+                                                            const uint32_t* __restrict__ lows, uint32_t n,
+                                                            uint32_t* __restrict__ long_list,
+                                                            uint32_t* __restrict__ long_count) {
+  constexpr unsigned long long kNoH = ~0ull;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+  unsigned long long hw[8];
+  uint32_t v[8];
+  if (p0 + 4 <= n) {
+    const uint4 a = *reinterpret_cast<const uint4*>(hkeys + p0);
+    const uint4 c = *reinterpret_cast<const uint4*>(vals + p0);
+    hw[0] = a.x;
+    hw[1] = a.y;
+    hw[2] = a.z;
+    hw[3] = a.w;
+    v[0] = c.x;
+    v[1] = c.y;
+    v[2] = c.z;
+    v[3] = c.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      hw[j] = p0 + j < n ? (unsigned long long)hkeys[p0 + j] : kNoH;
+      v[j] = p0 + j < n ? vals[p0 + j] : 0u;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    hw[4 + j] = __shfl_down_sync(0xffffffffu, hw[j], 1);
+    v[4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
+  }
+  if (lane == 31) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      hw[4 + j] = p0 + 4 + j < n ? (unsigned long long)hkeys[p0 + 4 + j] : kNoH;
+      v[4 + j] = p0 + 4 + j < n ? vals[p0 + 4 + j] : 0u;
+    }
+  }
+  unsigned long long hprev = __shfl_up_sync(0xffffffffu, hw[3], 1);
+  if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? (unsigned long long)hkeys[p0 - 1] : kNoH;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const unsigned long long hp = j == 0 ? hprev : hw[j - 1];
+    if (hw[j] == kNoH || hw[j] == hp || hw[j] != hw[j + 1]) continue;  // not the start of a run of 2+
+    const uint32_t s = p0 + j;
+    int m = 2;
+#pragma unroll
+    for (int q = j + 2; q < 8; ++q) m += (m == q - j && hw[q] == hw[j]) ? 1 : 0;
+    if (j + m == 8 && p0 + 8 < n && (unsigned long long)hkeys[p0 + 8] == hw[j]) {
+      long_list[atomicAdd(long_count, 1u)] = s;
+      continue;
+    }
+    if (m == 2) {  // the common case: swap when out of order
+      if (__ldg(lows + v[j]) > __ldg(lows + v[j + 1])) {
+        vals[s] = v[j + 1];
+        vals[s + 1] = v[j];
+      }
+      continue;
+    }
+    unsigned long long w[8];  // L in the window slots of the run (positions order the ties)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) w[i] = (i >= j && i < j + m) ? (unsigned long long)__ldg(lows + v[i]) : 0ull;
+    uint32_t rk[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      rk[i] = (i >= j && i < j + m) ? window_rank(w, j, m, i, ~0ull) + (uint32_t)j : (uint32_t)i;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (i >= j && i < j + m && rk[i] != (uint32_t)i) vals[p0 + rk[i]] = v[i];
+  }
+}
+
+// One block per listed run of split codes: find its end; up to kRankMax items are ranked by
+// counting, longer runs are sorted block-wide with their low bits staged in scratch_a.
+__global__ void __launch_bounds__(kFixThreads) k_fixrun_split_long(const uint32_t* __restrict__ hkeys,
+                                                               uint32_t* __restrict__ vals,
+                                                               const uint32_t* __restrict__ lows, uint32_t n,
+                                                               int lbits, unsigned long long* __restrict__ scratch_a,
+                                                               unsigned long long* __restrict__ scratch_b,
+                                                               uint32_t* __restrict__ tvals,
+                                                               const uint32_t* __restrict__ long_list,
+                                                               const uint32_t* __restrict__ long_count) {
+  __shared__ uint32_t s_wh[8 * 256];
+  __shared__ uint32_t s_off[256];
+  __shared__ uint32_t s_w[8];
+  __shared__ uint32_t s_e;
+  const uint32_t count = __ldcg(long_count);
+  const int t = threadIdx.x;
+  for (uint32_t li = blockIdx.x; li < count; li += gridDim.x) {
+    const uint32_t s = __ldcg(long_list + li);
+    const uint32_t h = hkeys[s];
+    if (t == 0) s_e = n;
+    __syncthreads();
+    for (uint32_t base = s + 1; base < n; base += kFixThreads) {
+      const uint32_t q = base + t;
+      if (q < n && hkeys[q] != h) atomicMin(&s_e, q);
+      __syncthreads();
+      const bool found = s_e != n;
+      __syncthreads();
+      if (found) break;
+    }
+    const uint32_t m = s_e - s;
+    if (m <= kRankMax) {
+      for (uint32_t q = t; q < m; q += kFixThreads) s_wh[q] = __ldg(lows + vals[s + q]);
+      __syncthreads();
+      uint32_t vq[kRankMax / kFixThreads], rq[kRankMax / kFixThreads];
+#pragma unroll
+      for (int r = 0; r < kRankMax / kFixThreads; ++r) {
+        const uint32_t q = t + (uint32_t)r * kFixThreads;
+        if (q < m) {
+          const uint32_t lq = s_wh[q];
+          uint32_t rank = 0;
+          for (uint32_t x = 0; x < m; ++x) {
+            const uint32_t lx = s_wh[x];
+            rank += (lx < lq) || (lx == lq && x < q);
+          }
+          vq[r] = vals[s + q];
+          rq[r] = rank;
+        }
+      }
+      __syncthreads();  // every value of the run is read before any is written
+#pragma unroll
+      for (int r = 0; r < kRankMax / kFixThreads; ++r) {
+        const uint32_t q = t + (uint32_t)r * kFixThreads;
+        if (q < m && rq[r] != q) vals[s + rq[r]] = vq[r];
+      }
+    } else {
+      for (uint32_t q = t; q < m; q += kFixThreads) scratch_a[s + q] = __ldg(lows + vals[s + q]);
+      block_sort_run(scratch_a, vals, scratch_b, tvals, s, m, lbits, s_wh, s_off, s_w);
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
@@ -287,6 +425,16 @@ cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned lon
   if (n < 2) return cudaSuccess;
   k_fixrun_short<<<div_up(div_up(n, 4u), 256u), 256, 0, st>>>(keys, vals, n, lbits, long_list, long_count);
   k_fixrun_long<<<152, kFixThreads, 0, st>>>(keys, vals, tkeys, tvals, n, lbits, long_list, long_count);
+  return cudaGetLastError();
+}
+
+cudaError_t sort_fix_runs_split(const uint32_t* hkeys, uint32_t* vals, const uint32_t* lows, uint32_t n, int lbits,
+                                unsigned long long* scratch_a, unsigned long long* scratch_b, uint32_t* tvals,
+                                uint32_t* long_list, uint32_t* long_count, cudaStream_t st) {
+  if (n < 2) return cudaSuccess;
+  k_fixrun_split_short<<<div_up(div_up(n, 4u), 256u), 256, 0, st>>>(hkeys, vals, lows, n, long_list, long_count);
+  k_fixrun_split_long<<<152, kFixThreads, 0, st>>>(hkeys, vals, lows, n, lbits, scratch_a, scratch_b, tvals,
+                                                   long_list, long_count);
   return cudaGetLastError();
 }
 

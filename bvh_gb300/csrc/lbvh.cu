@@ -186,12 +186,15 @@ __device__ __forceinline__ K tri_code(float x0, float y0, float z0, float x1, fl
   return (K)morton_code<BITS>(nx, ny, nz);
 }
 
+// Codes of more than 32 bits are written split: keys = the high 32 bits (code >> (BITS - 32)),
+// which the radix passes sort, and lows = the rest, in input order.
 template <int BITS, typename K>
-__global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4, K* __restrict__ keys,
-                                                Box* __restrict__ boxes, uint32_t* __restrict__ scratch,
-                                                ScratchLayout L) {
+__global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4, uint32_t* __restrict__ keys,
+                                                uint32_t* __restrict__ lows, Box* __restrict__ boxes,
+                                                uint32_t* __restrict__ scratch, ScratchLayout L) {
   constexpr int P = 4;                                   // 8-bit digit passes
   constexpr int S0 = sizeof(K) == 8 ? BITS - 32 : 0;     // first sorted bit
+  constexpr unsigned long long kLowMask = (1ull << S0) - 1ull;
   __shared__ uint32_t s_hist[P][256];
   for (int i = threadIdx.x; i < P * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0;
   __shared__ float s_scene[8];
@@ -217,13 +220,11 @@ __global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4
       c[1] = tri_code<BITS, K>(x0.y, y0.y, z0.y, x1.y, y1.y, z1.y, x2.y, y2.y, z2.y, smn, sext, b[1]);
       c[2] = tri_code<BITS, K>(x0.z, y0.z, z0.z, x1.z, y1.z, z1.z, x2.z, y2.z, z2.z, smn, sext, b[2]);
       c[3] = tri_code<BITS, K>(x0.w, y0.w, z0.w, x1.w, y1.w, z1.w, x2.w, y2.w, z2.w, smn, sext, b[3]);
-      if constexpr (sizeof(K) == 4) {
-        reinterpret_cast<uint4*>(keys)[q] = make_uint4(c[0], c[1], c[2], c[3]);
-      } else {
-        ulonglong2* kp = reinterpret_cast<ulonglong2*>(keys) + 2 * (size_t)q;
-        kp[0] = make_ulonglong2(c[0], c[1]);
-        kp[1] = make_ulonglong2(c[2], c[3]);
-      }
+      reinterpret_cast<uint4*>(keys)[q] = make_uint4((uint32_t)(c[0] >> S0), (uint32_t)(c[1] >> S0),
+                                                     (uint32_t)(c[2] >> S0), (uint32_t)(c[3] >> S0));
+      if constexpr (sizeof(K) == 8)
+        reinterpret_cast<uint4*>(lows)[q] = make_uint4((uint32_t)(c[0] & kLowMask), (uint32_t)(c[1] & kLowMask),
+                                                       (uint32_t)(c[2] & kLowMask), (uint32_t)(c[3] & kLowMask));
       float4* bp = reinterpret_cast<float4*>(boxes + 4 * (size_t)q);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -239,7 +240,8 @@ __global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4
     Box b;
     K c = tri_code<BITS, K>(m.v[0][i], m.v[1][i], m.v[2][i], m.v[3][i], m.v[4][i], m.v[5][i], m.v[6][i],
                             m.v[7][i], m.v[8][i], smn, sext, b);
-    keys[i] = c;
+    keys[i] = (uint32_t)(c >> S0);
+    if constexpr (sizeof(K) == 8) lows[i] = (uint32_t)(c & kLowMask);
     boxes[i] = b;
 #pragma unroll
     for (int p2 = 0; p2 < P; ++p2) atomicAdd(&s_hist[p2][(uint32_t)(c >> (S0 + 8 * p2)) & 255u], 1u);
@@ -612,31 +614,41 @@ static inline void rec(StageEvents* evs, int k, cudaStream_t st) {
   if (evs && evs->use) cudaEventRecord(evs->ev[k], st);
 }
 
+// Split codes keep their low bits in the node buffer, which emission writes only after the delta
+// pass: [lows by original index: 4n B][64-bit run scratch: 8n B], 16-byte aligned; at most
+// 12n + 16 bytes of the 96n - 48 the nodes take.
+static inline uint32_t* split_lows(const Workspace& ws) { return reinterpret_cast<uint32_t*>(ws.nodes); }
+static inline unsigned long long* split_run_scratch(const Workspace& ws, uint32_t n) {
+  return reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(ws.nodes) +
+                                               (((size_t)n * 4 + 15) & ~(size_t)15));
+}
+
 template <int BITS, typename K>
 static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
                                const ScratchLayout& L, int* final_buf) {
-  const int vec4 = all_aligned16(m) ? 1 : 0;
-  // zero only the descriptors this build's passes use
+  uint32_t* lows = sizeof(K) == 8 ? split_lows(ws) : nullptr;
+  const int vec4 = all_aligned16(m) && (reinterpret_cast<uintptr_t>(lows) & 15) == 0 ? 1 : 0;
+  // zero only the descriptors this build's passes use (the passes sort 32-bit keys)
   ScratchLayout Lz = L;
-  const int kb = (int)sizeof(K);
   Lz.zero_end = L.desc + (size_t)4 * div_up(std::max<uint32_t>(n, 1),
-                                             (uint32_t)sort_variant_tile(kb, ws.sort_variant[kb == 4 ? 0 : 1])) * 256;
+                                             (uint32_t)sort_variant_tile(4, ws.sort_variant[0])) * 256;
   k_bounds<<<kBoundsBlocks, 256, 0, st>>>(m, n, vec4, ws.scratch, Lz);
   rec(evs, 1, st);
   const uint32_t work = vec4 ? div_up(n, 4) : n;
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(work, 256), 152 * 8));
-  k_morton<BITS, K><<<grid, 256, 0, st>>>(m, n, vec4, reinterpret_cast<K*>(ws.keys[0]), ws.boxes, ws.scratch, L);
+  k_morton<BITS, K><<<grid, 256, 0, st>>>(m, n, vec4, reinterpret_cast<uint32_t*>(ws.keys[0]), lows, ws.boxes,
+                                          ws.scratch, L);
   rec(evs, 2, st);
-  // 32-bit keys: 4 passes sort them whole.  64-bit keys: 4 passes sort by the high 32 bits
-  // (BITS-32 .. BITS-1), then each run of equal high halves is ordered by its low bits.
-  constexpr int S0 = sizeof(K) == 8 ? BITS - 32 : 0;
-  cudaError_t e = run_sort<K>(ws, n, 4, st, L, final_buf, S0);
+  // 4 passes sort the 32-bit keys: the whole 30-bit code, or the high 32 bits of a 60/63-bit
+  // code; then each run of equal high halves is ordered by its low bits.
+  cudaError_t e = run_sort<uint32_t>(ws, n, 4, st, L, final_buf, 0);
   if (e == cudaSuccess && sizeof(K) == 8) {
     const int fb = *final_buf;
     // the long-run list lives in the delta bytes, which emission has not written yet
-    e = sort_fix_runs(reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb],
-                      reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, S0,
-                      reinterpret_cast<uint32_t*>(ws.delta), ws.scratch + L.counters + kLongRunCounter, st);
+    e = sort_fix_runs_split(reinterpret_cast<const uint32_t*>(ws.keys[fb]), ws.vals[fb], lows, n, BITS - 32,
+                            reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), split_run_scratch(ws, n),
+                            ws.vals[fb ^ 1], reinterpret_cast<uint32_t*>(ws.delta),
+                            ws.scratch + L.counters + kLongRunCounter, st);
   }
   rec(evs, 3, st);
   return e;
@@ -651,13 +663,15 @@ cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStre
   return e;
 }
 
-template <typename K, bool PARENTS>
+template <int BITS, bool PARENTS>
 static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& L, cudaStream_t st) {
-  const K* keys = reinterpret_cast<const K*>(ws.keys[fb]);
+  const uint32_t* keys = reinterpret_cast<const uint32_t*>(ws.keys[fb]);
   const uint32_t* epoch = ws.scratch + L.epoch;
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer, 8 B per position
-  k_delta<K, false><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], nullptr, ws.delta, n);
+  if (BITS == 30) k_delta<uint32_t, false><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], nullptr, ws.delta, n);
+  else
+    k_delta_split<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], split_lows(ws), BITS - 32, ws.delta, n);
   k_emit<SegSingle, PARENTS, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
       ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, SegSingle{n}, nullptr, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegSingle, PARENTS><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
@@ -680,14 +694,18 @@ cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, i
   if (bits == 30) {
     e = lbvh_prefix<30, uint32_t>(ws, m, n, st, evs, L, &fb);
     if (e != cudaSuccess) return e;
-    if (parents) launch_emit<uint32_t, true>(ws, fb, n, L, st);
-    else launch_emit<uint32_t, false>(ws, fb, n, L, st);
-  } else {
-    if (bits == 60) e = lbvh_prefix<60, unsigned long long>(ws, m, n, st, evs, L, &fb);
-    else e = lbvh_prefix<63, unsigned long long>(ws, m, n, st, evs, L, &fb);
+    if (parents) launch_emit<30, true>(ws, fb, n, L, st);
+    else launch_emit<30, false>(ws, fb, n, L, st);
+  } else if (bits == 60) {
+    e = lbvh_prefix<60, unsigned long long>(ws, m, n, st, evs, L, &fb);
     if (e != cudaSuccess) return e;
-    if (parents) launch_emit<unsigned long long, true>(ws, fb, n, L, st);
-    else launch_emit<unsigned long long, false>(ws, fb, n, L, st);
+    if (parents) launch_emit<60, true>(ws, fb, n, L, st);
+    else launch_emit<60, false>(ws, fb, n, L, st);
+  } else {
+    e = lbvh_prefix<63, unsigned long long>(ws, m, n, st, evs, L, &fb);
+    if (e != cudaSuccess) return e;
+    if (parents) launch_emit<63, true>(ws, fb, n, L, st);
+    else launch_emit<63, false>(ws, fb, n, L, st);
   }
   rec(evs, 4, st);
   if (treelet_rounds > 0 && n >= 2) {

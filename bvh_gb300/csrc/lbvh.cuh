@@ -135,6 +135,13 @@ cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cu
 cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
                           uint32_t n, int lbits, uint32_t* long_list, uint32_t* long_count, cudaStream_t st);
 
+// The same for codes held split: hkeys = code >> lbits (sorted by the passes), lows = the low
+// bits by original index.  Only the values move.  scratch_a/scratch_b (8 B per position) and
+// tvals serve the block-wide sort of runs longer than 1024.
+cudaError_t sort_fix_runs_split(const uint32_t* hkeys, uint32_t* vals, const uint32_t* lows, uint32_t n, int lbits,
+                                unsigned long long* scratch_a, unsigned long long* scratch_b, uint32_t* tvals,
+                                uint32_t* long_list, uint32_t* long_count, cudaStream_t st);
+
 // Treelet restructuring passes (LBVH+) after emission; fb = the sort's final ping-pong buffer
 // (the other one is scratch).
 cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream_t st, int fb,
