@@ -81,11 +81,14 @@ __device__ __forceinline__ float pair_area(float4 xa, float4 xb, float4 ja, floa
 }
 
 __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
-  extern __shared__ float4 sw[];  // (kNnTile + 2r) boxes as lo, hi float4 pairs
+  // (kNnTile + 2r) boxes: all lo corners, then all hi corners (lanes read consecutive 16 bytes)
+  extern __shared__ float4 sw[];
   float* sD = reinterpret_cast<float*>(sw + 2 * (kNnTile + 2 * r));  // [kNnKc][kNnTile]
   const uint32_t c = __ldcg(B.ctrl + 0);
   const Box* __restrict__ cbox = B.cbox[__ldcg(B.ctrl + 3) & 1u];
   const int span = kNnTile + 2 * r;
+  float4* s_lo = sw;
+  float4* s_hi = sw + span;
   const int t = threadIdx.x;
   const float kInf = __int_as_float(0x7f800000);
   for (uint32_t base = blockIdx.x * (uint32_t)kNnTile; base < c; base += gridDim.x * (uint32_t)kNnTile) {
@@ -96,8 +99,8 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       const int j = lo + k;
       if (j >= 0 && j < (int)c) {
         const float4* bp = reinterpret_cast<const float4*>(cbox + j);
-        sw[2 * k] = __ldcg(bp);
-        sw[2 * k + 1] = __ldcg(bp + 1);
+        s_lo[k] = __ldcg(bp);
+        s_hi[k] = __ldcg(bp + 1);
       }
     }
     __syncthreads();
@@ -109,8 +112,8 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       fd[m] = ed[m] = kInf;
       fj[m] = ej[m] = -1;
       const int xi = t + m * kPlocThreads;
-      xa[m] = sw[2 * min(xi + r, span - 1)];
-      xb[m] = sw[2 * min(xi + r, span - 1) + 1];
+      xa[m] = s_lo[min(xi + r, span - 1)];
+      xb[m] = s_hi[min(xi + r, span - 1)];
     }
     for (int k0 = 1; k0 <= r; k0 += kNnKc) {
       const int kc = min(kNnKc, r - k0 + 1);
@@ -122,7 +125,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
           const int kmax = min(kc, (int)c - 1 - ((int)base + xi) - k0 + 1);  // j = base + xi + k < c
           for (int kk = 0; kk < kmax; ++kk) {
             const int jw = xi + r + k0 + kk;
-            const float d = pair_area(xa[m], xb[m], sw[2 * jw], sw[2 * jw + 1]);
+            const float d = pair_area(xa[m], xb[m], s_lo[jw], s_hi[jw]);
             if (d < fd[m]) {  // increasing j: the first of equal areas stays
               fd[m] = d;
               fj[m] = (int)base + xi + k0 + kk;
@@ -139,7 +142,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
           const int h = (int)base + p - k;  // the halo cluster; p is the tile-relative target
           if (h >= 0) {
             const int hw = p - k + r;
-            sD[kk * kNnTile + p] = pair_area(sw[2 * hw], sw[2 * hw + 1], sw[2 * (p + r)], sw[2 * (p + r) + 1]);
+            sD[kk * kNnTile + p] = pair_area(s_lo[hw], s_hi[hw], s_lo[p + r], s_hi[p + r]);
           }
         }
       }
