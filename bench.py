@@ -98,23 +98,34 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
 
 def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0, tree_height: int = 0) -> int:
     """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
-    fix-up for 64-bit keys, delta + emission + frontier climb; per treelet pass five (heights,
-    counts, offsets, grouping by height, the fallback check) plus growth, DP and loop control per
-    tree level; PLOC adds
-    cluster init, 4 per clustering iteration (neighbours, tile counts + scan, merge + compaction,
-    loop control) and the root fix
-    (its 30-bit prefix stops after the sort)."""
+    fix-up of 60/63-bit codes (short runs, listed long runs), delta + emission + frontier climb;
+    per treelet pass five (heights, counts, offsets, grouping by height, the fallback check) plus
+    growth, DP and loop control per tree level; PLOC adds cluster init, 4 per clustering iteration
+    (neighbours, tile counts + scan, merge + compaction, loop control) and the root fix (its
+    30-bit prefix stops after the sort)."""
     if algo == "ploc":
         return 2 + 4 + 1 + 4 * ploc_iterations + 1
-    n = 2 + 4 + (1 if bits != 30 else 0) + 3
+    n = 2 + 4 + (2 if bits != 30 else 0) + 3
     return n + (rounds * (5 + 3 * tree_height) if algo == "lbvh_plus" else 0)
+
+
+def batched_kernels_per_build(meshes: int) -> int:
+    """Launches in one batched build: per-mesh box init, bounds and Morton, ceil(K/8) onesweep
+    passes over the K = 30 + mesh-bits keys (4 when K > 32, followed by the two run fix-up
+    kernels), delta + emission + frontier climb."""
+    mbits = 1
+    while mbits < 34 and (1 << mbits) < meshes:
+        mbits += 1
+    kbits = 30 + mbits
+    passes = 4 if kbits > 32 else (kbits + 7) // 8
+    return 3 + passes + (2 if kbits > 32 else 0) + 3
 
 
 STAGE_KERNELS = {
     "scene_bounds": "k_bounds",
     "morton_boxes_hist": "k_morton",
-    "onesweep_sort": "k_onesweep x4 (+ k_fixrun for 60/63-bit keys)",
-    "emit_refit": "k_delta + k_emit + k_emit_climb",
+    "onesweep_sort": "k_onesweep x4 (+ k_fixrun_split_short/_long for 60/63-bit codes)",
+    "emit_refit": "k_delta (k_delta_split for 60/63-bit codes) + k_emit + k_emit_climb",
     "treelet_or_ploc_loop": "LBVH+: k_tl_heights, k_tl_count, k_tl_offsets, k_tl_scatter, then k_tl_grow +"
                             " k_tl_dp per tree height; PLOC: k_ploc_nn, k_ploc_count, k_ploc_scatter, k_ploc_step"
                             " per iteration + k_ploc_root",
@@ -506,7 +517,7 @@ def run_batched(args):
                      "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": bpt},
         "e2e": {"value": round(n * ws / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
                 "d2h_bytes_per_step": 48 * n_nodes + 4 * n, "ms_per_step": round(e2e_ms, 3)},
-        "gpu_launches": args.steps * 13,
+        "gpu_launches": args.steps * batched_kernels_per_build(count),
         "clocks": clk.summary(),
         "autotune": tuning,
     }
