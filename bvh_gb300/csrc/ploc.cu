@@ -115,22 +115,43 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       xa[m] = s_lo[min(xi + r, span - 1)];
       xb[m] = s_hi[min(xi + r, span - 1)];
     }
+    // interior tile: every cluster has all r neighbours on both sides, so full offset chunks
+    // take a path without bounds checks (fully unrolled)
+    const bool interior = (int)base >= r && base + (uint32_t)kNnTile + (uint32_t)r <= c;
     for (int k0 = 1; k0 <= r; k0 += kNnKc) {
       const int kc = min(kNnKc, r - k0 + 1);
+      const bool full = interior && kc == kNnKc;
       // pairs (x, x + k), k in [k0, k0 + kc): forward candidates of x, table entries for x + k
+      if (full) {
 #pragma unroll
-      for (int m = 0; m < kNnPer; ++m) {
-        const int xi = t + m * kPlocThreads;
-        if (xi < tile_n) {
-          const int kmax = min(kc, (int)c - 1 - ((int)base + xi) - k0 + 1);  // j = base + xi + k < c
-          for (int kk = 0; kk < kmax; ++kk) {
+        for (int m = 0; m < kNnPer; ++m) {
+          const int xi = t + m * kPlocThreads;
+#pragma unroll
+          for (int kk = 0; kk < kNnKc; ++kk) {
             const int jw = xi + r + k0 + kk;
             const float d = pair_area(xa[m], xb[m], s_lo[jw], s_hi[jw]);
-            if (d < fd[m]) {  // increasing j: the first of equal areas stays
+            if (d < fd[m]) {
               fd[m] = d;
               fj[m] = (int)base + xi + k0 + kk;
             }
-            if (xi + k0 + kk < tile_n) sD[kk * kNnTile + xi + k0 + kk] = d;
+            if (xi + k0 + kk < kNnTile) sD[kk * kNnTile + xi + k0 + kk] = d;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < kNnPer; ++m) {
+          const int xi = t + m * kPlocThreads;
+          if (xi < tile_n) {
+            const int kmax = min(kc, (int)c - 1 - ((int)base + xi) - k0 + 1);  // j = base + xi + k < c
+            for (int kk = 0; kk < kmax; ++kk) {
+              const int jw = xi + r + k0 + kk;
+              const float d = pair_area(xa[m], xb[m], s_lo[jw], s_hi[jw]);
+              if (d < fd[m]) {  // increasing j: the first of equal areas stays
+                fd[m] = d;
+                fj[m] = (int)base + xi + k0 + kk;
+              }
+              if (xi + k0 + kk < tile_n) sD[kk * kNnTile + xi + k0 + kk] = d;
+            }
           }
         }
       }
@@ -148,17 +169,32 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       }
       __syncthreads();
       // backward candidates j - k of this thread's clusters
+      if (full) {
 #pragma unroll
-      for (int m = 0; m < kNnPer; ++m) {
-        const int xi = t + m * kPlocThreads;
-        if (xi < tile_n) {
-          for (int kk = 0; kk < kc; ++kk) {
-            const int src = (int)base + xi - k0 - kk;
-            if (src < 0) break;
+        for (int m = 0; m < kNnPer; ++m) {
+          const int xi = t + m * kPlocThreads;
+#pragma unroll
+          for (int kk = 0; kk < kNnKc; ++kk) {
             const float d = sD[kk * kNnTile + xi];
-            if (d < kInf && d <= ed[m]) {  // later offset = smaller index: wins ties
+            if (d < kInf && d <= ed[m]) {
               ed[m] = d;
-              ej[m] = src;
+              ej[m] = (int)base + xi - k0 - kk;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < kNnPer; ++m) {
+          const int xi = t + m * kPlocThreads;
+          if (xi < tile_n) {
+            for (int kk = 0; kk < kc; ++kk) {
+              const int src = (int)base + xi - k0 - kk;
+              if (src < 0) break;
+              const float d = sD[kk * kNnTile + xi];
+              if (d < kInf && d <= ed[m]) {  // later offset = smaller index: wins ties
+                ed[m] = d;
+                ej[m] = src;
+              }
             }
           }
         }

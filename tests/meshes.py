@@ -51,6 +51,7 @@ def small_cases():
     for n in (1, 2, 3, 5, 17, 64, 255, 256, 257, 1000, 3071, 3072, 3073, 4097):
         out[f"uniform{n}"] = meshgen.uniform_small(n, seed=n)
     out["identical100"] = identical(100)
+    out["identical5000"] = identical(5000)                    # one run of equal codes > 1024
     out["identical1"] = identical(1)
     out["flat2000"] = flat_z(2000)
     out["clumped5000"] = clumped(5000)
