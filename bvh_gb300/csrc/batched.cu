@@ -95,10 +95,13 @@ __global__ void __launch_bounds__(256) k_seg_bounds(MeshPtrs m, const SegItem* _
   }
 }
 
+// Keys mesh << 30 | code30 are written split: hkeys = key >> shift0 (the passes sort these 32
+// bits) and, when shift0 > 0, lows = the rest, in input order.
 __global__ void __launch_bounds__(256) k_seg_morton(MeshPtrs m, const SegItem* __restrict__ items, uint32_t n_items,
                                                     const float* __restrict__ mbox, int passes, int shift0,
-                                                    unsigned long long* __restrict__ keys, Box* __restrict__ boxes,
-                                                    uint32_t* __restrict__ scratch, ScratchLayout L) {
+                                                    uint32_t* __restrict__ hkeys, uint32_t* __restrict__ lows,
+                                                    Box* __restrict__ boxes, uint32_t* __restrict__ scratch,
+                                                    ScratchLayout L) {
   __shared__ uint32_t s_hist[kMaxPasses][256];
   __shared__ float s_scene[6];
   for (int k = threadIdx.x; k < kMaxPasses * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
@@ -125,7 +128,8 @@ __global__ void __launch_bounds__(256) k_seg_morton(MeshPtrs m, const SegItem* _
         nc[k] = __fdiv_rn(__fsub_rn(c, s_scene[k]), s_scene[3 + k]);
       }
       const unsigned long long key = mesh_bits | morton_code<30>(nc[0], nc[1], nc[2]);
-      keys[i] = key;
+      hkeys[i] = (uint32_t)(key >> shift0);
+      if (shift0) lows[i] = (uint32_t)(key & ((1ull << shift0) - 1ull));
       float4* bp = reinterpret_cast<float4*>(boxes + i);
       bp[0] = make_float4(lo[0], lo[1], lo[2], 0.f);
       bp[1] = make_float4(hi[0], hi[1], hi[2], 0.f);
@@ -149,38 +153,43 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   int mbits = 1;
   while (mbits < 34 && (1ull << mbits) < count) ++mbits;
   // keys have 30 + mbits bits: up to 32 are sorted whole; longer keys are sorted by their high
-  // 32 bits and the runs of equal high bits are then ordered by the rest (sort_fix_runs)
+  // 32 bits and the runs of equal high bits are then ordered by the rest (sort_fix_runs_split);
+  // mbits <= 32 (count is 32-bit), so shift0 <= 30
   const int kbits = 30 + mbits;
   const int shift0 = kbits > 32 ? kbits - 32 : 0;
   const int passes = kbits > 32 ? 4 : (kbits + 7) / 8;
-  L.zero_end = L.desc + (size_t)passes * div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_variant_tile(8, ws.sort_variant[1])) * 256;
+  L.zero_end = L.desc + (size_t)passes * div_up(std::max<uint32_t>(n, 1),
+                                                 (uint32_t)sort_variant_tile(4, ws.sort_variant[0])) * 256;
+  // the low key bits live at the start of the node buffer until the delta pass has read them
+  uint32_t* lows = reinterpret_cast<uint32_t*>(ws.nodes);
+  unsigned long long* run_scratch = reinterpret_cast<unsigned long long*>(
+      reinterpret_cast<unsigned char*>(ws.nodes) + (((size_t)n * 4 + 15) & ~(size_t)15));
   if (evs && evs->use) cudaEventRecord(evs->ev[0], st);
   k_seg_init<<<152 * 4, 256, 0, st>>>(d_mbox, count, ws.scratch, L);
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(n_items, 152 * 8));
   k_seg_bounds<<<grid, 256, 0, st>>>(m, d_items, n_items, d_mbox);
   if (evs && evs->use) cudaEventRecord(evs->ev[1], st);
   k_seg_morton<<<grid, 256, 0, st>>>(m, d_items, n_items, d_mbox, passes, shift0,
-                                                reinterpret_cast<unsigned long long*>(ws.keys[0]), ws.boxes,
-                                                ws.scratch, L);
+                                     reinterpret_cast<uint32_t*>(ws.keys[0]), lows, ws.boxes, ws.scratch, L);
   if (evs && evs->use) cudaEventRecord(evs->ev[2], st);
   int fb = 0;
-  if ((e = run_sort_u64(ws, n, passes, st, L, &fb, shift0)) != cudaSuccess) return e;
+  if ((e = run_sort_u32(ws, n, passes, st, L, &fb)) != cudaSuccess) return e;
+  const uint32_t* hkeys = reinterpret_cast<const uint32_t*>(ws.keys[fb]);
   if (shift0 > 0 &&
-      (e = sort_fix_runs(reinterpret_cast<unsigned long long*>(ws.keys[fb]), ws.vals[fb],
-                         reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), ws.vals[fb ^ 1], n, shift0,
-                         reinterpret_cast<uint32_t*>(ws.delta), ws.scratch + L.counters + kLongRunCounter, st)) !=
-          cudaSuccess)
+      (e = sort_fix_runs_split(hkeys, ws.vals[fb], lows, n, shift0,
+                               reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), run_scratch, ws.vals[fb ^ 1],
+                               reinterpret_cast<uint32_t*>(ws.delta), ws.scratch + L.counters + kLongRunCounter,
+                               st)) != cudaSuccess)
     return e;
   if (evs && evs->use) cudaEventRecord(evs->ev[3], st);
-  const unsigned long long* keys = reinterpret_cast<const unsigned long long*>(ws.keys[fb]);
-  k_delta<unsigned long long, true><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], d_offsets, ws.delta, n);
+  k_delta_seg_split<<<div_up(n, 256), 256, 0, st>>>(hkeys, ws.vals[fb], lows, d_offsets, shift0, ws.delta, n);
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer
+  const SegBatch seg{hkeys, d_offsets, 30 - shift0};
   k_emit<SegBatch, false, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
-      ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, SegBatch{keys, d_offsets}, d_indices, frontier, fcount,
-      kEmitMaxSteps);
+      ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, seg, d_indices, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegBatch, false><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
-      ws.delta, ws.nodes, ws.slots, ws.scratch + L.epoch, n, SegBatch{keys, d_offsets}, frontier, fcount);
+      ws.delta, ws.nodes, ws.slots, ws.scratch + L.epoch, n, seg, frontier, fcount);
   if (evs && evs->use) {
     cudaEventRecord(evs->ev[4], st);
     cudaEventRecord(evs->ev[5], st);

@@ -33,11 +33,13 @@ struct SegSingle {
 
 // Batched meshes: key = mesh << 30 | code30; mesh m owns sorted positions
 // [offsets[m], offsets[m+1]) and node ids [2*offsets[m] - m, ...).
+// hkeys = (mesh << 30 | code30) >> shift0, so the mesh is hkeys >> (30 - shift0).
 struct SegBatch {
-  const unsigned long long* keys;
+  const uint32_t* hkeys;
   const uint32_t* offsets;
+  int mshift;  // 30 - shift0
   __device__ __forceinline__ void get(uint32_t i, uint32_t& off, uint32_t& cnt, uint32_t& nbase) const {
-    const uint32_t m = (uint32_t)(__ldg(keys + i) >> 30);
+    const uint32_t m = __ldg(hkeys + i) >> mshift;
     off = __ldg(offsets + m);
     cnt = __ldg(offsets + m + 1) - off;
     nbase = 2 * off - m;
@@ -122,6 +124,31 @@ static __global__ void __launch_bounds__(256)
     const uint32_t va = __ldg(vals + k), vb = __ldg(vals + k + 1);
     const uint32_t la = __ldg(lows + va), lb = __ldg(lows + vb);
     d = la != lb ? 32 + __clz(la ^ lb) : 96 + __clz(va ^ vb);
+  }
+  D[k] = (uint8_t)(d + 1);
+}
+
+// Batched meshes: keys mesh << 30 | code30 held split as hk = key >> shift0 (sorted) and lows =
+// key & (2^shift0 - 1) by original index.  delta = -1 across meshes, the clz of the 30-bit code
+// XOR within a mesh, 32 + clz of the in-mesh indices' XOR for equal codes (as k_delta<u64, true>).
+static __global__ void __launch_bounds__(256)
+    k_delta_seg_split(const uint32_t* __restrict__ hk, const uint32_t* __restrict__ vals,
+                      const uint32_t* __restrict__ lows, const uint32_t* __restrict__ offsets, int shift0,
+                      uint8_t* __restrict__ D, uint32_t n) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k + 1 >= n) return;
+  const uint32_t a = __ldg(hk + k), b = __ldg(hk + k + 1);
+  const uint32_t ma = a >> (30 - shift0), mb = b >> (30 - shift0);
+  int d;
+  if (ma != mb) {
+    d = -1;
+  } else if (a != b) {
+    d = __clz((uint32_t)((unsigned long long)(a ^ b) << shift0));
+  } else {
+    const uint32_t va = __ldg(vals + k), vb = __ldg(vals + k + 1);
+    const uint32_t la = shift0 ? __ldg(lows + va) : 0u, lb = shift0 ? __ldg(lows + vb) : 0u;
+    const uint32_t off = __ldg(offsets + ma);
+    d = la != lb ? __clz(la ^ lb) : 32 + __clz((va - off) ^ (vb - off));
   }
   D[k] = (uint8_t)(d + 1);
 }

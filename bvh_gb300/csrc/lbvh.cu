@@ -683,6 +683,11 @@ cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st,
   return run_sort<unsigned long long>(ws, n, passes, st, L, final_buf, shift0);
 }
 
+cudaError_t run_sort_u32(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
+                         int* final_buf) {
+  return run_sort<uint32_t>(ws, n, passes, st, L, final_buf, 0);
+}
+
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,
                        StageEvents* evs, uint32_t** out_indices, bool host_loops) {
   cudaError_t e = workspace_reserve(ws, n, st);

@@ -153,6 +153,9 @@ constexpr size_t kTlCtlWord = 256 + 264 + 256;
 // `passes` stable 8-bit LSD passes over 64-bit keys, starting at bit shift0.
 cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
                          int* final_buf, int shift0 = 0);
+// The same over 32-bit keys (the whole key; passes * 8 bits of it).
+cudaError_t run_sort_u32(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
+                         int* final_buf);
 
 // A slice of one mesh handled by one block of the batched per-mesh kernels.
 struct SegItem {
