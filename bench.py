@@ -456,7 +456,7 @@ def run_batched(args):
         # plain per-mesh loop of single-mesh builds on the same device-resident data
         single = bvh_gb300.Context(local)
         single.reserve(int(counts.max()))
-        single.set_tuning(*ctx.tuning())
+        single.set_tuning(ctx.tuning())
         loop_reps = 2
         for _ in range(1):
             for m in range(count):

@@ -145,13 +145,14 @@ class Context:
         C.check(self.lib.bvh_autotune(self.handle, n, ctypes.c_void_p(stream), buf, len(buf)), "bvh_autotune")
         return json.loads(buf.value.decode())
 
-    def tuning(self):
-        a, b = ctypes.c_int32(), ctypes.c_int32()
-        C.check(self.lib.bvh_tuning_get(self.handle, ctypes.byref(a), ctypes.byref(b)), "bvh_tuning_get")
-        return a.value, b.value
+    def tuning(self) -> int:
+        """The sort variant this context uses (bvh_tuning_get)."""
+        a = ctypes.c_int32()
+        C.check(self.lib.bvh_tuning_get(self.handle, ctypes.byref(a)), "bvh_tuning_get")
+        return a.value
 
-    def set_tuning(self, v32: int, v64: int):
-        C.check(self.lib.bvh_tuning_set(self.handle, v32, v64), "bvh_tuning_set")
+    def set_tuning(self, variant: int):
+        C.check(self.lib.bvh_tuning_set(self.handle, variant), "bvh_tuning_set")
 
     def build_host(self, mesh: TriangleMesh, params: C.Params, stream: int = 0):
         """Upload, build, download (BVHBuilder::build).  Returns (nodes, indices)."""

@@ -159,7 +159,7 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   const int shift0 = kbits > 32 ? kbits - 32 : 0;
   const int passes = kbits > 32 ? 4 : (kbits + 7) / 8;
   L.zero_end = L.desc + (size_t)passes * div_up(std::max<uint32_t>(n, 1),
-                                                 (uint32_t)sort_variant_tile(4, ws.sort_variant[0])) * 256;
+                                                 (uint32_t)sort_variant_tile(ws.sort_variant)) * 256;
   // the low key bits live at the start of the node buffer until the delta pass has read them
   uint32_t* lows = reinterpret_cast<uint32_t*>(ws.nodes);
   unsigned long long* run_scratch = reinterpret_cast<unsigned long long*>(

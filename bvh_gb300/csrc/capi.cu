@@ -469,43 +469,36 @@ extern "C" bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char*
   cudaSetDevice(ctx->device);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int nv = sort_variant_count();
-  std::vector<float> ms(2 * nv, 0.0f);
+  std::vector<float> ms(nv, 0.0f);
   cudaError_t e = autotune_sort(ctx->ws, n, st, ms.data());
   if (e != cudaSuccess) return from_cuda(e);
   if (json_out && json_cap) {
-    std::string js = "{\"n\": " + std::to_string(n) + ", \"sort\": {";
-    for (int kb = 0; kb < 2; ++kb) {
-      js += std::string(kb ? ", " : "") + (kb ? "\"keys64\"" : "\"keys32\"") + ": {\"chosen\": " +
-            std::to_string(ctx->ws.sort_variant[kb]) + ", \"variants\": [";
-      for (int v = 0; v < nv; ++v) {
-        int ipt, w, mb;
-        sort_variant_describe(kb ? 8 : 4, v, &ipt, &w, &mb);
-        char buf[160];
-        snprintf(buf, sizeof(buf), "%s{\"items_per_thread\": %d, \"lookback_window\": %d, \"min_blocks\": %d, "
-                 "\"ms\": %.4f}", v ? ", " : "", ipt, w, mb, ms[kb * nv + v]);
-        js += buf;
-      }
-      js += "]}";
+    std::string js = "{\"n\": " + std::to_string(n) + ", \"sort\": {\"chosen\": " +
+                     std::to_string(ctx->ws.sort_variant) + ", \"variants\": [";
+    for (int v = 0; v < nv; ++v) {
+      int ipt, w, mb;
+      sort_variant_describe(v, &ipt, &w, &mb);
+      char buf[160];
+      snprintf(buf, sizeof(buf), "%s{\"items_per_thread\": %d, \"lookback_window\": %d, \"min_blocks\": %d, "
+               "\"ms\": %.4f}", v ? ", " : "", ipt, w, mb, ms[v]);
+      js += buf;
     }
-    js += "}}";
+    js += "]}}";
     if (js.size() + 1 > json_cap) return BVH_ERR_INVALID_ARG;
     memcpy(json_out, js.c_str(), js.size() + 1);
   }
   return BVH_OK;
 }
 
-extern "C" bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* v32, int32_t* v64) {
-  if (!ctx || !v32 || !v64) return BVH_ERR_INVALID_ARG;
-  *v32 = ctx->ws.sort_variant[0];
-  *v64 = ctx->ws.sort_variant[1];
+extern "C" bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant) {
+  if (!ctx || !variant) return BVH_ERR_INVALID_ARG;
+  *variant = ctx->ws.sort_variant;
   return BVH_OK;
 }
 
-extern "C" bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t v32, int32_t v64) {
-  const int nv = sort_variant_count();
-  if (!ctx || v32 < 0 || v32 >= nv || v64 < 0 || v64 >= nv) return BVH_ERR_INVALID_ARG;
-  ctx->ws.sort_variant[0] = v32;
-  ctx->ws.sort_variant[1] = v64;
+extern "C" bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant) {
+  if (!ctx || variant < 0 || variant >= sort_variant_count()) return BVH_ERR_INVALID_ARG;
+  ctx->ws.sort_variant = variant;
   return BVH_OK;
 }
 

@@ -80,31 +80,14 @@ __device__ __forceinline__ unsigned long long atom_exch_acq_rel(unsigned long lo
   return old;
 }
 
-// delta(k, k+1) + 1 as a byte.  K = key type; BATCH selects the segmented 30-bit rule.
-template <typename K, bool BATCH>
-__global__ void __launch_bounds__(256) k_delta(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
-                                               const uint32_t* __restrict__ offsets, uint8_t* __restrict__ D,
-                                               uint32_t n) {
+// delta(k, k+1) + 1 of 30-bit codes as a byte.
+static __global__ void __launch_bounds__(256) k_delta(const uint32_t* __restrict__ keys,
+                                                      const uint32_t* __restrict__ vals, uint8_t* __restrict__ D,
+                                                      uint32_t n) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k + 1 >= n) return;
-  const K a = __ldg(keys + k), b = __ldg(keys + k + 1);
-  int d;
-  if constexpr (BATCH) {
-    const uint32_t ma = (uint32_t)((unsigned long long)a >> 30), mb = (uint32_t)((unsigned long long)b >> 30);
-    if (ma != mb) {
-      d = -1;
-    } else if (a == b) {
-      const uint32_t off = __ldg(offsets + ma);
-      d = 32 + __clz((__ldg(vals + k) - off) ^ (__ldg(vals + k + 1) - off));
-    } else {
-      d = __clz((uint32_t)((a ^ b) & 0x3FFFFFFFull));
-    }
-  } else if constexpr (sizeof(K) == 4) {
-    d = a == b ? 32 + __clz(__ldg(vals + k) ^ __ldg(vals + k + 1)) : __clz((uint32_t)(a ^ b));
-  } else {
-    d = a == b ? 64 + __clzll((unsigned long long)(__ldg(vals + k) ^ __ldg(vals + k + 1)))
-               : __clzll((unsigned long long)(a ^ b));
-  }
+  const uint32_t a = __ldg(keys + k), b = __ldg(keys + k + 1);
+  const int d = a == b ? 32 + __clz(__ldg(vals + k) ^ __ldg(vals + k + 1)) : __clz(a ^ b);
   D[k] = (uint8_t)(d + 1);
 }
 
@@ -130,7 +113,7 @@ static __global__ void __launch_bounds__(256)
 
 // Batched meshes: keys mesh << 30 | code30 held split as hk = key >> shift0 (sorted) and lows =
 // key & (2^shift0 - 1) by original index.  delta = -1 across meshes, the clz of the 30-bit code
-// XOR within a mesh, 32 + clz of the in-mesh indices' XOR for equal codes (as k_delta<u64, true>).
+// XOR within a mesh, 32 + clz of the in-mesh indices' XOR for equal codes.
 static __global__ void __launch_bounds__(256)
     k_delta_seg_split(const uint32_t* __restrict__ hk, const uint32_t* __restrict__ vals,
                       const uint32_t* __restrict__ lows, const uint32_t* __restrict__ offsets, int shift0,

@@ -1,20 +1,22 @@
-// fixrun.cu -- finishes a 64-bit key sort whose radix passes covered only the high 32 bits.
+// fixrun.cu -- finishes a sort of 60/63-bit codes (and of the batched path's mesh-prefixed
+// keys) whose radix passes covered only the high 32 bits.
 //
 // The LBVH with 60/63-bit Morton codes needs the (code, original index) order that a full
 // 8-pass LSD radix sort produces (cub::DeviceRadixSort::SortPairs, lbvh_builder.cu:413-438;
-// thrust::sort_by_key, lbvh_plus_builder.cu:465).  Here the onesweep passes sort only by
-// H = code >> lbits (4 passes, lbits = 31 or 28); within each run of equal H the items are then
-// still in original-index order (every pass is stable and the first one numbers the items), so
-// ordering each run by (L = code & (2^lbits - 1), position) completes the sort.  On real meshes
-// almost every run has length 1, so this costs one read of the keys instead of four more passes.
+// thrust::sort_by_key, lbvh_plus_builder.cu:465).  Here the codes are held split: the onesweep
+// passes sort (H = code >> lbits, original index) pairs, and L = code & (2^lbits - 1) stays in
+// input order.  Within each run of equal H the items are then still in original-index order
+// (every pass is stable and the first one numbers the items), so ordering each run by
+// (L, position) completes the sort.  On real meshes most runs have length 1 or 2, so this costs
+// one read of the sorted halves instead of four more passes.
 //
-// k_fixrun_short: one thread per 4 consecutive positions, with the next thread's 4 keys (from
-// the adjacent lane) as an 8-key window.  A thread owns the runs that START in its 4 positions
-// (a run's first position differs from its predecessor).  A run that ends inside the window is
-// ranked in registers (rank = count of smaller (L, position) pairs) and written back in place;
-// a longer one is appended to a list,
-// which k_fixrun_long sorts, one run per block, with a block-wide stable LSD over L through the
-// same positions of the other key/value buffer.  Other threads read positions of a run only
+// k_fixrun_split_short: one thread per 4 consecutive positions, with the next thread's 4 (from
+// the adjacent lane) as an 8-position window.  A thread owns the runs that START in its 4
+// positions (a run's first position differs from its predecessor).  A run that ends inside the
+// window is ranked in registers (rank = count of smaller (L, position) pairs; pairs take one
+// compare) and only its values move; a longer one is appended to a list, which
+// k_fixrun_split_long ranks by counting in shared memory (up to 1024 items) or sorts with a
+// block-wide stable LSD over L through idle buffers.  Other threads read positions of a run only
 // for H, which a permutation within the run does not change.
 #include "lbvh.cuh"
 
@@ -127,161 +129,7 @@ __device__ __forceinline__ uint32_t window_rank(const unsigned long long (&w)[8]
   return r;
 }
 
-__global__ void __launch_bounds__(256, 4) k_fixrun_short(unsigned long long* __restrict__ keys,
-                                                      uint32_t* __restrict__ vals, uint32_t n, int lbits,
-                                                      uint32_t* __restrict__ long_list,
-                                                      uint32_t* __restrict__ long_count) {
-  constexpr unsigned long long kNoH = ~0ull;  // "no position": H is below 2^32
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
-  // window: this thread's 4 keys, then the next thread's 4 (kNoH-keyed past n)
-  // (values alongside, so that a reorder needs no second round trip)
-  unsigned long long w[8];
-  uint32_t v[8];
-  if (p0 + 4 <= n) {
-    const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(keys + p0);
-    const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(keys + p0 + 2);
-    const uint4 c = *reinterpret_cast<const uint4*>(vals + p0);
-    w[0] = a.x;
-    w[1] = a.y;
-    w[2] = b.x;
-    w[3] = b.y;
-    v[0] = c.x;
-    v[1] = c.y;
-    v[2] = c.z;
-    v[3] = c.w;
-  } else {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      w[j] = p0 + j < n ? keys[p0 + j] : kNoH;
-      v[j] = p0 + j < n ? vals[p0 + j] : 0u;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    w[4 + j] = __shfl_down_sync(0xffffffffu, w[j], 1);
-    v[4 + j] = __shfl_down_sync(0xffffffffu, v[j], 1);
-  }
-  if (lane == 31) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      w[4 + j] = p0 + 4 + j < n ? keys[p0 + 4 + j] : kNoH;
-      v[4 + j] = p0 + 4 + j < n ? vals[p0 + 4 + j] : 0u;
-    }
-  }
-  unsigned long long hw[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) hw[q] = w[q] == kNoH ? kNoH : w[q] >> lbits;
-  unsigned long long hprev = __shfl_up_sync(0xffffffffu, hw[3], 1);
-  if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? keys[p0 - 1] >> lbits : kNoH;
-  const unsigned long long lmask = (1ull << lbits) - 1ull;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const unsigned long long hp = j == 0 ? hprev : hw[j - 1];
-    if (hw[j] == kNoH || hw[j] == hp || hw[j] != hw[j + 1]) continue;  // not the start of a run of 2+
-    const uint32_t s = p0 + j;
-    // run length inside the window
-    int m = 2;
-#pragma unroll
-    for (int q = j + 2; q < 8; ++q) m += (m == q - j && hw[q] == hw[j]) ? 1 : 0;
-    // a run that reaches the end of the window and goes on (at least 6 items) takes the
-    // block-wide path
-    if (j + m == 8 && p0 + 8 < n && (keys[p0 + 8] >> lbits) == hw[j]) {
-      long_list[atomicAdd(long_count, 1u)] = s;
-      continue;
-    }
-    if (m == 2) {  // the common case: swap when out of order
-      if ((w[j] & lmask) > (w[j + 1] & lmask)) {
-        keys[s] = w[j + 1];
-        keys[s + 1] = w[j];
-        vals[s] = v[j + 1];
-        vals[s + 1] = v[j];
-      }
-      continue;
-    }
-    uint32_t rk[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      rk[i] = (i >= j && i < j + m) ? window_rank(w, j, m, i, lmask) + (uint32_t)j : (uint32_t)i;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if (i >= j && i < j + m && rk[i] != (uint32_t)i) {
-        keys[p0 + rk[i]] = w[i];
-        vals[p0 + rk[i]] = v[i];
-      }
-    }
-  }
-}
-
-// One block per listed run (one that outgrew its thread's window): find its end, then sort it
-// by its low bits.
-__global__ void __launch_bounds__(kFixThreads) k_fixrun_long(unsigned long long* __restrict__ keys,
-                                                         uint32_t* __restrict__ vals,
-                                                         unsigned long long* __restrict__ tkeys,
-                                                         uint32_t* __restrict__ tvals, uint32_t n, int lbits,
-                                                         const uint32_t* __restrict__ long_list,
-                                                         const uint32_t* __restrict__ long_count) {
-  __shared__ uint32_t s_wh[8 * 256];
-  __shared__ uint32_t s_off[256];
-  __shared__ uint32_t s_w[8];
-  __shared__ uint32_t s_e;
-  const uint32_t count = __ldcg(long_count);
-  const int t = threadIdx.x;
-  for (uint32_t li = blockIdx.x; li < count; li += gridDim.x) {
-    const uint32_t s = __ldcg(long_list + li);
-    const unsigned long long h = keys[s] >> lbits;
-    if (t == 0) s_e = n;
-    __syncthreads();
-    for (uint32_t base = s + 1; base < n; base += kFixThreads) {
-      const uint32_t q = base + t;
-      if (q < n && (keys[q] >> lbits) != h) atomicMin(&s_e, q);
-      __syncthreads();
-      const bool found = s_e != n;
-      __syncthreads();
-      if (found) break;
-    }
-    const uint32_t m = s_e - s;
-    if (m <= kRankMax) {
-      // rank by counting: each thread takes items t, t + 256, ...; the low bits of the run's
-      // keys sit in s_wh (kRankMax words)
-      const unsigned long long lmask = (1ull << lbits) - 1ull;
-      for (uint32_t q = t; q < m; q += kFixThreads) s_wh[q] = (uint32_t)(keys[s + q] & lmask);
-      __syncthreads();
-      unsigned long long kq[kRankMax / kFixThreads];
-      uint32_t vq[kRankMax / kFixThreads], rq[kRankMax / kFixThreads];
-#pragma unroll
-      for (int r = 0; r < kRankMax / kFixThreads; ++r) {
-        const uint32_t q = t + (uint32_t)r * kFixThreads;
-        if (q < m) {
-          const uint32_t lq = s_wh[q];
-          uint32_t rank = 0;
-          for (uint32_t x = 0; x < m; ++x) {
-            const uint32_t lx = s_wh[x];
-            rank += (lx < lq) || (lx == lq && x < q);
-          }
-          kq[r] = keys[s + q];
-          vq[r] = vals[s + q];
-          rq[r] = rank;
-        }
-      }
-      __syncthreads();  // every item of the run is read before any is written
-#pragma unroll
-      for (int r = 0; r < kRankMax / kFixThreads; ++r) {
-        const uint32_t q = t + (uint32_t)r * kFixThreads;
-        if (q < m && rq[r] != q) {
-          keys[s + rq[r]] = kq[r];
-          vals[s + rq[r]] = vq[r];
-        }
-      }
-    } else {
-      block_sort_run(keys, vals, tkeys, tvals, s, m, lbits, s_wh, s_off, s_w);
-    }
-    __syncthreads();
-  }
-}
-
-// Split codes: H = hkeys[position] (sorted), L = lows[original index].  Same ownership rules as
-// k_fixrun_short; only the values of a run move.
+// H = hkeys[position] (sorted), L = lows[original index]; only the values of a run move.
 __global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __restrict__ hkeys,
                                                             uint32_t* __restrict__ vals,
                                                             const uint32_t* __restrict__ lows, uint32_t n,
@@ -419,14 +267,6 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun_split_long(const uint32_
 }
 
 }  // namespace
-
-cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
-                          uint32_t n, int lbits, uint32_t* long_list, uint32_t* long_count, cudaStream_t st) {
-  if (n < 2) return cudaSuccess;
-  k_fixrun_short<<<div_up(div_up(n, 4u), 256u), 256, 0, st>>>(keys, vals, n, lbits, long_list, long_count);
-  k_fixrun_long<<<152, kFixThreads, 0, st>>>(keys, vals, tkeys, tvals, n, lbits, long_list, long_count);
-  return cudaGetLastError();
-}
 
 cudaError_t sort_fix_runs_split(const uint32_t* hkeys, uint32_t* vals, const uint32_t* lows, uint32_t n, int lbits,
                                 unsigned long long* scratch_a, unsigned long long* scratch_b, uint32_t* tvals,

@@ -25,7 +25,7 @@ namespace bvhgb {
 // ---------------------------------------------------------------------------------------
 // scratch
 // ---------------------------------------------------------------------------------------
-int sort_tile(int key_bytes) { return kSortThreads * (key_bytes == 4 ? 8 : 6); }  // smallest variant tile
+int sort_tile() { return kSortThreads * 8; }  // smallest variant tile (8 keys per thread)
 
 ScratchLayout scratch_layout(uint32_t n) {
   ScratchLayout L;
@@ -42,8 +42,8 @@ ScratchLayout scratch_layout(uint32_t n) {
   L.counters = o; o += 16;
   L.hist = o; o += (size_t)kMaxPasses * 256;
   L.desc = o;
-  // the smaller tile (64-bit keys) gives the most tiles
-  size_t tiles = div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_tile(8));
+  // the smallest variant tile gives the most tiles
+  size_t tiles = div_up(std::max<uint32_t>(n, 1), (uint32_t)sort_tile());
   o += (size_t)kMaxPasses * tiles * 256;
   L.zero_end = o;
   L.total = o;
@@ -311,7 +311,7 @@ __device__ __forceinline__ void warp_rank(const K (&key)[IPT], uint32_t (&rnk)[I
 template <typename K, int THREADS, int IPT, int W, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                       K* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
-                                                      int pass, int shift0, uint32_t* __restrict__ scratch, ScratchLayout L,
+                                                      int pass, uint32_t* __restrict__ scratch, ScratchLayout L,
                                                       uint32_t tiles) {
   constexpr int BINS = 256, NW = THREADS / 32, TILE = THREADS * IPT;
   static_assert(THREADS == BINS, "one thread per bin");
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict_
   uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_scan + 32);
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int shift = shift0 + 8 * pass;  // digit `pass` of the bits sorted by this sequence of passes
+  const int shift = 8 * pass;  // digit `pass` of the key
   if (tid == 0) *s_tile = atomicAdd(scratch + L.counters + pass, 1u);
   for (int b = tid; b < NW * BINS; b += THREADS) s_whist[b] = 0;
   __syncthreads();
@@ -419,25 +419,18 @@ constexpr SortVariant make_variant() {
                          (size_t)(kSortThreads / 32) * 256 * 4 + 2 * 256 * 4 + 32 * 8 + 16};
 }
 
-static const SortVariant kVariants32[] = {
+static const SortVariant kVariants[] = {
     make_variant<uint32_t, 16, 32, 2>(), make_variant<uint32_t, 16, 16, 3>(), make_variant<uint32_t, 12, 32, 3>(),
     make_variant<uint32_t, 8, 32, 4>(),
 };
-static const SortVariant kVariants64[] = {
-    make_variant<unsigned long long, 12, 32, 2>(), make_variant<unsigned long long, 12, 16, 3>(),
-    make_variant<unsigned long long, 8, 32, 3>(), make_variant<unsigned long long, 6, 32, 4>(),
-};
 constexpr int kNumVariants = 4;
 
-static const SortVariant& variant(int key_bytes, int v) {
-  v = v < 0 || v >= kNumVariants ? 0 : v;
-  return key_bytes == 4 ? kVariants32[v] : kVariants64[v];
-}
+static const SortVariant& variant(int v) { return kVariants[v < 0 || v >= kNumVariants ? 0 : v]; }
 
 int sort_variant_count() { return kNumVariants; }
-int sort_variant_tile(int key_bytes, int v) { return kSortThreads * variant(key_bytes, v).ipt; }
-void sort_variant_describe(int key_bytes, int v, int* ipt, int* window, int* minb) {
-  const SortVariant& sv = variant(key_bytes, v);
+int sort_variant_tile(int v) { return kSortThreads * variant(v).ipt; }
+void sort_variant_describe(int v, int* ipt, int* window, int* minb) {
+  const SortVariant& sv = variant(v);
   *ipt = sv.ipt;
   *window = sv.window;
   *minb = sv.minb;
@@ -446,19 +439,18 @@ void sort_variant_describe(int key_bytes, int v, int* ipt, int* window, int* min
 // Kernel attributes set once per device, outside any stream capture.
 cudaError_t prepare_kernels() {
   for (int v = 0; v < kNumVariants; ++v) {
-    for (int kb : {4, 8}) {
-      const SortVariant& sv = variant(kb, v);
-      cudaError_t e = cudaFuncSetAttribute(sv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv.smem);
-      if (e != cudaSuccess) return e;
-    }
+    const SortVariant& sv = variant(v);
+    cudaError_t e = cudaFuncSetAttribute(sv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sv.smem);
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
-template <typename K>
-cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L, int* final_buf,
-                     int shift0 = 0) {
-  const SortVariant& sv = variant((int)sizeof(K), ws.sort_variant[sizeof(K) == 4 ? 0 : 1]);
+// `passes` stable 8-bit passes over the 32-bit keys in ws.keys[0] (values: the original index).
+static cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
+                            int* final_buf) {
+  using K = uint32_t;
+  const SortVariant& sv = variant(ws.sort_variant);
   const uint32_t tile = (uint32_t)kSortThreads * sv.ipt;
   uint32_t tiles = div_up(n, tile);
   int cur = 0;
@@ -469,7 +461,7 @@ cudaError_t run_sort(Workspace& ws, uint32_t n, int passes, cudaStream_t st, con
     uint32_t* vout = ws.vals[cur ^ 1];
     uint32_t* scratch = ws.scratch;
     ScratchLayout Lc = L;
-    void* args[] = {(void*)&kin, (void*)&vin, (void*)&kout, (void*)&vout, (void*)&n, (void*)&p, (void*)&shift0, (void*)&scratch,
+    void* args[] = {(void*)&kin, (void*)&vin, (void*)&kout, (void*)&vout, (void*)&n, (void*)&p, (void*)&scratch,
                     (void*)&Lc, (void*)&tiles};
     cudaError_t e = cudaLaunchKernel(sv.fn, dim3(tiles), dim3(kSortThreads), args, sv.smem, st);
     if (e != cudaSuccess) return e;
@@ -489,41 +481,36 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 
-// Pseudo-random keys (63 or 30 bits) with the radix histograms of the 4 passes that start at
-// bit shift0.
-template <typename K>
-__global__ void __launch_bounds__(256) k_tune_keys(K* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
-                                                   int shift0) {
+// Pseudo-random 32-bit keys with the radix histograms of the 4 passes.
+__global__ void __launch_bounds__(256) k_tune_keys(uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
   constexpr int P = 4;
   __shared__ uint32_t s_hist[P][256];
   for (int k = threadIdx.x; k < P * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
   __syncthreads();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const unsigned long long z = mix64(i);
-    const K k = sizeof(K) == 4 ? (K)(z >> 34) : (K)(z >> 1);
+    const uint32_t k = (uint32_t)(mix64(i) >> 32);
     keys[i] = k;
 #pragma unroll
-    for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p][(uint32_t)(k >> (shift0 + 8 * p)) & 255u], 1u);
+    for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p][(k >> (8 * p)) & 255u], 1u);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < P * 256; k += blockDim.x)
     if ((&s_hist[0][0])[k]) atomicAdd(hist + k, (&s_hist[0][0])[k]);
 }
 
-template <typename K>
-static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const ScratchLayout& L, float* ms) {
-  const int kb = (int)sizeof(K);
-  cudaError_t e = cudaMemsetAsync(ws.scratch + L.zero_begin, 0, (L.zero_end - L.zero_begin) * 4, st);
+cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms) {
+  cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
-  // the builds sort 64-bit keys by their high 32 bits (then fix runs), 32-bit keys whole
-  const int shift0 = kb == 8 ? 31 : 0;
-  k_tune_keys<K><<<152 * 8, 256, 0, st>>>(reinterpret_cast<K*>(ws.keys[0]), n, ws.scratch + L.hist, shift0);
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  if ((e = cudaMemsetAsync(ws.scratch + L.zero_begin, 0, (L.zero_end - L.zero_begin) * 4, st)) != cudaSuccess)
+    return e;
+  k_tune_keys<<<152 * 8, 256, 0, st>>>(reinterpret_cast<uint32_t*>(ws.keys[0]), n, ws.scratch + L.hist);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   int best = 0;
   for (int v = 0; v < kNumVariants; ++v) {
-    ws.sort_variant[kb == 4 ? 0 : 1] = v;
+    ws.sort_variant = v;
     float vbest = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {
       // tile counters and look-back words start at zero; the histograms stay valid (the keys
@@ -532,7 +519,7 @@ static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const 
       cudaMemsetAsync(ws.scratch + L.desc, 0, (L.zero_end - L.desc) * 4, st);
       int fb = 0;
       cudaEventRecord(e0, st);
-      e = run_sort<K>(ws, n, 4, st, L, &fb, shift0);
+      e = run_sort(ws, n, 4, st, L, &fb);
       cudaEventRecord(e1, st);
       if (e == cudaSuccess) e = cudaEventSynchronize(e1);
       if (e != cudaSuccess) break;
@@ -546,16 +533,8 @@ static cudaError_t tune_width(Workspace& ws, uint32_t n, cudaStream_t st, const 
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  ws.sort_variant[kb == 4 ? 0 : 1] = best;
+  ws.sort_variant = best;
   return e;
-}
-
-cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out) {
-  cudaError_t e = workspace_reserve(ws, n, st);
-  if (e != cudaSuccess) return e;
-  ScratchLayout L = scratch_layout(ws.cap_n);
-  if ((e = tune_width<uint32_t>(ws, n, st, L, ms_out)) != cudaSuccess) return e;
-  return tune_width<unsigned long long>(ws, n, st, L, ms_out + kNumVariants);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -631,7 +610,7 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   // zero only the descriptors this build's passes use (the passes sort 32-bit keys)
   ScratchLayout Lz = L;
   Lz.zero_end = L.desc + (size_t)4 * div_up(std::max<uint32_t>(n, 1),
-                                             (uint32_t)sort_variant_tile(4, ws.sort_variant[0])) * 256;
+                                             (uint32_t)sort_variant_tile(ws.sort_variant)) * 256;
   k_bounds<<<kBoundsBlocks, 256, 0, st>>>(m, n, vec4, ws.scratch, Lz);
   rec(evs, 1, st);
   const uint32_t work = vec4 ? div_up(n, 4) : n;
@@ -641,7 +620,7 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   rec(evs, 2, st);
   // 4 passes sort the 32-bit keys: the whole 30-bit code, or the high 32 bits of a 60/63-bit
   // code; then each run of equal high halves is ordered by its low bits.
-  cudaError_t e = run_sort<uint32_t>(ws, n, 4, st, L, final_buf, 0);
+  cudaError_t e = run_sort(ws, n, 4, st, L, final_buf);
   if (e == cudaSuccess && sizeof(K) == 8) {
     const int fb = *final_buf;
     // the long-run list lives in the delta bytes, which emission has not written yet
@@ -669,7 +648,7 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
   const uint32_t* epoch = ws.scratch + L.epoch;
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer, 8 B per position
-  if (BITS == 30) k_delta<uint32_t, false><<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], nullptr, ws.delta, n);
+  if (BITS == 30) k_delta<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], ws.delta, n);
   else
     k_delta_split<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], split_lows(ws), BITS - 32, ws.delta, n);
   k_emit<SegSingle, PARENTS, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
@@ -678,14 +657,9 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
       ws.delta, ws.nodes, ws.slots, epoch, n, SegSingle{n}, frontier, fcount);
 }
 
-cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
-                         int* final_buf, int shift0) {
-  return run_sort<unsigned long long>(ws, n, passes, st, L, final_buf, shift0);
-}
-
 cudaError_t run_sort_u32(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
                          int* final_buf) {
-  return run_sort<uint32_t>(ws, n, passes, st, L, final_buf, 0);
+  return run_sort(ws, n, passes, st, L, final_buf);
 }
 
 cudaError_t lbvh_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int bits, int treelet_rounds, cudaStream_t st,

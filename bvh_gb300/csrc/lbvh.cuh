@@ -15,7 +15,7 @@ struct MeshPtrs {
 // Device workspace owned by a context; grown on demand, reused across builds.
 struct Workspace {
   uint32_t cap_n = 0;        // triangles the buffers can hold
-  int sort_variant[2] = {0, 0};  // onesweep variant for 32-bit / 64-bit keys (bvh_autotune)
+  int sort_variant = 0;      // onesweep variant (bvh_autotune)
   void* keys[2] = {nullptr, nullptr};
   uint32_t* vals[2] = {nullptr, nullptr};
   Box* boxes = nullptr;      // per-triangle AABB in input order
@@ -75,17 +75,17 @@ struct ScratchLayout {
 
 constexpr int kBoundsBlocks = 152 * 4;
 constexpr int kSortThreads = 256;
-constexpr int kMaxPasses = 8;
+constexpr int kMaxPasses = 4;  // 8-bit passes over 32-bit keys
 constexpr int kFrontierCounter = 15;  // counters[15]: emission frontier length (passes use 0..7)
 constexpr int kLongRunCounter = 14;   // counters[14]: runs listed for the block-wide fix-up
 
 ScratchLayout scratch_layout(uint32_t n);
-int sort_tile(int key_bytes);  // smallest tile over all variants (sizes the look-back scratch)
+int sort_tile();  // smallest tile over all variants (sizes the look-back scratch)
 int sort_variant_count();
-int sort_variant_tile(int key_bytes, int v);
-void sort_variant_describe(int key_bytes, int v, int* ipt, int* window, int* minb);
-// Times every onesweep variant on `n` pseudo-random keys of each width and keeps the fastest in ws.
-cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out /* 2 x variants */);
+int sort_variant_tile(int v);
+void sort_variant_describe(int v, int* ipt, int* window, int* minb);
+// Times every onesweep variant on `n` pseudo-random 32-bit keys and keeps the fastest in ws.
+cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out /* per variant */);
 
 // Builds stage events: [0] start, [1] bounds, [2] morton, [3] sort, [4] emit, [5] optimise.
 struct StageEvents {
@@ -128,15 +128,10 @@ struct EvalResult {
 size_t evaluate_scratch_bytes(uint32_t n_nodes);
 cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cudaStream_t st, EvalResult* out);
 
-// Completes a sort of 64-bit keys whose radix passes covered only bits lbits..lbits+31: orders
-// every run of equal key >> lbits by (key low bits, position), in place; tkeys/tvals (the other
-// ping-pong buffers) are scratch for runs longer than a few items, whose starts are listed in
-// long_list (room for n / 6 words) behind the zeroed counter long_count.
-cudaError_t sort_fix_runs(unsigned long long* keys, uint32_t* vals, unsigned long long* tkeys, uint32_t* tvals,
-                          uint32_t n, int lbits, uint32_t* long_list, uint32_t* long_count, cudaStream_t st);
-
-// The same for codes held split: hkeys = code >> lbits (sorted by the passes), lows = the low
-// bits by original index.  Only the values move.  scratch_a/scratch_b (8 B per position) and
+// Completes a sort of codes held split: hkeys = code >> lbits (sorted by the radix passes),
+// lows = the low lbits bits by original index.  Orders every run of equal hkeys by (low bits,
+// position), moving only the values; run starts that need the block-wide path are listed in
+// long_list (room for n / 6 words) behind the zeroed counter long_count.  scratch_a/scratch_b (8 B per position) and
 // tvals serve the block-wide sort of runs longer than 1024.
 cudaError_t sort_fix_runs_split(const uint32_t* hkeys, uint32_t* vals, const uint32_t* lows, uint32_t n, int lbits,
                                 unsigned long long* scratch_a, unsigned long long* scratch_b, uint32_t* tvals,
@@ -149,11 +144,8 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
 // Treelet control words (scratch + L.hist + kTlCtlWord): [0] too high, [1] tree height.
 constexpr size_t kTlCtlWord = 256 + 264 + 256;
 
-// Stable sort of ws.keys[0] (64-bit) with implicit indices over `passes` 8-bit digits.
-// `passes` stable 8-bit LSD passes over 64-bit keys, starting at bit shift0.
-cudaError_t run_sort_u64(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
-                         int* final_buf, int shift0 = 0);
-// The same over 32-bit keys (the whole key; passes * 8 bits of it).
+// Stable sort of the 32-bit keys in ws.keys[0] with implicit indices over `passes` 8-bit digits;
+// *final_buf = the ping-pong buffer holding the result.
 cudaError_t run_sort_u32(Workspace& ws, uint32_t n, int passes, cudaStream_t st, const ScratchLayout& L,
                          int* final_buf);
 

@@ -25,8 +25,8 @@ constexpr size_t kValsBytes = align256((size_t)kStaticMaxTris * 4);
 constexpr size_t kBoxBytes = align256((size_t)kStaticMaxTris * sizeof(Box));
 constexpr size_t kSlotBytes = align256((size_t)kStaticMaxTris * 8);
 constexpr size_t kDeltaBytes = align256((size_t)kStaticMaxTris + 16);
-// scratch words: fixed part + look-back descriptors for the smallest sort tile (6 x 256 keys)
-constexpr size_t kDescWords = (size_t)kMaxPasses * ((kStaticMaxTris + 1535) / 1536) * 256;
+// scratch words: fixed part + look-back descriptors for the smallest sort tile (8 x 256 keys)
+constexpr size_t kDescWords = (size_t)kMaxPasses * ((kStaticMaxTris + 2047) / 2048) * 256;
 constexpr size_t kScratchBytes = align256((8 + 16 + 8 + 16 + (size_t)kBoundsBlocks * 8 + 16 + kMaxPasses * 256 +
                                            kDescWords + 64) * 4);
 constexpr size_t kStaticBytes = 2 * kKeysBytes + kValsBytes + kBoxBytes + kSlotBytes + kDeltaBytes + kScratchBytes;

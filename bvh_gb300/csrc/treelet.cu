@@ -776,6 +776,7 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   uint32_t* cursor = off + 264;              // 256
   uint32_t* ctl = cursor + 256;              // [0] too high, [1] largest height, [2] current height
   static_assert(kTlCtlWord == 256 + 264 + 256, "control words of the treelet pass");
+  static_assert(kTlCtlWord + 3 <= (size_t)kMaxPasses * 256, "treelet words fit the histogram area");
   const uint32_t* epoch = ws.scratch + L.epoch;
   const uint32_t grow_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(stride, kGrowThreads), sms * 16));
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;

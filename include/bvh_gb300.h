@@ -188,12 +188,13 @@ bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_par
                              bvh_tree* out);
 
 /* Autotuner (no reference counterpart): times every radix-sort variant (items per thread,
- * look-back window, blocks per SM) on n pseudo-random keys of each width, keeps the fastest in
- * the context and writes a JSON table of the timings to json_out (may be NULL).  Synchronous. */
+ * look-back window, blocks per SM) on n pseudo-random 32-bit keys (every build sorts 32-bit keys:
+ * 30-bit codes whole, the high halves of longer codes), keeps the fastest in the context and
+ * writes a JSON table of the timings to json_out (may be NULL).  Synchronous. */
 bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char* json_out, size_t json_cap);
-/* Read or set the sort variants a context uses (index per key width: 32-bit, 64-bit). */
-bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant32, int32_t* variant64);
-bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant32, int32_t variant64);
+/* Read or set the sort variant a context uses (0 .. 3). */
+bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant);
+bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
 
 /* LBVH build that allocates nothing (no counterpart in the reference).  For callers that cannot
  * call cudaMalloc -- a host that forbids device allocations after start-up, a real-time loop

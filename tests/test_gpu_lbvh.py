@@ -144,22 +144,21 @@ def test_lbvh63_full_size_c1_bit_exact(ctx, gpu, oracle_lib):
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_every_sort_variant_bit_exact(ctx, gpu, oracle_lib, variant):
     O = oracle_lib
-    ctx.set_tuning(variant, variant)
+    ctx.set_tuning(variant)
     try:
         for bits, m in ((30, meshgen.uniform_small(70_001, seed=3)), (63, meshgen.clustered(90_007, seed=4))):
             nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=bits))
             onodes, oidx, _ = O.lbvh(m.arrays(), bits)
             assert np.array_equal(idx, oidx) and O.node_fields_equal(nodes, onodes)
     finally:
-        ctx.set_tuning(0, 0)
+        ctx.set_tuning(0)
 
 
 def test_autotune_table(ctx, gpu, oracle_lib):
     table = ctx.autotune(1 << 20)
-    for w in ("keys32", "keys64"):
-        assert 0 <= table["sort"][w]["chosen"] < 4
-        assert all(v["ms"] > 0 for v in table["sort"][w]["variants"])
-    assert ctx.tuning() == (table["sort"]["keys32"]["chosen"], table["sort"]["keys64"]["chosen"])
+    assert 0 <= table["sort"]["chosen"] < 4
+    assert len(table["sort"]["variants"]) == 4 and all(v["ms"] > 0 for v in table["sort"]["variants"])
+    assert ctx.tuning() == table["sort"]["chosen"]
     m = meshgen.clustered(50_000, seed=8)
     nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=63))
     onodes, oidx, _ = oracle_lib.lbvh(m.arrays(), 63)
