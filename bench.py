@@ -87,10 +87,13 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
         return 36.0
     if stage == "morton_boxes_hist":
         return 36.0 + kb + 4 + 32.0
+    # 60/63-bit codes: the run fix-up at the end of the sort stage also writes the delta bytes, so
+    # the delta's key read and byte write (kb + 1) move from the emission stage to the sort stage
+    delta = kb + 1 if bits != 30 and algo != "ploc" else 0
     if stage == "onesweep_sort":
-        return kb + 2.0 * d * (kb + 4)
+        return kb + 2.0 * d * (kb + 4) + delta
     if stage == "emit_refit":  # PLOC: leaf nodes + cluster init in this slot
-        return 116.0 if algo == "ploc" else kb + 4 + 36 + 48 + 12 + 48 + 4 + 48
+        return 116.0 if algo == "ploc" else kb + 4 + 36 + 48 + 12 + 48 + 4 + 48 - delta
     if algo == "ploc":
         return 160.0 * cluster_sum_per_tri
     return 144.0 * rounds
@@ -98,14 +101,15 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
 
 def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0, tree_height: int = 0) -> int:
     """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
-    fix-up of 60/63-bit codes (short runs, listed long runs), delta + emission + frontier climb;
+    fix-up of 60/63-bit codes (short runs, listed long runs; it writes the delta bytes too) or the
+    delta pass of 30-bit codes, emission + frontier climb;
     per treelet pass five (heights, counts, offsets, grouping by height, the fallback check) plus
     growth, DP and loop control per tree level; PLOC adds cluster init, 4 per clustering iteration
     (neighbours, tile counts + scan, merge + compaction, loop control) and the root fix (its
     30-bit prefix stops after the sort)."""
     if algo == "ploc":
         return 2 + 4 + 1 + 4 * ploc_iterations + 1
-    n = 2 + 4 + (2 if bits != 30 else 0) + 3
+    n = 2 + 4 + (2 + 2 if bits != 30 else 3)
     return n + (rounds * (5 + 3 * tree_height) if algo == "lbvh_plus" else 0)
 
 
@@ -125,7 +129,7 @@ STAGE_KERNELS = {
     "scene_bounds": "k_bounds",
     "morton_boxes_hist": "k_morton",
     "onesweep_sort": "k_onesweep x4 (+ k_fixrun_split_short/_long for 60/63-bit codes)",
-    "emit_refit": "k_delta (k_delta_split for 60/63-bit codes) + k_emit + k_emit_climb",
+    "emit_refit": "k_delta (30-bit codes; the run fix-up writes them for 60/63-bit codes) + k_emit + k_emit_climb",
     "treelet_or_ploc_loop": "LBVH+: k_tl_heights, k_tl_count, k_tl_offsets, k_tl_scatter, then k_tl_grow +"
                             " k_tl_dp per tree height; PLOC: k_ploc_nn, k_ploc_count, k_ploc_scatter, k_ploc_step"
                             " per iteration + k_ploc_root",
@@ -136,8 +140,8 @@ STAGE_KERNELS = {
 # the stage's traffic grows with the triangle count, so a launch over n triangles moves about
 # n times this.  Keyed by (algorithm, Morton bits, stage).
 MEASURED_TRAFFIC_PER_TRI = {
-    ("lbvh", 63, "emit_refit"): (201.1, "profiles/emit_fixrun_c1_4m.md: k_delta_split + k_emit + k_emit_climb at "
-                                        "4M, 804 MB / 4M triangles, scaled by the triangle count"),
+    ("lbvh", 63, "emit_refit"): (191.6, "profiles/emit_fixrun_c1_4m.md: k_emit + k_emit_climb at 4M, "
+                                        "766 MB / 4M triangles, scaled by the triangle count"),
 }
 
 

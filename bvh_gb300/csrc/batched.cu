@@ -179,7 +179,7 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
       (e = sort_fix_runs_split(hkeys, ws.vals[fb], lows, n, shift0,
                                reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), run_scratch, ws.vals[fb ^ 1],
                                reinterpret_cast<uint32_t*>(ws.delta), ws.scratch + L.counters + kLongRunCounter,
-                               st)) != cudaSuccess)
+                               nullptr, st)) != cudaSuccess)
     return e;
   if (evs && evs->use) cudaEventRecord(evs->ev[3], st);
   k_delta_seg_split<<<div_up(n, 256), 256, 0, st>>>(hkeys, ws.vals[fb], lows, d_offsets, shift0, ws.delta, n);

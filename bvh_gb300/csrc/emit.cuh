@@ -3,9 +3,10 @@
 // Reference: kBuildInternalNodes_nt (src/cuda/lbvh_builder.cu:183-229), kInitLeafNodes_nt
 // (:231-241) and kRefitHierarchy_nt (:243-274); same node ids, children and boxes.
 //
-// Step 1 (k_delta): D[k] = delta(k, k+1) + 1 for adjacent sorted positions, one byte each
-// (delta_nt, lbvh_builder.cu:33-43: common-prefix length of the codes, or 32/64 +
-// clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0 marks a segment boundary).
+// Step 1 (k_delta; for 60/63-bit codes the run fix-up writes them): D[k] = delta(k, k+1) + 1 for
+// adjacent sorted positions, one byte each (delta_nt, lbvh_builder.cu:33-43: common-prefix
+// length of the codes, or 32/64 + clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0
+// marks a segment boundary).
 // Step 2 (k_emit): one thread per sorted position climbs; merges whose two children belong to
 // threads of one block happen in shared memory.  Nodes whose sibling is built by another block,
 // and nodes still climbing after kEmitMaxSteps levels, are listed as a frontier, from which
@@ -88,26 +89,6 @@ static __global__ void __launch_bounds__(256) k_delta(const uint32_t* __restrict
   if (k + 1 >= n) return;
   const uint32_t a = __ldg(keys + k), b = __ldg(keys + k + 1);
   const int d = a == b ? 32 + __clz(__ldg(vals + k) ^ __ldg(vals + k + 1)) : __clz(a ^ b);
-  D[k] = (uint8_t)(d + 1);
-}
-
-// delta(k, k+1) + 1 of 60/63-bit codes held split: hk = code >> lbits (sorted), lows = the low
-// lbits bits by original index.  The same values as k_delta on the whole codes (clz of the
-// 64-bit XOR, or 64 + clz of the 64-bit XOR of the indices for equal codes).
-static __global__ void __launch_bounds__(256)
-    k_delta_split(const uint32_t* __restrict__ hk, const uint32_t* __restrict__ vals,
-                  const uint32_t* __restrict__ lows, int lbits, uint8_t* __restrict__ D, uint32_t n) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k + 1 >= n) return;
-  const uint32_t a = __ldg(hk + k), b = __ldg(hk + k + 1);
-  int d;
-  if (a != b) {
-    d = __clz(a ^ b) + 32 - lbits;
-  } else {
-    const uint32_t va = __ldg(vals + k), vb = __ldg(vals + k + 1);
-    const uint32_t la = __ldg(lows + va), lb = __ldg(lows + vb);
-    d = la != lb ? 32 + __clz(la ^ lb) : 96 + __clz(va ^ vb);
-  }
   D[k] = (uint8_t)(d + 1);
 }
 

@@ -129,11 +129,24 @@ __device__ __forceinline__ uint32_t window_rank(const unsigned long long (&w)[8]
   return r;
 }
 
-// H = hkeys[position] (sorted), L = lows[original index]; only the values of a run move.
+// delta(k, k+1) + 1 of codes held split (the value of the delta pass on whole 64-bit codes:
+// clz of their XOR, or 64 + clz of the 64-bit XOR of the indices for equal codes): neighbours
+// whose high halves differ, and neighbours inside a run (equal high halves).
+__device__ __forceinline__ uint8_t delta_hi(uint32_t a, uint32_t b, int lbits) {
+  return (uint8_t)(__clz(a ^ b) + 32 - lbits + 1);
+}
+__device__ __forceinline__ uint8_t delta_lo(uint32_t la, uint32_t lb, uint32_t va, uint32_t vb) {
+  return (uint8_t)((la != lb ? 32 + __clz(la ^ lb) : 96 + __clz(va ^ vb)) + 1);
+}
+
+// H = hkeys[position] (sorted), L = lows[original index]; only the values of a run move.  With
+// DELTA the kernel also writes D[k] = delta(k, k+1) + 1 (of the final order) for every k whose
+// high half differs from the next one's, and for the inner positions of the runs it orders.
+template <bool DELTA>
 __global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __restrict__ hkeys,
                                                             uint32_t* __restrict__ vals,
-                                                            const uint32_t* __restrict__ lows, uint32_t n,
-                                                            uint32_t* __restrict__ long_list,
+                                                            const uint32_t* __restrict__ lows, uint32_t n, int lbits,
+                                                            uint8_t* __restrict__ D, uint32_t* __restrict__ long_list,
                                                             uint32_t* __restrict__ long_count) {
   constexpr unsigned long long kNoH = ~0ull;
   const uint32_t lane = threadIdx.x & 31;
@@ -172,6 +185,11 @@ __global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __re
   }
   unsigned long long hprev = __shfl_up_sync(0xffffffffu, hw[3], 1);
   if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? (unsigned long long)hkeys[p0 - 1] : kNoH;
+  if (DELTA) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (p0 + j + 1 < n && hw[j] != hw[j + 1]) D[p0 + j] = delta_hi((uint32_t)hw[j], (uint32_t)hw[j + 1], lbits);
+  }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const unsigned long long hp = j == 0 ? hprev : hw[j - 1];
@@ -185,10 +203,12 @@ __global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __re
       continue;
     }
     if (m == 2) {  // the common case: swap when out of order
-      if (__ldg(lows + v[j]) > __ldg(lows + v[j + 1])) {
+      const uint32_t la = __ldg(lows + v[j]), lb = __ldg(lows + v[j + 1]);
+      if (la > lb) {
         vals[s] = v[j + 1];
         vals[s + 1] = v[j];
       }
+      if (DELTA) D[s] = delta_lo(la, lb, v[j], v[j + 1]);
       continue;
     }
     unsigned long long w[8];  // L in the window slots of the run (positions order the ties)
@@ -201,20 +221,40 @@ __global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __re
 #pragma unroll
     for (int i = 0; i < 8; ++i)
       if (i >= j && i < j + m && rk[i] != (uint32_t)i) vals[p0 + rk[i]] = v[i];
+    if (DELTA) {
+      // inner positions: item i lands at p0 + rk[i]; its successor is the item ranked next
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (i >= j && i < j + m && rk[i] + 1 < (uint32_t)(j + m)) {
+          uint32_t ls = 0, vs = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if (q >= j && q < j + m && rk[q] == rk[i] + 1) {
+              ls = (uint32_t)w[q];
+              vs = v[q];
+            }
+          }
+          D[p0 + rk[i]] = delta_lo((uint32_t)w[i], ls, v[i], vs);
+        }
+      }
+    }
   }
 }
 
 // One block per listed run of split codes: find its end; up to kRankMax items are ranked by
 // counting, longer runs are sorted block-wide with their low bits staged in scratch_a.
+template <bool DELTA>
 __global__ void __launch_bounds__(kFixThreads) k_fixrun_split_long(const uint32_t* __restrict__ hkeys,
                                                                uint32_t* __restrict__ vals,
                                                                const uint32_t* __restrict__ lows, uint32_t n,
                                                                int lbits, unsigned long long* __restrict__ scratch_a,
                                                                unsigned long long* __restrict__ scratch_b,
-                                                               uint32_t* __restrict__ tvals,
+                                                               uint32_t* __restrict__ tvals, uint8_t* __restrict__ D,
                                                                const uint32_t* __restrict__ long_list,
                                                                const uint32_t* __restrict__ long_count) {
-  __shared__ uint32_t s_wh[8 * 256];
+  static_assert(kRankMax <= 1024, "sorted low bits share s_wh with the unsorted ones");
+  __shared__ uint32_t s_wh[8 * 256];  // [0, kRankMax): L in run order; [1024, 1024 + kRankMax): L by rank
+  __shared__ uint32_t s_sv[kRankMax];  // values by rank
   __shared__ uint32_t s_off[256];
   __shared__ uint32_t s_w[8];
   __shared__ uint32_t s_e;
@@ -256,11 +296,26 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun_split_long(const uint32_
 #pragma unroll
       for (int r = 0; r < kRankMax / kFixThreads; ++r) {
         const uint32_t q = t + (uint32_t)r * kFixThreads;
-        if (q < m && rq[r] != q) vals[s + rq[r]] = vq[r];
+        if (q < m) {
+          if (rq[r] != q) vals[s + rq[r]] = vq[r];
+          if (DELTA) {
+            s_wh[1024 + rq[r]] = s_wh[q];
+            s_sv[rq[r]] = vq[r];
+          }
+        }
+      }
+      if (DELTA) {
+        __syncthreads();
+        for (uint32_t q = t; q + 1 < m; q += kFixThreads)
+          D[s + q] = delta_lo(s_wh[1024 + q], s_wh[1024 + q + 1], s_sv[q], s_sv[q + 1]);
       }
     } else {
       for (uint32_t q = t; q < m; q += kFixThreads) scratch_a[s + q] = __ldg(lows + vals[s + q]);
       block_sort_run(scratch_a, vals, scratch_b, tvals, s, m, lbits, s_wh, s_off, s_w);
+      if (DELTA) {
+        for (uint32_t q = t; q + 1 < m; q += kFixThreads)
+          D[s + q] = delta_lo((uint32_t)scratch_a[s + q], (uint32_t)scratch_a[s + q + 1], vals[s + q], vals[s + q + 1]);
+      }
     }
     __syncthreads();
   }
@@ -270,11 +325,18 @@ __global__ void __launch_bounds__(kFixThreads) k_fixrun_split_long(const uint32_
 
 cudaError_t sort_fix_runs_split(const uint32_t* hkeys, uint32_t* vals, const uint32_t* lows, uint32_t n, int lbits,
                                 unsigned long long* scratch_a, unsigned long long* scratch_b, uint32_t* tvals,
-                                uint32_t* long_list, uint32_t* long_count, cudaStream_t st) {
+                                uint32_t* long_list, uint32_t* long_count, uint8_t* D, cudaStream_t st) {
   if (n < 2) return cudaSuccess;
-  k_fixrun_split_short<<<div_up(div_up(n, 4u), 256u), 256, 0, st>>>(hkeys, vals, lows, n, long_list, long_count);
-  k_fixrun_split_long<<<152, kFixThreads, 0, st>>>(hkeys, vals, lows, n, lbits, scratch_a, scratch_b, tvals,
-                                                   long_list, long_count);
+  const uint32_t grid = div_up(div_up(n, 4u), 256u);
+  if (D) {
+    k_fixrun_split_short<true><<<grid, 256, 0, st>>>(hkeys, vals, lows, n, lbits, D, long_list, long_count);
+    k_fixrun_split_long<true><<<152, kFixThreads, 0, st>>>(hkeys, vals, lows, n, lbits, scratch_a, scratch_b, tvals,
+                                                           D, long_list, long_count);
+  } else {
+    k_fixrun_split_short<false><<<grid, 256, 0, st>>>(hkeys, vals, lows, n, lbits, D, long_list, long_count);
+    k_fixrun_split_long<false><<<152, kFixThreads, 0, st>>>(hkeys, vals, lows, n, lbits, scratch_a, scratch_b, tvals,
+                                                            D, long_list, long_count);
+  }
   return cudaGetLastError();
 }
 

@@ -593,13 +593,17 @@ static inline void rec(StageEvents* evs, int k, cudaStream_t st) {
   if (evs && evs->use) cudaEventRecord(evs->ev[k], st);
 }
 
-// Split codes keep their low bits in the node buffer, which emission writes only after the delta
-// pass: [lows by original index: 4n B][64-bit run scratch: 8n B], 16-byte aligned; at most
-// 12n + 16 bytes of the 96n - 48 the nodes take.
+// Split codes keep their low bits in the node buffer, which emission writes only after the run
+// fix-up: [lows by original index: 4n B][64-bit run scratch: 8n B][long-run list: n/6 words],
+// 16-byte aligned; at most 13n + 48 bytes of the 96n - 48 the nodes take.
+static inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 static inline uint32_t* split_lows(const Workspace& ws) { return reinterpret_cast<uint32_t*>(ws.nodes); }
 static inline unsigned long long* split_run_scratch(const Workspace& ws, uint32_t n) {
-  return reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(ws.nodes) +
-                                               (((size_t)n * 4 + 15) & ~(size_t)15));
+  return reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(ws.nodes) + align16((size_t)n * 4));
+}
+static inline uint32_t* split_long_list(const Workspace& ws, uint32_t n) {
+  return reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(ws.nodes) + align16((size_t)n * 4) +
+                                     align16((size_t)n * 8));
 }
 
 template <int BITS, typename K>
@@ -623,11 +627,11 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   cudaError_t e = run_sort(ws, n, 4, st, L, final_buf);
   if (e == cudaSuccess && sizeof(K) == 8) {
     const int fb = *final_buf;
-    // the long-run list lives in the delta bytes, which emission has not written yet
+    // the fix-up also writes the delta bytes of the final order
     e = sort_fix_runs_split(reinterpret_cast<const uint32_t*>(ws.keys[fb]), ws.vals[fb], lows, n, BITS - 32,
                             reinterpret_cast<unsigned long long*>(ws.keys[fb ^ 1]), split_run_scratch(ws, n),
-                            ws.vals[fb ^ 1], reinterpret_cast<uint32_t*>(ws.delta),
-                            ws.scratch + L.counters + kLongRunCounter, st);
+                            ws.vals[fb ^ 1], split_long_list(ws, n), ws.scratch + L.counters + kLongRunCounter,
+                            ws.delta, st);
   }
   rec(evs, 3, st);
   return e;
@@ -648,9 +652,7 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
   const uint32_t* epoch = ws.scratch + L.epoch;
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer, 8 B per position
-  if (BITS == 30) k_delta<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], ws.delta, n);
-  else
-    k_delta_split<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], split_lows(ws), BITS - 32, ws.delta, n);
+  if (BITS == 30) k_delta<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], ws.delta, n);  // 60/63: by the fix-up
   k_emit<SegSingle, PARENTS, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
       ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, SegSingle{n}, nullptr, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegSingle, PARENTS><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(

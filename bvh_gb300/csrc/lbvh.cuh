@@ -133,9 +133,12 @@ cudaError_t evaluate_tree(const Node* nodes, uint32_t n_nodes, void* scratch, cu
 // position), moving only the values; run starts that need the block-wide path are listed in
 // long_list (room for n / 6 words) behind the zeroed counter long_count.  scratch_a/scratch_b (8 B per position) and
 // tvals serve the block-wide sort of runs longer than 1024.
+// With D non-null it also writes the delta bytes D[k] = delta(k, k+1) + 1 of the final order
+// (60/63-bit codes: clz of the 64-bit code XOR, 64 + clz of the index XOR for equal codes), so
+// no separate delta pass is needed; long_list must then lie outside D.
 cudaError_t sort_fix_runs_split(const uint32_t* hkeys, uint32_t* vals, const uint32_t* lows, uint32_t n, int lbits,
                                 unsigned long long* scratch_a, unsigned long long* scratch_b, uint32_t* tvals,
-                                uint32_t* long_list, uint32_t* long_count, cudaStream_t st);
+                                uint32_t* long_list, uint32_t* long_count, uint8_t* D, cudaStream_t st);
 
 // Treelet restructuring passes (LBVH+) after emission; fb = the sort's final ping-pong buffer
 // (the other one is scratch).
