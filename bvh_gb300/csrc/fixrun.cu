@@ -143,7 +143,7 @@ __device__ __forceinline__ uint8_t delta_lo(uint32_t la, uint32_t lb, uint32_t v
 // DELTA the kernel also writes D[k] = delta(k, k+1) + 1 (of the final order) for every k whose
 // high half differs from the next one's, and for the inner positions of the runs it orders.
 template <bool DELTA>
-__global__ void __launch_bounds__(256) k_fixrun_split_short(const uint32_t* __restrict__ hkeys,
+__global__ void __launch_bounds__(256, 4) k_fixrun_split_short(const uint32_t* __restrict__ hkeys,
                                                             uint32_t* __restrict__ vals,
                                                             const uint32_t* __restrict__ lows, uint32_t n, int lbits,
                                                             uint8_t* __restrict__ D, uint32_t* __restrict__ long_list,
