@@ -101,15 +101,15 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
 
 def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0, tree_height: int = 0) -> int:
     """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
-    fix-up of 60/63-bit codes (short runs, listed long runs; it writes the delta bytes too) or the
-    delta pass of 30-bit codes, emission + frontier climb;
+    fix-up of 60/63-bit codes (short runs, listed long runs; it writes the delta bytes too),
+    emission (which computes the delta bytes of 30-bit codes) + frontier climb;
     per treelet pass five (heights, counts, offsets, grouping by height, the fallback check) plus
     growth, DP and loop control per tree level; PLOC adds cluster init, 4 per clustering iteration
     (neighbours, tile counts + scan, merge + compaction, loop control) and the root fix (its
     30-bit prefix stops after the sort)."""
     if algo == "ploc":
         return 2 + 4 + 1 + 4 * ploc_iterations + 1
-    n = 2 + 4 + (2 + 2 if bits != 30 else 3)
+    n = 2 + 4 + (2 if bits != 30 else 0) + 2
     return n + (rounds * (5 + 3 * tree_height) if algo == "lbvh_plus" else 0)
 
 
@@ -129,7 +129,7 @@ STAGE_KERNELS = {
     "scene_bounds": "k_bounds",
     "morton_boxes_hist": "k_morton",
     "onesweep_sort": "k_onesweep x4 (+ k_fixrun_split_short/_long for 60/63-bit codes)",
-    "emit_refit": "k_delta (30-bit codes; the run fix-up writes them for 60/63-bit codes) + k_emit + k_emit_climb",
+    "emit_refit": "k_emit (with the delta bytes of 30-bit codes) + k_emit_climb",
     "treelet_or_ploc_loop": "LBVH+: k_tl_heights, k_tl_count, k_tl_offsets, k_tl_scatter, then k_tl_grow +"
                             " k_tl_dp per tree height; PLOC: k_ploc_nn, k_ploc_count, k_ploc_scatter, k_ploc_step"
                             " per iteration + k_ploc_root",

@@ -187,7 +187,7 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer
   const SegBatch seg{hkeys, d_offsets, 30 - shift0};
   k_emit<SegBatch, false, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
-      ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, seg, d_indices, frontier, fcount, kEmitMaxSteps);
+      ws.delta, nullptr, ws.vals[fb], ws.boxes, ws.nodes, n, seg, d_indices, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegBatch, false><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
       ws.delta, ws.nodes, ws.slots, ws.scratch + L.epoch, n, seg, frontier, fcount);
   if (evs && evs->use) {

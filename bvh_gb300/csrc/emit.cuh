@@ -3,10 +3,11 @@
 // Reference: kBuildInternalNodes_nt (src/cuda/lbvh_builder.cu:183-229), kInitLeafNodes_nt
 // (:231-241) and kRefitHierarchy_nt (:243-274); same node ids, children and boxes.
 //
-// Step 1 (k_delta; for 60/63-bit codes the run fix-up writes them): D[k] = delta(k, k+1) + 1 for
-// adjacent sorted positions, one byte each (delta_nt, lbvh_builder.cu:33-43: common-prefix
-// length of the codes, or 32/64 + clz(origIdx_k ^ origIdx_k+1) when the codes are equal; 0
-// marks a segment boundary).
+// Step 1: D[k] = delta(k, k+1) + 1 for adjacent sorted positions, one byte each (delta_nt,
+// lbvh_builder.cu:33-43: common-prefix length of the codes, or 32/64 + clz(origIdx_k ^
+// origIdx_k+1) when the codes are equal; 0 marks a segment boundary).  30-bit codes: k_emit
+// computes them for its tile; 60/63-bit codes: the run fix-up writes them; batched keys:
+// k_delta_seg_split.
 // Step 2 (k_emit): one thread per sorted position climbs; merges whose two children belong to
 // threads of one block happen in shared memory.  Nodes whose sibling is built by another block,
 // and nodes still climbing after kEmitMaxSteps levels, are listed as a frontier, from which
@@ -81,17 +82,6 @@ __device__ __forceinline__ unsigned long long atom_exch_acq_rel(unsigned long lo
   return old;
 }
 
-// delta(k, k+1) + 1 of 30-bit codes as a byte.
-static __global__ void __launch_bounds__(256) k_delta(const uint32_t* __restrict__ keys,
-                                                      const uint32_t* __restrict__ vals, uint8_t* __restrict__ D,
-                                                      uint32_t n) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k + 1 >= n) return;
-  const uint32_t a = __ldg(keys + k), b = __ldg(keys + k + 1);
-  const int d = a == b ? 32 + __clz(__ldg(vals + k) ^ __ldg(vals + k + 1)) : __clz(a ^ b);
-  D[k] = (uint8_t)(d + 1);
-}
-
 // Batched meshes: keys mesh << 30 | code30 held split as hk = key >> shift0 (sorted) and lows =
 // key & (2^shift0 - 1) by original index.  delta = -1 across meshes, the clz of the 30-bit code
 // XOR within a mesh, 32 + clz of the in-mesh indices' XOR for equal codes.
@@ -137,14 +127,19 @@ struct Climb {
 
 // T sorted positions per block, one thread each (a larger block leaves fewer nodes whose sibling
 // lies in another block to the frontier pass).
-template <typename Seg, bool PARENTS, uint32_t T = 256>
-__global__ void __launch_bounds__(T, 2048 / T) k_emit(const uint8_t* __restrict__ D, const uint32_t* __restrict__ vals,
+// KEYS30: the tile's delta bytes are computed here from the sorted 30-bit keys (the delta_nt
+// rule, as k_delta) and written to D for k_emit_climb; otherwise they are read from D.
+template <typename Seg, bool PARENTS, uint32_t T = 256, bool KEYS30 = false>
+__global__ void __launch_bounds__(T, 2048 / T) k_emit(uint8_t* __restrict__ D, const uint32_t* __restrict__ keys30,
+                                            const uint32_t* __restrict__ vals,
                                             const Box* __restrict__ tri_boxes, Node* __restrict__ nodes,
                                             uint32_t n, Seg seg, uint32_t* __restrict__ out_idx,
                                             uint2* __restrict__ frontier, uint32_t* __restrict__ frontier_count,
                                             uint32_t max_steps) {
   // D of positions bbase-1 .. bbase+T-1 (0 outside [0, n-1) : a segment boundary)
   __shared__ uint8_t s_D[T + 1];
+  // KEYS30: keys and values of positions bbase-1 .. bbase+T
+  __shared__ uint32_t s_k[KEYS30 ? T + 2 : 1], s_v[KEYS30 ? T + 2 : 1];
   // rendezvous slot k <-> split gamma = bbase + k: one side per child (0 left, 1 right); the
   // child's box with its id in lo.w and its far end (f of a left child, l of a right child) in hi.w
   __shared__ uint32_t s_flag[T];
@@ -171,8 +166,33 @@ __global__ void __launch_bounds__(T, 2048 / T) k_emit(const uint8_t* __restrict_
     c.my = (int32_t)(cnt - 1) + (int32_t)(i - off);
     store_node(nodes, nb + (uint32_t)c.my, c.box, (int32_t)(prim | kLeafBit), -1, -1);
     if (cnt == 1) active = false;  // a one-triangle mesh: the leaf is the root
+    if (KEYS30) {
+      s_k[tid + 1] = __ldg(keys30 + i);
+      s_v[tid + 1] = prim_g;
+    }
   }
-  {
+  if (KEYS30) {
+    if (tid == 0 && bbase > 0) {
+      s_k[0] = __ldg(keys30 + bbase - 1);
+      s_v[0] = __ldg(vals + bbase - 1);
+    }
+    if (tid == T - 1 && bbase + T < n) {
+      s_k[T + 1] = __ldg(keys30 + bbase + T);
+      s_v[T + 1] = __ldg(vals + bbase + T);
+    }
+    __syncthreads();
+    // s_D[k] = D[bbase - 1 + k]; position j and j + 1 sit at s_k[k], s_k[k + 1]
+    for (uint32_t k = tid; k <= T; k += T) {
+      const int64_t j = (int64_t)bbase - 1 + k;
+      uint8_t d = 0;
+      if (j >= 0 && j + 1 < (int64_t)n) {
+        const uint32_t a = s_k[k], b = s_k[k + 1];
+        d = (uint8_t)((a == b ? 32 + __clz(s_v[k] ^ s_v[k + 1]) : __clz(a ^ b)) + 1);
+        if (k >= 1) D[j] = d;  // the tile's own positions bbase .. bbase + T - 1
+      }
+      s_D[k] = d;
+    }
+  } else {
     const int64_t j = (int64_t)bbase - 1 + tid;
     s_D[tid] = (j >= 0 && j + 1 < (int64_t)n) ? __ldg(D + j) : (uint8_t)0;
     if (tid == 0) {

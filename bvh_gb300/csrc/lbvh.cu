@@ -652,9 +652,9 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
   const uint32_t* epoch = ws.scratch + L.epoch;
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer, 8 B per position
-  if (BITS == 30) k_delta<<<div_up(n, 256), 256, 0, st>>>(keys, ws.vals[fb], ws.delta, n);  // 60/63: by the fix-up
-  k_emit<SegSingle, PARENTS, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
-      ws.delta, ws.vals[fb], ws.boxes, ws.nodes, n, SegSingle{n}, nullptr, frontier, fcount, kEmitMaxSteps);
+  // delta bytes: computed by k_emit from the 30-bit keys, written by the run fix-up for 60/63 bits
+  k_emit<SegSingle, PARENTS, kEmitTile, BITS == 30><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
+      ws.delta, keys, ws.vals[fb], ws.boxes, ws.nodes, n, SegSingle{n}, nullptr, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegSingle, PARENTS><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
       ws.delta, ws.nodes, ws.slots, epoch, n, SegSingle{n}, frontier, fcount);
 }
