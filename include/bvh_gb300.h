@@ -192,7 +192,7 @@ bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_par
  * 30-bit codes whole, the high halves of longer codes), keeps the fastest in the context and
  * writes a JSON table of the timings to json_out (may be NULL).  Synchronous. */
 bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char* json_out, size_t json_cap);
-/* Read or set the sort variant a context uses (0 .. 3). */
+/* Read or set the sort variant a context uses (0 .. 4). */
 bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant);
 bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
 

@@ -141,7 +141,7 @@ def test_lbvh63_full_size_c1_bit_exact(ctx, gpu, oracle_lib):
     assert O.sah(nodes) == O.sah(onodes)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
 def test_every_sort_variant_bit_exact(ctx, gpu, oracle_lib, variant):
     O = oracle_lib
     ctx.set_tuning(variant)
@@ -156,8 +156,8 @@ def test_every_sort_variant_bit_exact(ctx, gpu, oracle_lib, variant):
 
 def test_autotune_table(ctx, gpu, oracle_lib):
     table = ctx.autotune(1 << 20)
-    assert 0 <= table["sort"]["chosen"] < 4
-    assert len(table["sort"]["variants"]) == 4 and all(v["ms"] > 0 for v in table["sort"]["variants"])
+    assert 0 <= table["sort"]["chosen"] < 5
+    assert len(table["sort"]["variants"]) == 5 and all(v["ms"] > 0 for v in table["sort"]["variants"])
     assert ctx.tuning() == table["sort"]["chosen"]
     m = meshgen.clustered(50_000, seed=8)
     nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=63))
