@@ -30,6 +30,7 @@ struct PlocBufs {
   Box* cbox[2];
   int32_t* cid[2];
   int32_t* nbr;
+  uint2* flags;  // per (tile, warp, round): the merge and survivor ballots of 32 clusters
   unsigned long long* desc;
   Node* nodes;
   uint32_t* ctrl;
@@ -294,8 +295,10 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
       int32_t j;
       bool m, v;
       item_flags(B.nbr, c, base + r * 32 + lane, j, m, v);
-      tm += __popc(__ballot_sync(0xffffffffu, m));
-      tv += __popc(__ballot_sync(0xffffffffu, v));
+      const uint32_t mb = __ballot_sync(0xffffffffu, m), vb = __ballot_sync(0xffffffffu, v);
+      if (lane == 0) B.flags[((size_t)tile * (kPlocThreads / 32) + w) * kPlocRounds + r] = make_uint2(mb, vb);
+      tm += __popc(mb);
+      tv += __popc(vb);
     }
     if (lane == 0) s_w[w] = ((unsigned long long)tm << 31) | tv;
     __syncthreads();
@@ -336,12 +339,14 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_scatter(PlocBufs B) {
     uint32_t mb[kPlocRounds], vb[kPlocRounds];
     int32_t nj[kPlocRounds];
     uint32_t tm = 0, tv = 0;
+    // the ballots k_ploc_count stored; the partner of each merging cluster
+    const uint2* fl = B.flags + ((size_t)tile * (kPlocThreads / 32) + w) * kPlocRounds;
 #pragma unroll
     for (int r = 0; r < kPlocRounds; ++r) {
-      bool m, v;
-      item_flags(B.nbr, c, base + r * 32 + lane, nj[r], m, v);
-      mb[r] = __ballot_sync(0xffffffffu, m);
-      vb[r] = __ballot_sync(0xffffffffu, v);
+      const uint2 f = __ldcg(fl + r);
+      mb[r] = f.x;
+      vb[r] = f.y;
+      nj[r] = ((f.x >> lane) & 1u) ? __ldcg(B.nbr + base + r * 32 + lane) : -1;
       tm += __popc(mb[r]);
       tv += __popc(vb[r]);
     }
@@ -437,8 +442,10 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   if ((e = cudaMalloc(&ws.cid[0], (size_t)cap * 4)) != cudaSuccess) return e;
   if ((e = cudaMalloc(&ws.cid[1], (size_t)cap * 4)) != cudaSuccess) return e;
   // neighbours (cap) + per-tile merge totals / prefixes (64-bit) share one allocation
+  // ... and the per-round ballots (8 B per 32 clusters)
   size_t desc_words = div_up(cap, kPlocTile) + 8;
-  if ((e = cudaMalloc(&ws.nbr, (size_t)cap * 4 + desc_words * 8 + 64)) != cudaSuccess) return e;
+  size_t flag_words = (size_t)div_up(cap, kPlocTile) * (kPlocThreads / 32) * kPlocRounds;
+  if ((e = cudaMalloc(&ws.nbr, (size_t)cap * 4 + desc_words * 8 + flag_words * 8 + 64)) != cudaSuccess) return e;
   ws.ploc_cap = cap;
   return cudaSuccess;
 }
@@ -499,6 +506,7 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   B.nbr = ws.nbr;
   B.desc = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(ws.nbr) +
                                                   (((size_t)ws.ploc_cap * 4 + 15) & ~size_t(15)));
+  B.flags = reinterpret_cast<uint2*>(B.desc + div_up(ws.ploc_cap, kPlocTile) + 8);
   B.nodes = ws.nodes;
   B.ctrl = ws.scratch + L.ploc;
   B.status = ws.scratch + L.status;
