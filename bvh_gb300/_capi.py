@@ -125,6 +125,10 @@ SIGNATURES = {
                                   POINTER(Hits), c_void_p]),
     "bvh_pinhole_rays": (c_int, [POINTER(Camera), c_int32, c_int32] + [c_void_p] * 6 + [c_void_p]),
     "bvh_auto_camera": (c_int, [c_void_p, POINTER(Camera)]),
+    "bvh_shade": (c_int, [c_void_p, POINTER(MeshSoA), POINTER(Camera), c_int32, c_int32, POINTER(Hits), c_int32,
+                          ctypes.c_float, c_void_p, c_void_p, c_void_p]),
+    "bvh_heatmap": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p, ctypes.c_float, c_void_p, c_void_p, c_void_p]),
+    "bvh_rgb8": (c_int, [c_void_p, c_uint32, c_void_p, c_void_p]),
     "bvh_build_batched": (c_int, [c_void_p, POINTER(Batch), POINTER(Params), c_void_p, POINTER(Tree)]),
     "bvh_autotune": (c_int, [c_void_p, c_uint32, c_void_p, c_char_p, ctypes.c_size_t]),
     "bvh_tuning_get": (c_int, [c_void_p, POINTER(c_int32)]),

@@ -199,6 +199,29 @@ class Context:
                                            ctypes.byref(cam), width, height, ctypes.byref(h),
                                            ctypes.c_void_p(stream)), "bvh_trace_pinhole")
 
+    def shade(self, mesh_ptrs: Sequence[int], n_tris: int, cam: C.Camera, width: int, height: int,
+              hit_ptrs: Sequence[int], mode: int, scene_diag: float, light_dir, rgb_ptr: int, stream: int = 0):
+        """kRenderKernel's shading of a trace_pinhole result into device float RGB (bvh_shade);
+        mode 0 normal, 1 depth, 2 diffuse, 3 node visits."""
+        m = C.mesh_struct(mesh_ptrs, n_tris)
+        h = C.Hits(*hit_ptrs)
+        light = (ctypes.c_float * 3)(*[float(x) for x in light_dir])
+        C.check(self.lib.bvh_shade(self.handle, ctypes.byref(m), ctypes.byref(cam), width, height, ctypes.byref(h),
+                                   int(mode), ctypes.c_float(scene_diag), ctypes.cast(light, ctypes.c_void_p),
+                                   ctypes.c_void_p(rgb_ptr), ctypes.c_void_p(stream)), "bvh_shade")
+
+    def heatmap(self, visits_ptr: int, n_pixels: int, colormap_ptr: int, rgb_ptr: int, fixed_max: float = 0.0,
+                used_max_ptr: int = 0, stream: int = 0):
+        """applyHeatmapColormap on device node-visit counts with a device 256 x 3 colormap (bvh_heatmap)."""
+        C.check(self.lib.bvh_heatmap(self.handle, ctypes.c_void_p(visits_ptr), n_pixels, ctypes.c_void_p(colormap_ptr),
+                                     ctypes.c_float(fixed_max), ctypes.c_void_p(rgb_ptr),
+                                     ctypes.c_void_p(used_max_ptr or None), ctypes.c_void_p(stream)), "bvh_heatmap")
+
+    def rgb8(self, rgb_ptr: int, n_values: int, out_ptr: int, stream: int = 0):
+        """savePPM's float-to-byte conversion on the device (bvh_rgb8)."""
+        C.check(self.lib.bvh_rgb8(ctypes.c_void_p(rgb_ptr), n_values, ctypes.c_void_p(out_ptr),
+                                  ctypes.c_void_p(stream)), "bvh_rgb8")
+
 
 def load_obj(path: str, threads: int = 0) -> "TriangleMesh":
     """loadOBJ (src/loader.cpp:10-74) as a multi-threaded parse straight to SoA (bvh_load_obj)."""

@@ -27,6 +27,7 @@ struct bvh_ctx {
   cudaStream_t capture_stream = nullptr;  // for CUDA graph capture (never the legacy stream)
   void* eval_buf = nullptr;               // bvh_evaluate scratch
   size_t eval_bytes = 0;
+  void* heat_buf = nullptr;               // bvh_heatmap scratch (heatmap_scratch_bytes())
   StageEvents evs;
   bvh_timing last{};
   int last_algo = -1;
@@ -97,6 +98,7 @@ extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
   if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
   workspace_free(ctx->ws);
   cudaFree(ctx->eval_buf);
+  cudaFree(ctx->heat_buf);
   for (int k = 0; k < 8; ++k) cudaEventDestroy(ctx->evs.ev[k]);
   cudaFreeHost(ctx->h_status);
   delete ctx;
@@ -572,6 +574,37 @@ extern "C" bvh_status bvh_pinhole_rays(const bvh_camera* cam, int32_t width, int
   if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
   if (!ox || !oy || !oz || !dx || !dy || !dz) return BVH_ERR_INVALID_ARG;
   return from_cuda(pinhole_rays(b, ox, oy, oz, dx, dy, dz, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+extern "C" bvh_status bvh_shade(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_camera* cam, int32_t width,
+                                int32_t height, const bvh_hits* hits, int32_t mode, float scene_diag,
+                                const float* light_dir, float* rgb, void* stream) {
+  if (!ctx || !mesh_ok(mesh) || !hits || !hits->t || !hits->prim || !hits->nodes_visited || !rgb || !light_dir)
+    return BVH_ERR_INVALID_ARG;
+  PinholeBasis b;
+  if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  ShadeIn in{hits->t, hits->prim, hits->nodes_visited};
+  return from_cuda(shade_pixels(b, mesh_ptrs(mesh), mesh->n, in, mode, scene_diag,
+                                make_float3(light_dir[0], light_dir[1], light_dir[2]), rgb,
+                                reinterpret_cast<cudaStream_t>(stream)));
+}
+
+extern "C" bvh_status bvh_heatmap(bvh_ctx* ctx, const int32_t* nodes_visited, uint32_t n_pixels, const float* colormap,
+                                  float fixed_max, float* rgb, float* used_max, void* stream) {
+  if (!ctx || (n_pixels && (!nodes_visited || !colormap || !rgb))) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  if (!ctx->heat_buf) {
+    cudaError_t e = cudaMalloc(&ctx->heat_buf, heatmap_scratch_bytes());
+    if (e != cudaSuccess) return from_cuda(e);
+  }
+  return from_cuda(heatmap(nodes_visited, n_pixels, colormap, fixed_max, ctx->heat_buf, rgb, used_max,
+                           reinterpret_cast<cudaStream_t>(stream)));
+}
+
+extern "C" bvh_status bvh_rgb8(const float* rgb, uint32_t n_values, uint8_t* out, void* stream) {
+  if (n_values && (!rgb || !out)) return BVH_ERR_INVALID_ARG;
+  return from_cuda(rgb_to_bytes(rgb, n_values, out, reinterpret_cast<cudaStream_t>(stream)));
 }
 
 // autoCamera, src/render_engine.cu:601-637.

@@ -5,6 +5,8 @@
 // first, 128-entry stack that silently drops pushes when full), same counters (a node counts as
 // visited before its box test), same closest-hit rule (strict <).  Every float operation is an
 // explicitly rounded intrinsic so that the CPU oracle reproduces the results bit for bit.
+#include <algorithm>
+
 #include "lbvh.cuh"
 #include "trace.cuh"
 
@@ -133,6 +135,216 @@ __global__ void k_pinhole_rays(PinholeBasis cam, float* ox, float* oy, float* oz
   const float3 d = pinhole_dir(cam, (int)(r % (uint32_t)cam.width), (int)(r / (uint32_t)cam.width));
   ox[r] = cam.eye[0]; oy[r] = cam.eye[1]; oz[r] = cam.eye[2];
   dx[r] = d.x; dy[r] = d.y; dz[r] = d.z;
+}
+
+// ---------------------------------------------------------------------------------------
+// Shading and the traversal-cost heatmap: kRenderKernel's shading (src/render_engine.cu:395-446)
+// and the host post-processing of renderImage -- applyHeatmapColormap (:541-595) with
+// getTurboColor (:519-535), and savePPM's float-to-byte conversion (:502-507) -- on the device,
+// with the same explicitly rounded operations as the traversal above.
+// ---------------------------------------------------------------------------------------
+constexpr float kBgR = 0.15f, kBgG = 0.15f, kBgB = 0.18f;  // a pixel without a hit (BG_R/G/B)
+
+// d_normalize (:130-135): zero below length 1e-12, else each component times 1 / length.
+__device__ __forceinline__ float3 normalize3(float x, float y, float z) {
+  const float len = __fsqrt_rn(dot3(x, y, z, x, y, z));
+  if (len < 1e-12f) return make_float3(0.f, 0.f, 0.f);
+  const float inv = __fdiv_rn(1.0f, len);
+  return make_float3(__fmul_rn(x, inv), __fmul_rn(y, inv), __fmul_rn(z, inv));
+}
+
+// Geometric normal of triangle p (intersectTriangle, :267-271): normalise(e1 x e2).
+__device__ __forceinline__ float3 tri_normal(const MeshPtrs& m, uint32_t p) {
+  const float v0x = __ldg(m.v[0] + p), v0y = __ldg(m.v[1] + p), v0z = __ldg(m.v[2] + p);
+  const float e1x = __fsub_rn(__ldg(m.v[3] + p), v0x), e1y = __fsub_rn(__ldg(m.v[4] + p), v0y),
+              e1z = __fsub_rn(__ldg(m.v[5] + p), v0z);
+  const float e2x = __fsub_rn(__ldg(m.v[6] + p), v0x), e2y = __fsub_rn(__ldg(m.v[7] + p), v0y),
+              e2z = __fsub_rn(__ldg(m.v[8] + p), v0z);
+  return normalize3(cross_c(e1y, e2z, e1z, e2y), cross_c(e1z, e2x, e1x, e2z), cross_c(e1x, e2y, e1y, e2x));
+}
+
+__global__ void __launch_bounds__(256) k_shade(PinholeBasis cam, MeshPtrs m, uint32_t n_tris, ShadeIn in, int mode,
+                                               float diag, float3 light, float* __restrict__ rgb) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
+  if (r >= total) return;
+  const int32_t p = in.prim[r];
+  float cr, cg, cb;
+  if (p < 0 || (uint32_t)p >= n_tris) {
+    cr = kBgR; cg = kBgG; cb = kBgB;
+  } else if (mode == 0) {  // normal mapped to RGB
+    const float3 n = tri_normal(m, (uint32_t)p);
+    cr = __fmul_rn(__fadd_rn(n.x, 1.0f), 0.5f);
+    cg = __fmul_rn(__fadd_rn(n.y, 1.0f), 0.5f);
+    cb = __fmul_rn(__fadd_rn(n.z, 1.0f), 0.5f);
+  } else if (mode == 1) {  // depth: closer is brighter
+    const float depth = fmaxf(0.0f, fminf(1.0f, __fdiv_rn(in.t[r], diag)));
+    cr = cg = cb = __fsub_rn(1.0f, depth);
+  } else if (mode == 2) {  // diffuse: directional light + ambient, normal facing the camera
+    float3 n = tri_normal(m, (uint32_t)p);
+    const float3 d = pinhole_dir(cam, (int)(r % (uint32_t)cam.width), (int)(r / (uint32_t)cam.width));
+    if (dot3(n.x, n.y, n.z, d.x, d.y, d.z) > 0.0f) n = make_float3(-n.x, -n.y, -n.z);
+    const float diffuse = fmaxf(0.0f, dot3(n.x, n.y, n.z, light.x, light.y, light.z));
+    const float shade = fminf(1.0f, __fadd_rn(0.15f, __fmul_rn(diffuse, 0.85f)));
+    cr = __fmul_rn(shade, __fadd_rn(0.7f, __fmul_rn(0.3f, fabsf(n.x))));
+    cg = __fmul_rn(shade, __fadd_rn(0.7f, __fmul_rn(0.3f, fabsf(n.y))));
+    cb = __fmul_rn(shade, __fadd_rn(0.7f, __fmul_rn(0.3f, fabsf(n.z))));
+  } else if (mode == 3) {  // raw node visits (the heatmap colours them afterwards)
+    cr = cg = cb = (float)in.vis[r];
+  } else {  // unknown mode: magenta
+    cr = 1.0f; cg = 0.0f; cb = 1.0f;
+  }
+  rgb[3 * (size_t)r + 0] = cr;
+  rgb[3 * (size_t)r + 1] = cg;
+  rgb[3 * (size_t)r + 2] = cb;
+}
+
+// The heatmap's normalisation (applyHeatmapColormap, :547-572): the value at index
+// min(k - 1, floor(k * 0.999)) of the k nonzero visit counts in ascending order (128 when k = 0),
+// at least 1.  Found by a two-level select on the counts' high and low 16 bits: histogram the
+// high halves, find the bin holding that rank, histogram the low halves inside it.
+// ctl: [0] k, [1] high half of the value, [2] rank inside that bin, [3] value.
+__global__ void __launch_bounds__(256) k_heat_hist(const int32_t* __restrict__ vis, uint32_t np, int level,
+                                                   uint32_t* __restrict__ hist, const uint32_t* __restrict__ ctl) {
+  const uint32_t hi = level == 0 ? 0u : __ldcg(ctl + 1);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    const int32_t c = vis[i];
+    if (c <= 0) continue;
+    const uint32_t u = (uint32_t)c;
+    if (level == 0) atomicAdd(hist + (u >> 16), 1u);
+    else if ((u >> 16) == hi) atomicAdd(hist + (u & 0xffffu), 1u);
+  }
+}
+
+// One block of 1024 threads: level 0 counts k, picks the rank and finds its high-half bin;
+// level 1 finds the rank inside the low-half histogram.
+__global__ void __launch_bounds__(1024) k_heat_find(const uint32_t* __restrict__ hist, int level,
+                                                    uint32_t* __restrict__ ctl) {
+  constexpr int kBins = 65536, kPer = kBins / 1024;
+  __shared__ uint32_t s_sum[1024];
+  const int t = threadIdx.x;
+  uint32_t sum = 0;
+  for (int j = 0; j < kPer; ++j) sum += hist[t * kPer + j];
+  s_sum[t] = sum;
+  __syncthreads();
+  // inclusive scan of the 1024 partial sums (Hillis-Steele)
+  for (int o = 1; o < 1024; o <<= 1) {
+    const uint32_t v = t >= o ? s_sum[t - o] : 0u;
+    __syncthreads();
+    s_sum[t] += v;
+    __syncthreads();
+  }
+  const uint32_t total = s_sum[1023];
+  uint32_t rank;
+  if (level == 0) {
+    if (total == 0) {
+      if (t == 0) ctl[0] = 0;
+      return;
+    }
+    const unsigned long long k = total;
+    const unsigned long long q = (unsigned long long)((double)k * 0.999);
+    rank = (uint32_t)(q < k - 1 ? q : k - 1);
+  } else {
+    rank = __ldcg(ctl + 2);
+  }
+  const uint32_t before = t ? s_sum[t - 1] : 0u;
+  if (rank >= before && rank < s_sum[t]) {  // exactly one thread holds the rank
+    uint32_t cum = before;
+    for (int j = 0; j < kPer; ++j) {
+      const uint32_t h = hist[t * kPer + j];
+      if (rank < cum + h) {
+        const uint32_t bin = (uint32_t)(t * kPer + j);
+        if (level == 0) {
+          ctl[0] = total;
+          ctl[1] = bin;
+          ctl[2] = rank - cum;
+        } else {
+          ctl[3] = (__ldcg(ctl + 1) << 16) | bin;
+        }
+        break;
+      }
+      cum += h;
+    }
+  }
+}
+
+// getTurboColor + the per-pixel loop of applyHeatmapColormap (:519-535, 574-594): t = count /
+// max clamped to [0, 1], linear interpolation between the two nearest of 256 colormap entries;
+// a count of 0 gets the background.
+__global__ void __launch_bounds__(256) k_heat_color(const int32_t* __restrict__ vis, uint32_t np,
+                                                    const float* __restrict__ lut, float fixed_max,
+                                                    const uint32_t* __restrict__ ctl, float* __restrict__ rgb,
+                                                    float* __restrict__ used_max) {
+  float mx = fixed_max;
+  if (!(mx > 0.0f)) {
+    const uint32_t k = __ldcg(ctl + 0);
+    mx = k == 0 ? 128.0f : fmaxf(1.0f, (float)__ldcg(ctl + 3));
+  }
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && used_max) *used_max = mx;
+  if (i >= np) return;
+  const int32_t c = vis[i];
+  float cr, cg, cb;
+  if (c == 0) {
+    cr = kBgR; cg = kBgG; cb = kBgB;
+  } else {
+    float t = fmaxf(0.0f, fminf(1.0f, __fdiv_rn((float)c, mx)));
+    t = fmaxf(0.0f, fminf(1.0f, t));
+    const float scaled = __fmul_rn(t, 255.0f);
+    const int i0 = (int)scaled;
+    const int i1 = min(i0 + 1, 255);
+    const float frac = __fsub_rn(scaled, (float)i0);
+    const float w0 = __fsub_rn(1.0f, frac);
+    cr = __fadd_rn(__fmul_rn(__ldg(lut + 3 * i0 + 0), w0), __fmul_rn(__ldg(lut + 3 * i1 + 0), frac));
+    cg = __fadd_rn(__fmul_rn(__ldg(lut + 3 * i0 + 1), w0), __fmul_rn(__ldg(lut + 3 * i1 + 1), frac));
+    cb = __fadd_rn(__fmul_rn(__ldg(lut + 3 * i0 + 2), w0), __fmul_rn(__ldg(lut + 3 * i1 + 2), frac));
+  }
+  rgb[3 * (size_t)i + 0] = cr;
+  rgb[3 * (size_t)i + 1] = cg;
+  rgb[3 * (size_t)i + 2] = cb;
+}
+
+// savePPM's conversion (:502-507): clamp to [0, 1], v * 255 + 0.5, truncated to a byte.
+__global__ void __launch_bounds__(256) k_rgb8(const float* __restrict__ rgb, uint32_t nv, uint8_t* __restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+    const float v = fmaxf(0.0f, fminf(1.0f, rgb[i]));
+    out[i] = (uint8_t)__fadd_rn(__fmul_rn(v, 255.0f), 0.5f);
+  }
+}
+
+cudaError_t shade_pixels(const PinholeBasis& cam, const MeshPtrs& m, uint32_t n_tris, const ShadeIn& in, int mode,
+                         float diag, float3 light, float* rgb, cudaStream_t st) {
+  const uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
+  if (total == 0) return cudaSuccess;
+  k_shade<<<div_up(total, 256), 256, 0, st>>>(cam, m, n_tris, in, mode, diag, light, rgb);
+  return cudaGetLastError();
+}
+
+size_t heatmap_scratch_bytes() { return (size_t)2 * 65536 * 4 + 16 * 4; }
+
+cudaError_t heatmap(const int32_t* vis, uint32_t np, const float* lut, float fixed_max, void* scratch, float* rgb,
+                    float* used_max, cudaStream_t st) {
+  if (np == 0) return cudaSuccess;
+  uint32_t* h1 = static_cast<uint32_t*>(scratch);
+  uint32_t* h2 = h1 + 65536;
+  uint32_t* ctl = h2 + 65536;
+  cudaError_t e;
+  if (!(fixed_max > 0.0f)) {
+    if ((e = cudaMemsetAsync(scratch, 0, heatmap_scratch_bytes(), st)) != cudaSuccess) return e;
+    const uint32_t grid = std::min<uint32_t>(div_up(np, 256), 152 * 8);
+    k_heat_hist<<<grid, 256, 0, st>>>(vis, np, 0, h1, ctl);
+    k_heat_find<<<1, 1024, 0, st>>>(h1, 0, ctl);
+    k_heat_hist<<<grid, 256, 0, st>>>(vis, np, 1, h2, ctl);
+    k_heat_find<<<1, 1024, 0, st>>>(h2, 1, ctl);
+  }
+  k_heat_color<<<div_up(np, 256), 256, 0, st>>>(vis, np, lut, fixed_max, ctl, rgb, used_max);
+  return cudaGetLastError();
+}
+
+cudaError_t rgb_to_bytes(const float* rgb, uint32_t nv, uint8_t* out, cudaStream_t st) {
+  if (nv == 0) return cudaSuccess;
+  k_rgb8<<<std::min<uint32_t>(div_up(nv, 256), 152 * 16), 256, 0, st>>>(rgb, nv, out);
+  return cudaGetLastError();
 }
 
 cudaError_t trace_rays(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const RayPtrs& rays,

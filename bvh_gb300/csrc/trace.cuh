@@ -27,11 +27,26 @@ struct PinholeBasis {
   int32_t width, height;
 };
 
+struct ShadeIn {
+  const float* t;
+  const int32_t* prim;
+  const int32_t* vis;
+};
+
 cudaError_t trace_rays(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const RayPtrs& rays,
                        uint32_t nr, const HitOut& out, cudaStream_t st);
 cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeBasis& cam,
                           const HitOut& out, cudaStream_t st);
 cudaError_t pinhole_rays(const PinholeBasis& cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz,
                          cudaStream_t st);
+// kRenderKernel's shading of traced pinhole pixels (mode 0 normal, 1 depth, 2 diffuse, 3 visits).
+cudaError_t shade_pixels(const PinholeBasis& cam, const MeshPtrs& m, uint32_t n_tris, const ShadeIn& in, int mode,
+                         float diag, float3 light, float* rgb, cudaStream_t st);
+// applyHeatmapColormap on np visit counts with a 256-entry RGB colormap (device); scratch holds
+// heatmap_scratch_bytes().  fixed_max <= 0: the 99.9th-percentile normalisation.
+size_t heatmap_scratch_bytes();
+cudaError_t heatmap(const int32_t* vis, uint32_t np, const float* lut, float fixed_max, void* scratch, float* rgb,
+                    float* used_max, cudaStream_t st);
+cudaError_t rgb_to_bytes(const float* rgb, uint32_t nv, uint8_t* out, cudaStream_t st);
 
 }  // namespace bvhgb

@@ -17,6 +17,9 @@
  *   bvh_trace         traverseBVH over explicit rays (src/render_engine.cu:289-356).
  *   bvh_trace_pinhole kRenderKernel's primary rays + traversal (src/render_engine.cu:362-446),
  *                     returning per-pixel hit t / primitive / counters instead of colours.
+ *   bvh_shade,        kRenderKernel's shading (src/render_engine.cu:395-446) and renderImage's
+ *   bvh_heatmap,      host post-processing -- applyHeatmapColormap (:541-595), savePPM's
+ *   bvh_rgb8          conversion (:502-507) -- on the device.
  *   bvh_build_batched many independent meshes in one launch sequence (no reference counterpart;
  *                     each result equals bvh_build_device of that mesh alone).
  *
@@ -306,6 +309,27 @@ bvh_status bvh_pinhole_rays(const bvh_camera* cam, int32_t width, int32_t height
                             float* dx, float* dy, float* dz, void* stream);
 /* autoCamera (src/render_engine.cu:601-637) from the root box of a tree (host node). */
 bvh_status bvh_auto_camera(const bvh_node* host_root, bvh_camera* cam);
+
+/* Pixel shading of a bvh_trace_pinhole result (kRenderKernel's shading, src/render_engine.cu:
+ * 395-446), on the device: `hits` from bvh_trace_pinhole with the same camera and size; mode 0
+ * normal mapped to RGB, 1 depth (t / scene_diag, closer is brighter), 2 diffuse (light_dir, a
+ * host float[3], normalised by the caller; ambient 0.15), 3 the raw node-visit count (colour it
+ * with bvh_heatmap); a miss gets the background (0.15, 0.15, 0.18).  rgb: device float[3 * w * h].
+ * Asynchronous. */
+bvh_status bvh_shade(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_camera* cam, int32_t width, int32_t height,
+                     const bvh_hits* hits, int32_t mode, float scene_diag, const float* light_dir, float* rgb,
+                     void* stream);
+/* Traversal-cost heatmap (applyHeatmapColormap, src/render_engine.cu:541-595) on the device: each
+ * pixel's node-visit count over fixed_max, or, when fixed_max <= 0, over the 99.9th percentile of
+ * the nonzero counts (128 when there are none; at least 1), clamped to [0, 1] and looked up with
+ * linear interpolation in `colormap` (device float[256 * 3], RGB per entry -- the reference passes
+ * its Turbo table); a count of 0 gets the background.  used_max (device float, may be NULL)
+ * receives the normalisation.  Asynchronous. */
+bvh_status bvh_heatmap(bvh_ctx* ctx, const int32_t* nodes_visited, uint32_t n_pixels, const float* colormap,
+                       float fixed_max, float* rgb, float* used_max, void* stream);
+/* Float RGB to bytes as savePPM writes them (src/render_engine.cu:502-507): clamp to [0, 1],
+ * v * 255 + 0.5 truncated.  Device buffers of n_values each.  Asynchronous. */
+bvh_status bvh_rgb8(const float* rgb, uint32_t n_values, uint8_t* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -681,6 +681,92 @@ void orc_pinhole_rays(const float eye[3], const float look[3], const float up[3]
   }
 }
 
+/* kRenderKernel's shading of traced pixels, src/render_engine.cu:395-446: rd = each pixel's
+ * ray direction, t / prim from the traversal; a miss gets the background (:33-36). */
+void orc_shade(const orc_mesh* m, const float* rd, const float* t, const int32_t* prim, const int32_t* vis,
+               uint32_t np, int mode, float diag, const float light[3], float* rgb) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)np; ++i) {
+    float c[3];
+    const int32_t p = prim[i];
+    if (p < 0 || (uint32_t)p >= m->n) {
+      c[0] = 0.15f; c[1] = 0.15f; c[2] = 0.18f;
+    } else if (mode == 3) {
+      c[0] = c[1] = c[2] = (float)vis[i];
+    } else if (mode == 1) {
+      float depth = orc_fmax(0.0f, orc_fmin(1.0f, t[i] / diag));
+      c[0] = c[1] = c[2] = 1.0f - depth;
+    } else if (mode == 0 || mode == 2) {
+      /* geometric normal: normalise(e1 x e2), intersectTriangle :267-271 */
+      float v0x = m->v[0][p], v0y = m->v[1][p], v0z = m->v[2][p];
+      float e1x = m->v[3][p] - v0x, e1y = m->v[4][p] - v0y, e1z = m->v[5][p] - v0z;
+      float e2x = m->v[6][p] - v0x, e2y = m->v[7][p] - v0y, e2z = m->v[8][p] - v0z;
+      float n[3] = {e1y * e2z - e1z * e2y, e1z * e2x - e1x * e2z, e1x * e2y - e1y * e2x};
+      normalize3(n);
+      if (mode == 0) {
+        for (int k = 0; k < 3; ++k) c[k] = (n[k] + 1.0f) * 0.5f;
+      } else {
+        const float* d = rd + 3 * i;
+        if ((n[0] * d[0] + n[1] * d[1]) + n[2] * d[2] > 0.0f) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
+        float diffuse = orc_fmax(0.0f, (n[0] * light[0] + n[1] * light[1]) + n[2] * light[2]);
+        float shade = orc_fmin(1.0f, 0.15f + diffuse * 0.85f);
+        for (int k = 0; k < 3; ++k) c[k] = shade * (0.7f + 0.3f * fabsf(n[k]));
+      }
+    } else {
+      c[0] = 1.0f; c[1] = 0.0f; c[2] = 1.0f;
+    }
+    for (int k = 0; k < 3; ++k) rgb[3 * i + k] = c[k];
+  }
+}
+
+static int cmp_i32(const void* a, const void* b) {
+  const int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+  return (x > y) - (x < y);
+}
+
+/* applyHeatmapColormap with getTurboColor, src/render_engine.cu:519-595, for a 256 x 3 colormap;
+ * returns the normalisation used. */
+float orc_heatmap(const int32_t* vis, uint32_t np, const float* lut, float fixed_max, float* rgb) {
+  float mx = fixed_max;
+  if (mx <= 0.0f) {
+    size_t k = 0;
+    int32_t* h = (int32_t*)malloc(sizeof(int32_t) * (np ? np : 1));
+    for (uint32_t i = 0; i < np; ++i)
+      if (vis[i] > 0) h[k++] = vis[i];
+    mx = 128.0f;
+    if (k) {
+      qsort(h, k, sizeof(int32_t), cmp_i32);
+      size_t q = (size_t)((double)k * 0.999);
+      size_t idx = q < k - 1 ? q : k - 1;
+      mx = orc_fmax(1.0f, (float)h[idx]);
+    }
+    free(h);
+  }
+  for (uint32_t i = 0; i < np; ++i) {
+    if (vis[i] == 0) {
+      rgb[3 * i] = 0.15f; rgb[3 * i + 1] = 0.15f; rgb[3 * i + 2] = 0.18f;
+      continue;
+    }
+    float t = (float)vis[i] / mx;
+    t = orc_fmax(0.0f, orc_fmin(1.0f, t));
+    t = orc_fmax(0.0f, orc_fmin(1.0f, t));
+    float scaled = t * 255.0f;
+    int i0 = (int)scaled;
+    int i1 = i0 + 1 < 255 ? i0 + 1 : 255;
+    float frac = scaled - (float)i0;
+    for (int c = 0; c < 3; ++c) rgb[3 * i + c] = lut[3 * i0 + c] * (1.0f - frac) + lut[3 * i1 + c] * frac;
+  }
+  return mx;
+}
+
+/* savePPM's conversion, src/render_engine.cu:502-507. */
+void orc_rgb8(const float* rgb, uint32_t nv, uint8_t* out) {
+  for (uint32_t i = 0; i < nv; ++i) {
+    float v = orc_fmax(0.0f, orc_fmin(1.0f, rgb[i]));
+    out[i] = (uint8_t)(v * 255.0f + 0.5f);
+  }
+}
+
 /* BVHEvaluator::computeSAHRecursive, src/evaluator.cpp:54-88: DFS, float accumulation. */
 static float sah_rec(const orc_node* nodes, int nn, int x, float root_area) {
   if (x < 0 || x >= nn) return 0.0f;

@@ -94,6 +94,13 @@ int orc_tree_equal_canonical(const orc_node* a, uint32_t na, const orc_node* b, 
 int orc_threads(void);
 void orc_set_threads(int t);
 
+/* kRenderKernel's shading (src/render_engine.cu:395-446), applyHeatmapColormap (:519-595) and
+ * savePPM's byte conversion (:502-507). */
+void orc_shade(const orc_mesh* m, const float* rd, const float* t, const int32_t* prim, const int32_t* vis,
+               uint32_t np, int mode, float diag, const float light[3], float* rgb);
+float orc_heatmap(const int32_t* vis, uint32_t np, const float* lut, float fixed_max, float* rgb);
+void orc_rgb8(const float* rgb, uint32_t nv, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

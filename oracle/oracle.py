@@ -48,6 +48,11 @@ def lib():
         L.orc_trace.argtypes = [c_void_p, c_uint32, POINTER(OrcMesh), c_void_p, c_void_p, c_uint32, c_void_p,
                                 c_void_p, c_void_p, c_void_p, c_void_p]
         L.orc_pinhole_rays.argtypes = [c_void_p, c_void_p, c_void_p, c_float, c_int, c_int, c_void_p, c_void_p]
+        L.orc_shade.argtypes = [POINTER(OrcMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_int, c_float,
+                                c_void_p, c_void_p]
+        L.orc_heatmap.argtypes = [c_void_p, c_uint32, c_void_p, c_float, c_void_p]
+        L.orc_heatmap.restype = c_float
+        L.orc_rgb8.argtypes = [c_void_p, c_uint32, c_void_p]
         L.orc_sah.argtypes = [c_void_p, c_uint32]
         L.orc_sah.restype = c_float
         L.orc_depth_stats.argtypes = [c_void_p, c_uint32, POINTER(c_int), POINTER(c_float), POINTER(c_uint32)]
@@ -158,6 +163,36 @@ def pinhole_rays(eye, look, up, fovy, width, height):
     lib().orc_pinhole_rays(eye.ctypes.data, look.ctypes.data, up.ctypes.data, float(fovy), width, height,
                            ro.ctypes.data, rd.ctypes.data)
     return ro, rd
+
+
+def shade(arrays, rd, t, prim, vis, mode, diag, light):
+    """kRenderKernel's shading of traced pixels: float RGB (n, 3)."""
+    m, keep = _mesh(arrays)
+    rd = np.ascontiguousarray(rd, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(t, np.float32)
+    prim = np.ascontiguousarray(prim, np.int32)
+    vis = np.ascontiguousarray(vis, np.int32)
+    light = np.ascontiguousarray(light, np.float32)
+    rgb = np.zeros((t.shape[0], 3), np.float32)
+    lib().orc_shade(ctypes.byref(m), rd.ctypes.data, t.ctypes.data, prim.ctypes.data, vis.ctypes.data, t.shape[0],
+                    int(mode), float(diag), light.ctypes.data, rgb.ctypes.data)
+    return rgb
+
+
+def heatmap(vis, lut, fixed_max=0.0):
+    """applyHeatmapColormap with a (256, 3) colormap: (rgb (n, 3), normalisation)."""
+    vis = np.ascontiguousarray(vis, np.int32)
+    lut = np.ascontiguousarray(lut, np.float32).reshape(256, 3)
+    rgb = np.zeros((vis.shape[0], 3), np.float32)
+    mx = lib().orc_heatmap(vis.ctypes.data, vis.shape[0], lut.ctypes.data, float(fixed_max), rgb.ctypes.data)
+    return rgb, float(mx)
+
+
+def rgb8(rgb):
+    rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1)
+    out = np.zeros(rgb.shape[0], np.uint8)
+    lib().orc_rgb8(rgb.ctypes.data, rgb.shape[0], out.ctypes.data)
+    return out
 
 
 def sah(nodes) -> float:
