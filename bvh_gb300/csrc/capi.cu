@@ -34,6 +34,9 @@ struct bvh_ctx {
   bool have_timing = false;
   uint32_t* h_status = nullptr;  // pinned copy of the device status word
   cudaStream_t last_stream = nullptr;
+  // bvh_build_host: a second stream that copies the indices and leaves out while the build ends
+  cudaStream_t dl_stream = nullptr;
+  cudaEvent_t ev_leaves = nullptr, ev_dl = nullptr;
 };
 
 static bvh_status from_cuda(cudaError_t e) {
@@ -96,6 +99,9 @@ extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
   cudaDeviceSynchronize();
   if (ctx->bgraph.exec) cudaGraphExecDestroy(ctx->bgraph.exec);
   if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+  if (ctx->dl_stream) cudaStreamDestroy(ctx->dl_stream);
+  if (ctx->ev_leaves) cudaEventDestroy(ctx->ev_leaves);
+  if (ctx->ev_dl) cudaEventDestroy(ctx->ev_dl);
   workspace_free(ctx->ws);
   cudaFree(ctx->eval_buf);
   cudaFree(ctx->heat_buf);
@@ -293,11 +299,42 @@ extern "C" bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, con
   dm.v1x = dst[3]; dm.v1y = dst[4]; dm.v1z = dst[5];
   dm.v2x = dst[6]; dm.v2y = dst[7]; dm.v2z = dst[8];
   dm.n = n;
+  // A plain LBVH's indices are final after the sort and its leaves after the emission kernel:
+  // a second stream copies those out while the rest of the build runs; the internal nodes
+  // follow on the build's stream.  The copies use the link the whole time, which bounds the call.
+  const bool early = params->algo == BVH_ALGO_LBVH && n > 1;
+  if (early && !ctx->dl_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->dl_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_leaves, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_dl, cudaEventDisableTiming);
+    if (e != cudaSuccess) return from_cuda(e);
+  }
   bvh_tree tree;
+  ws.leaves_ready = early ? ctx->ev_leaves : nullptr;
   bvh_status s = build_impl(ctx, &dm, params, st, &tree);
+  ws.leaves_ready = nullptr;
   if (s != BVH_OK) return s;
-  s = bvh_tree_download(ctx, &tree, stream, host_nodes, host_indices);
-  if (s != BVH_OK) return s;
+  if (early) {
+    cudaStream_t dl = ctx->dl_stream;
+    cudaError_t e = cudaStreamWaitEvent(dl, ctx->evs.ev[3], 0);  // sort (and run fix-up) done
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_indices, tree.indices, (size_t)n * 4, cudaMemcpyDeviceToHost, dl);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(dl, ctx->ev_leaves, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(host_nodes + (n - 1), tree.nodes + (n - 1), (size_t)n * sizeof(bvh_node),
+                          cudaMemcpyDeviceToHost, dl);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_dl, dl);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(host_nodes, tree.nodes, (size_t)(n - 1) * sizeof(bvh_node), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->ev_dl, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(dl);
+      return from_cuda(e);
+    }
+  } else {
+    s = bvh_tree_download(ctx, &tree, stream, host_nodes, host_indices);
+    if (s != BVH_OK) return s;
+  }
   s = check_status_word(ctx);
   if (s == BVH_OK && n_nodes) *n_nodes = tree.n_nodes;
   return s;

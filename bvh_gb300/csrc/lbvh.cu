@@ -655,6 +655,7 @@ static void launch_emit(Workspace& ws, int fb, uint32_t n, const ScratchLayout& 
   // delta bytes: computed by k_emit from the 30-bit keys, written by the run fix-up for 60/63 bits
   k_emit<SegSingle, PARENTS, kEmitTile, BITS == 30><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
       ws.delta, keys, ws.vals[fb], ws.boxes, ws.nodes, n, SegSingle{n}, nullptr, frontier, fcount, kEmitMaxSteps);
+  if (ws.leaves_ready && !PARENTS) cudaEventRecord(ws.leaves_ready, st);
   k_emit_climb<SegSingle, PARENTS><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(
       ws.delta, ws.nodes, ws.slots, epoch, n, SegSingle{n}, frontier, fcount);
 }

@@ -52,6 +52,9 @@ struct Workspace {
   float* bat_mbox = nullptr;          // device, count * 8
   uint32_t* bat_indices = nullptr;    // device, n (mesh-local original indices)
   uint32_t bat_count_cap = 0, bat_n_cap = 0;
+  // recorded (when set) between the LBVH emission and its frontier climb: from there on the leaf
+  // nodes [n-1, 2n-1) of a plain LBVH are final and can be copied out while the climb runs
+  cudaEvent_t leaves_ready = nullptr;
 };
 
 // First epoch value; every build adds kEpochStride (emission uses E, treelet round r uses E+1+r).

@@ -169,7 +169,9 @@ bvh_status bvh_build_device(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_pa
                             bvh_tree* out);
 
 /* Build from host SoA, as BVHBuilder::build does: upload, build, download.  Synchronous.
- * host_nodes must hold 2n-1 entries (n >= 1), host_indices n entries. */
+ * host_nodes must hold 2n-1 entries (n >= 1), host_indices n entries.  For a plain LBVH the
+ * indices and the leaf nodes are copied out on a second stream of the context while the build
+ * finishes (pinned host buffers let those copies overlap the kernels). */
 bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
                           bvh_node* host_nodes, uint32_t* host_indices, uint32_t* n_nodes);
 

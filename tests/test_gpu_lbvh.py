@@ -67,13 +67,28 @@ def test_lbvh_unaligned_input_takes_scalar_path(ctx, gpu, oracle_lib):
     assert np.array_equal(idx, oidx) and O.node_fields_equal(nodes, onodes)
 
 
-def test_host_path_equals_device_path(ctx, gpu):
-    m = meshgen.clustered(50_000, seed=5)
-    p = ctx.params(C.ALGO_LBVH, morton_bits=63)
+@pytest.mark.parametrize("bits", [30, 60, 63])
+@pytest.mark.parametrize("n", [2, 3, 257, 50_000, 2_000_000])
+def test_host_path_equals_device_path(ctx, gpu, bits, n):
+    """bvh_build_host copies the indices and the leaves out on a second stream while the build
+    finishes; the result equals the device build's."""
+    m = meshgen.clustered(n, seed=5)
+    p = ctx.params(C.ALGO_LBVH, morton_bits=bits)
     hn, hi = ctx.build_host(m, p)
     dn, di, _, _ = build(ctx, gpu, m, p)
     assert np.array_equal(hi, di)
     assert np.array_equal(hn[["min", "max", "left", "right"]], dn[["min", "max", "left", "right"]])
+
+
+def test_host_path_repeated_and_mixed(ctx, gpu, oracle_lib):
+    """Host builds of shrinking and growing sizes, between device builds, against the oracle."""
+    O = oracle_lib
+    for n, bits in ((30000, 63), (300, 30), (30000, 30), (7, 63), (2, 30), (1, 63), (12000, 60)):
+        m = meshgen.uniform_small(n, seed=200 + n)
+        hn, hi = ctx.build_host(m, ctx.params(C.ALGO_LBVH, morton_bits=bits))
+        onodes, oidx, _ = O.lbvh(m.arrays(), bits)
+        assert np.array_equal(hi, oidx) and O.node_fields_equal(hn, onodes)
+        build(ctx, gpu, meshgen.uniform_small(999, seed=n), ctx.params(C.ALGO_PLOC))
 
 
 def test_repeated_builds_reuse_workspace(ctx, gpu, oracle_lib):
