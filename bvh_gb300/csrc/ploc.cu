@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   extern __shared__ float4 sw[];
   float* sD = reinterpret_cast<float*>(sw + 2 * (kNnTile + 2 * r));  // [kNnKc][kNnTile]
   const uint32_t c = __ldcg(B.ctrl + 0);
-  const Box* __restrict__ cbox = B.cbox[__ldcg(B.ctrl + 3) & 1u];
+  const Box* __restrict__ cbox = (__ldcg(B.ctrl + 3) & 1u) ? B.cbox[1] : B.cbox[0];  // no stack copy of B
   const int span = kNnTile + 2 * r;
   float4* s_lo = sw;
   float4* s_hi = sw + span;
@@ -219,11 +219,10 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
 // ids follow the cluster order.
 constexpr int kPlocRounds = kPlocTile / kPlocThreads;  // 8
 
-// Item i merges here (as the smaller index of a mutual pair) / survives.
-__device__ __forceinline__ void item_flags(const int32_t* __restrict__ nbr, uint32_t c, uint32_t i, int32_t& j,
-                                           bool& m, bool& v) {
-  j = i < c ? __ldcg(nbr + i) : -1;
-  const bool mutual = i < c && j >= 0 && (uint32_t)j < c && __ldcg(nbr + j) == (int32_t)i;
+// Item i merges here (as the smaller index of a mutual pair) / survives, from its neighbour j
+// and j's neighbour `back` (-1 where not loaded).
+__device__ __forceinline__ void item_flags(uint32_t c, uint32_t i, int32_t j, int32_t back, bool& m, bool& v) {
+  const bool mutual = i < c && j >= 0 && (uint32_t)j < c && back == (int32_t)i;
   m = mutual && (int32_t)i < j;
   v = i < c && !(mutual && j < (int32_t)i);
 }
@@ -289,17 +288,27 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const uint32_t base = tile * kPlocTile + w * (32 * kPlocRounds);
-    uint32_t tm = 0, tv = 0;
+    // all rounds' neighbours, then their neighbours, so that each load batch is in flight at once
+    int32_t j[kPlocRounds], back[kPlocRounds];
 #pragma unroll
     for (int r = 0; r < kPlocRounds; ++r) {
-      int32_t j;
+      const uint32_t i = base + r * 32 + lane;
+      j[r] = i < c ? __ldcg(B.nbr + i) : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < kPlocRounds; ++r) back[r] = (j[r] >= 0 && (uint32_t)j[r] < c) ? __ldcg(B.nbr + j[r]) : -1;
+    uint32_t tm = 0, tv = 0;
+    uint2 mine = make_uint2(0u, 0u);  // lane r keeps round r's ballots
+#pragma unroll
+    for (int r = 0; r < kPlocRounds; ++r) {
       bool m, v;
-      item_flags(B.nbr, c, base + r * 32 + lane, j, m, v);
+      item_flags(c, base + r * 32 + lane, j[r], back[r], m, v);
       const uint32_t mb = __ballot_sync(0xffffffffu, m), vb = __ballot_sync(0xffffffffu, v);
-      if (lane == 0) B.flags[((size_t)tile * (kPlocThreads / 32) + w) * kPlocRounds + r] = make_uint2(mb, vb);
+      if (lane == r) mine = make_uint2(mb, vb);
       tm += __popc(mb);
       tv += __popc(vb);
     }
+    if (lane < kPlocRounds) B.flags[((size_t)tile * (kPlocThreads / 32) + w) * kPlocRounds + lane] = mine;
     if (lane == 0) s_w[w] = ((unsigned long long)tm << 31) | tv;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -322,15 +331,17 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
   if (threadIdx.x == 0) B.ctrl[2] = 0;
 }
 
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_scatter(PlocBufs B) {
+__global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
   __shared__ unsigned long long s_w[kPlocThreads / 32];
   const uint32_t c = __ldcg(B.ctrl + 0);
   const uint32_t next = __ldcg(B.ctrl + 1);
   const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
-  const Box* __restrict__ cin = B.cbox[par];
-  const int32_t* __restrict__ idin = B.cid[par];
-  Box* __restrict__ cout = B.cbox[par ^ 1u];
-  int32_t* __restrict__ idout = B.cid[par ^ 1u];
+  // selects, not an indexed parameter array (which would be copied to the stack)
+  const Box* __restrict__ cin = par ? B.cbox[1] : B.cbox[0];
+  const int32_t* __restrict__ idin = par ? B.cid[1] : B.cid[0];
+  Box* __restrict__ cout = par ? B.cbox[0] : B.cbox[1];
+  int32_t* __restrict__ idout = par ? B.cid[0] : B.cid[1];
+  Node* __restrict__ nodes = B.nodes;
   const uint32_t tiles = div_up(c, kPlocTile);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
@@ -358,37 +369,56 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_scatter(PlocBufs B) {
       if (k < w) before += s_w[k];
     __syncthreads();  // s_w is rewritten by the next tile
     uint32_t mpos = (uint32_t)(before >> 31), vpos = (uint32_t)(before & 0x7fffffffull);
+    // two rounds at a time: both rounds' boxes and ids are loaded before either round stores
 #pragma unroll
-    for (int r = 0; r < kPlocRounds; ++r) {
-      const uint32_t i = base + r * 32 + lane;
-      const bool m = (mb[r] >> lane) & 1u, v = (vb[r] >> lane) & 1u;
-      if (m || v) {
-        const float4* ip = reinterpret_cast<const float4*>(cin + i);
-        float4 lo = __ldcg(ip), hi = __ldcg(ip + 1);
-        int32_t id = __ldcg(idin + i);
+    for (int r0 = 0; r0 < kPlocRounds; r0 += 2) {
+      float4 lo[2], hi[2], jlo[2], jhi[2];
+      int32_t id[2], jid[2];
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int r = r0 + g;
+        const uint32_t i = base + r * 32 + lane;
+        const bool m = (mb[r] >> lane) & 1u, v = (vb[r] >> lane) & 1u;
+        lo[g] = hi[g] = jlo[g] = jhi[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        id[g] = jid[g] = 0;
+        if (m || v) {
+          const float4* ip = reinterpret_cast<const float4*>(cin + i);
+          lo[g] = __ldcg(ip);
+          hi[g] = __ldcg(ip + 1);
+          id[g] = __ldcg(idin + i);
+        }
         if (m) {
-          const int32_t j = nj[r];
-          const float4* jp = reinterpret_cast<const float4*>(cin + j);
-          const float4 jlo = __ldcg(jp), jhi = __ldcg(jp + 1);
-          lo = make_float4(fminf(lo.x, jlo.x), fminf(lo.y, jlo.y), fminf(lo.z, jlo.z), 0.f);
-          hi = make_float4(fmaxf(hi.x, jhi.x), fmaxf(hi.y, jhi.y), fmaxf(hi.z, jhi.z), 0.f);
-          const int32_t nid = (int32_t)(next + mpos + __popc(mb[r] & lt));
-          float4* np = reinterpret_cast<float4*>(B.nodes + nid);
-          np[0] = lo;
-          np[1] = hi;
-          reinterpret_cast<int4*>(np + 2)[0] = make_int4(id, __ldcg(idin + j), 0, 0);
-          id = nid;
+          const float4* jp = reinterpret_cast<const float4*>(cin + nj[r]);
+          jlo[g] = __ldcg(jp);
+          jhi[g] = __ldcg(jp + 1);
+          jid[g] = __ldcg(idin + nj[r]);
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int r = r0 + g;
+        const bool m = (mb[r] >> lane) & 1u, v = (vb[r] >> lane) & 1u;
+        float4 a = lo[g], b = hi[g];
+        int32_t nid = id[g];
+        if (m) {
+          a = make_float4(fminf(a.x, jlo[g].x), fminf(a.y, jlo[g].y), fminf(a.z, jlo[g].z), 0.f);
+          b = make_float4(fmaxf(b.x, jhi[g].x), fmaxf(b.y, jhi[g].y), fmaxf(b.z, jhi[g].z), 0.f);
+          nid = (int32_t)(next + mpos + __popc(mb[r] & lt));
+          float4* np = reinterpret_cast<float4*>(nodes + nid);
+          np[0] = a;
+          np[1] = b;
+          reinterpret_cast<int4*>(np + 2)[0] = make_int4(id[g], jid[g], 0, 0);
         }
         if (v) {
           const uint32_t o = vpos + __popc(vb[r] & lt);
           float4* op = reinterpret_cast<float4*>(cout + o);
-          op[0] = lo;
-          op[1] = hi;
-          idout[o] = id;
+          op[0] = a;
+          op[1] = b;
+          idout[o] = nid;
         }
+        mpos += __popc(mb[r]);
+        vpos += __popc(vb[r]);
       }
-      mpos += __popc(mb[r]);
-      vpos += __popc(vb[r]);
     }
   }
 }
