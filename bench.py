@@ -39,6 +39,8 @@ WORKLOADS = {
                   "10M clustered triangles, PLOC radius 25"),
     "c1_lbvhplus": ("clustered", {"n": 10_000_000, "seed": 1}, "lbvh_plus", 60, 0,
                     "10M clustered triangles, LBVH+ 60-bit, 1 treelet pass"),
+    "c1_lbvhplus3": ("clustered", {"n": 10_000_000, "seed": 1}, "lbvh_plus", 60, 0,
+                     "10M clustered triangles, LBVH+ 60-bit, 3 treelet passes"),
     "c1_lbvh63_4m": ("clustered", {"n": 4_000_000, "seed": 1}, "lbvh", 63, 0,
                      "4M clustered triangles (config 1 distribution), LBVH 63-bit; profiling size"),
     "c1_lbvhplus_2m": ("clustered", {"n": 2_000_000, "seed": 1}, "lbvh_plus", 60, 0,
@@ -63,6 +65,12 @@ WORKLOADS = {
     "c0_lbvh30": ("uniform_small", {"n": 100_000, "seed": 0}, "lbvh", 30, 0,
                   "100k uniform triangles, LBVH 30-bit"),
 }
+# LBVH+ treelet passes per workload (1 where not listed: the reference's own count)
+TREELET_ROUNDS = {"c1_lbvhplus3": 3}
+
+
+def treelet_rounds(name: str) -> int:
+    return TREELET_ROUNDS.get(name, 1) if WORKLOADS[name][2] == "lbvh_plus" else 0
 
 
 def bytes_per_tri(algo: str, bits: int, rounds: int = 0, cluster_sum_per_tri: float = 0.0) -> float:
@@ -235,7 +243,7 @@ def cpu_baseline(name, mesh, budget_s=12.0):
         if algo == "ploc":
             O.ploc(arrays, radius)
         elif algo == "lbvh_plus":
-            O.lbvh_plus(arrays, bits, 1)
+            O.lbvh_plus(arrays, bits, treelet_rounds(name))
         else:
             O.lbvh(arrays, bits)
         reps += 1
@@ -264,6 +272,7 @@ def run_ours(args):
     algo_id = {"lbvh": C.ALGO_LBVH, "lbvh_plus": C.ALGO_LBVH_PLUS, "ploc": C.ALGO_PLOC}[algo]
     ctx = bvh_gb300.Context(local)
     params = ctx.params(algo_id, morton_bits=bits, ploc_radius=radius or 25,
+                        treelet_rounds=max(1, treelet_rounds(args.workload)),
                         host_loops=getattr(args, "host_loops", False))
     d_in = [torch.from_numpy(a).to(dev) for a in mesh.arrays()]
     ptrs = [t.data_ptr() for t in d_in]
@@ -310,7 +319,7 @@ def run_ours(args):
     st = np.array(stages, np.float64)
     med = np.median(st, axis=0)
     peak, peak_kind = hbm_peak()
-    rounds = 1 if algo == "lbvh_plus" else 0
+    rounds = treelet_rounds(args.workload)
     csum = ploc_csum / n if algo == "ploc" else 0.0
     # dominant stage: the largest share of device time (stage events on the launching stream)
     shares = {"scene_bounds": med[0], "morton_boxes_hist": med[1], "onesweep_sort": med[2], "emit_refit": med[3],
@@ -736,6 +745,9 @@ def run_reference(args):
     ref_algo = {"lbvh": "LBVHBuilderCUDA (30-bit Morton, CUB radix sort)",
                 "lbvh_plus": "LBVHPlusBuilderCUDA (60-bit, Thrust sort, 1 treelet pass)",
                 "ploc": f"PLOCBuilderCUDA(r={radius})"}[algo]
+    if treelet_rounds(args.workload) > 1:
+        ref_algo += f"; the reference has no multi-pass LBVH+, so this is its 1-pass build, not the " \
+                    f"workload's {treelet_rounds(args.workload)} passes"
     line = {
         "impl": "reference", "metric": "build Mtris/s (device-resident) + %HBM roofline",
         "value": round(value, 2), "unit": "Mtris/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

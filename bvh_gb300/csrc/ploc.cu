@@ -81,20 +81,20 @@ __device__ __forceinline__ float pair_area(float4 xa, float4 xb, float4 ja, floa
                 __fsub_rn(fmaxf(xb.z, jb.z), fminf(xa.z, ja.z)));
 }
 
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
-  // (kNnTile + 2r) boxes: all lo corners, then all hi corners (lanes read consecutive 16 bytes)
-  extern __shared__ float4 sw[];
-  float* sD = reinterpret_cast<float*>(sw + 2 * (kNnTile + 2 * r));  // [kNnKc][kNnTile]
-  const uint32_t c = __ldcg(B.ctrl + 0);
-  const Box* __restrict__ cbox = (__ldcg(B.ctrl + 3) & 1u) ? B.cbox[1] : B.cbox[0];  // no stack copy of B
-  const int span = kNnTile + 2 * r;
+template <int PER>
+__device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, const Box* __restrict__ cbox,
+                                         float4* sw) {
+  constexpr int TILE = kPlocThreads * PER;
+  // (TILE + 2r) boxes: all lo corners, then all hi corners (lanes read consecutive 16 bytes)
+  float* sD = reinterpret_cast<float*>(sw + 2 * (TILE + 2 * r));  // [kNnKc][TILE]
+  const int span = TILE + 2 * r;
   float4* s_lo = sw;
   float4* s_hi = sw + span;
   const int t = threadIdx.x;
   const float kInf = __int_as_float(0x7f800000);
-  for (uint32_t base = blockIdx.x * (uint32_t)kNnTile; base < c; base += gridDim.x * (uint32_t)kNnTile) {
+  for (uint32_t base = blockIdx.x * (uint32_t)TILE; base < c; base += gridDim.x * (uint32_t)TILE) {
     const int lo = (int)base - r;  // window position 0; may be negative
-    const int tile_n = (int)min((uint32_t)kNnTile, c - base);
+    const int tile_n = (int)min((uint32_t)TILE, c - base);
     __syncthreads();  // previous tile's window no longer read
     for (int k = t; k < span; k += kPlocThreads) {
       const int j = lo + k;
@@ -105,11 +105,11 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       }
     }
     __syncthreads();
-    float fd[kNnPer], ed[kNnPer];  // forward / backward best areas (+inf: none yet)
-    int fj[kNnPer], ej[kNnPer];
-    float4 xa[kNnPer], xb[kNnPer];
+    float fd[PER], ed[PER];  // forward / backward best areas (+inf: none yet)
+    int fj[PER], ej[PER];
+    float4 xa[PER], xb[PER];
 #pragma unroll
-    for (int m = 0; m < kNnPer; ++m) {
+    for (int m = 0; m < PER; ++m) {
       fd[m] = ed[m] = kInf;
       fj[m] = ej[m] = -1;
       const int xi = t + m * kPlocThreads;
@@ -118,14 +118,14 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
     }
     // interior tile: every cluster has all r neighbours on both sides, so full offset chunks
     // take a path without bounds checks (fully unrolled)
-    const bool interior = (int)base >= r && base + (uint32_t)kNnTile + (uint32_t)r <= c;
+    const bool interior = (int)base >= r && base + (uint32_t)TILE + (uint32_t)r <= c;
     for (int k0 = 1; k0 <= r; k0 += kNnKc) {
       const int kc = min(kNnKc, r - k0 + 1);
       const bool full = interior && kc == kNnKc;
       // pairs (x, x + k), k in [k0, k0 + kc): forward candidates of x, table entries for x + k
       if (full) {
 #pragma unroll
-        for (int m = 0; m < kNnPer; ++m) {
+        for (int m = 0; m < PER; ++m) {
           const int xi = t + m * kPlocThreads;
 #pragma unroll
           for (int kk = 0; kk < kNnKc; ++kk) {
@@ -135,12 +135,12 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
               fd[m] = d;
               fj[m] = (int)base + xi + k0 + kk;
             }
-            if (xi + k0 + kk < kNnTile) sD[kk * kNnTile + xi + k0 + kk] = d;
+            if (xi + k0 + kk < TILE) sD[kk * TILE + xi + k0 + kk] = d;
           }
         }
       } else {
 #pragma unroll
-        for (int m = 0; m < kNnPer; ++m) {
+        for (int m = 0; m < PER; ++m) {
           const int xi = t + m * kPlocThreads;
           if (xi < tile_n) {
             const int kmax = min(kc, (int)c - 1 - ((int)base + xi) - k0 + 1);  // j = base + xi + k < c
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
                 fd[m] = d;
                 fj[m] = (int)base + xi + k0 + kk;
               }
-              if (xi + k0 + kk < tile_n) sD[kk * kNnTile + xi + k0 + kk] = d;
+              if (xi + k0 + kk < tile_n) sD[kk * TILE + xi + k0 + kk] = d;
             }
           }
         }
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
           const int h = (int)base + p - k;  // the halo cluster; p is the tile-relative target
           if (h >= 0) {
             const int hw = p - k + r;
-            sD[kk * kNnTile + p] = pair_area(s_lo[hw], s_hi[hw], s_lo[p + r], s_hi[p + r]);
+            sD[kk * TILE + p] = pair_area(s_lo[hw], s_hi[hw], s_lo[p + r], s_hi[p + r]);
           }
         }
       }
@@ -172,11 +172,11 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       // backward candidates j - k of this thread's clusters
       if (full) {
 #pragma unroll
-        for (int m = 0; m < kNnPer; ++m) {
+        for (int m = 0; m < PER; ++m) {
           const int xi = t + m * kPlocThreads;
 #pragma unroll
           for (int kk = 0; kk < kNnKc; ++kk) {
-            const float d = sD[kk * kNnTile + xi];
+            const float d = sD[kk * TILE + xi];
             if (d < kInf && d <= ed[m]) {
               ed[m] = d;
               ej[m] = (int)base + xi - k0 - kk;
@@ -185,13 +185,13 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
         }
       } else {
 #pragma unroll
-        for (int m = 0; m < kNnPer; ++m) {
+        for (int m = 0; m < PER; ++m) {
           const int xi = t + m * kPlocThreads;
           if (xi < tile_n) {
             for (int kk = 0; kk < kc; ++kk) {
               const int src = (int)base + xi - k0 - kk;
               if (src < 0) break;
-              const float d = sD[kk * kNnTile + xi];
+              const float d = sD[kk * TILE + xi];
               if (d < kInf && d <= ed[m]) {  // later offset = smaller index: wins ties
                 ed[m] = d;
                 ej[m] = src;
@@ -203,20 +203,33 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
       __syncthreads();  // the table is refilled by the next chunk
     }
 #pragma unroll
-    for (int m = 0; m < kNnPer; ++m) {
+    for (int m = 0; m < PER; ++m) {
       const int xi = t + m * kPlocThreads;
       if (xi < tile_n) B.nbr[base + xi] = (ej[m] >= 0 && ed[m] <= fd[m]) ? ej[m] : fj[m];  // earlier index wins ties
     }
   }
 }
 
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
+  extern __shared__ float4 sw[];
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const Box* __restrict__ cbox = (__ldcg(B.ctrl + 3) & 1u) ? B.cbox[1] : B.cbox[0];  // no stack copy of B
+  // Once the live clusters no longer fill the grid with 4-per-thread tiles, an iteration lasts
+  // one tile's latency: smaller tiles (2 or 1 clusters per thread) then spread it over more
+  // blocks.  The result does not depend on the tiling.
+  const uint32_t g = gridDim.x * (uint32_t)kPlocThreads;
+  if (c > 2u * g) nn_tiles<kNnPer>(B, r, c, cbox, sw);
+  else if (c > g) nn_tiles<2>(B, r, c, cbox, sw);
+  else nn_tiles<1>(B, r, c, cbox, sw);
+}
+
 // Merge mutual pairs (i < j keeps position i, :211-264) and compact the survivors (:267-293),
-// as reduce-then-scan: k_ploc_count totals each 2048-cluster tile and its last block scans the
-// tile totals, k_ploc_scatter recomputes its tile's flags and writes, k_ploc_step ends the
-// iteration.  Warp w of a tile
-// takes its items w*256 + r*32 + lane in 8 rounds r of 32 consecutive clusters, so positions
-// within the warp come from ballots.  Counts are packed as merges << 31 | survivors; new node
-// ids follow the cluster order.
+// as reduce-then-scan: k_ploc_count totals each tile of 256 R clusters (R <= 8 rounds per warp)
+// and stores its ballots, its last block scans the tile totals, k_ploc_scatter reads the ballots
+// and writes, k_ploc_step ends the iteration.  Warp w of a tile takes its items w*32R + r*32 +
+// lane in R rounds r of 32 consecutive clusters, so positions within the warp come from ballots
+// and new node ids follow the cluster order whatever R is.  Counts are packed as
+// merges << 31 | survivors.
 constexpr int kPlocRounds = kPlocTile / kPlocThreads;  // 8
 
 // Item i merges here (as the smaller index of a mutual pair) / survives, from its neighbour j
@@ -281,26 +294,34 @@ __device__ __forceinline__ void ploc_scan_tiles(PlocBufs B, uint32_t tiles, unsi
   }
 }
 
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
-  __shared__ unsigned long long s_w[kPlocThreads / 32];
-  const uint32_t c = __ldcg(B.ctrl + 0);
-  const uint32_t tiles = div_up(c, kPlocTile);
+// Rounds of 32 clusters per warp in a merge tile (8 at most, 2048 clusters per tile): the fewest
+// whose tiles still fill the grid, so that late iterations (few clusters) spread over all blocks.
+// k_ploc_count and k_ploc_scatter run on the same grid and agree on it.
+__device__ __forceinline__ int ploc_rounds(uint32_t c) {
+#pragma unroll
+  for (int r = 1; r < kPlocRounds; r <<= 1)
+    if (div_up(c, (uint32_t)(kPlocThreads * r)) <= gridDim.x) return r;
+  return kPlocRounds;
+}
+
+template <int R>
+__device__ __forceinline__ void count_tiles(const PlocBufs& B, uint32_t c, uint32_t tiles, unsigned long long* s_w) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const uint32_t base = tile * kPlocTile + w * (32 * kPlocRounds);
+    const uint32_t base = tile * (uint32_t)(kPlocThreads * R) + w * (32u * R);
     // all rounds' neighbours, then their neighbours, so that each load batch is in flight at once
-    int32_t j[kPlocRounds], back[kPlocRounds];
+    int32_t j[R], back[R];
 #pragma unroll
-    for (int r = 0; r < kPlocRounds; ++r) {
+    for (int r = 0; r < R; ++r) {
       const uint32_t i = base + r * 32 + lane;
       j[r] = i < c ? __ldcg(B.nbr + i) : -1;
     }
 #pragma unroll
-    for (int r = 0; r < kPlocRounds; ++r) back[r] = (j[r] >= 0 && (uint32_t)j[r] < c) ? __ldcg(B.nbr + j[r]) : -1;
+    for (int r = 0; r < R; ++r) back[r] = (j[r] >= 0 && (uint32_t)j[r] < c) ? __ldcg(B.nbr + j[r]) : -1;
     uint32_t tm = 0, tv = 0;
     uint2 mine = make_uint2(0u, 0u);  // lane r keeps round r's ballots
 #pragma unroll
-    for (int r = 0; r < kPlocRounds; ++r) {
+    for (int r = 0; r < R; ++r) {
       bool m, v;
       item_flags(c, base + r * 32 + lane, j[r], back[r], m, v);
       const uint32_t mb = __ballot_sync(0xffffffffu, m), vb = __ballot_sync(0xffffffffu, v);
@@ -308,7 +329,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
       tm += __popc(mb);
       tv += __popc(vb);
     }
-    if (lane < kPlocRounds) B.flags[((size_t)tile * (kPlocThreads / 32) + w) * kPlocRounds + lane] = mine;
+    if (lane < R) B.flags[((size_t)tile * (kPlocThreads / 32) + w) * R + lane] = mine;
     if (lane == 0) s_w[w] = ((unsigned long long)tm << 31) | tv;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -318,6 +339,19 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
       B.desc[tile] = t;
     }
     __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
+  __shared__ unsigned long long s_w[kPlocThreads / 32];
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const int R = ploc_rounds(c);
+  const uint32_t tiles = div_up(c, (uint32_t)(kPlocThreads * R));
+  switch (R) {
+    case 1: count_tiles<1>(B, c, tiles, s_w); break;
+    case 2: count_tiles<2>(B, c, tiles, s_w); break;
+    case 4: count_tiles<4>(B, c, tiles, s_w); break;
+    default: count_tiles<kPlocRounds>(B, c, tiles, s_w); break;
   }
   // the last block to finish scans the tile totals (ticket in ctrl[2])
   __shared__ bool s_last;
@@ -331,29 +365,22 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
   if (threadIdx.x == 0) B.ctrl[2] = 0;
 }
 
-__global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
-  __shared__ unsigned long long s_w[kPlocThreads / 32];
-  const uint32_t c = __ldcg(B.ctrl + 0);
-  const uint32_t next = __ldcg(B.ctrl + 1);
-  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
-  // selects, not an indexed parameter array (which would be copied to the stack)
-  const Box* __restrict__ cin = par ? B.cbox[1] : B.cbox[0];
-  const int32_t* __restrict__ idin = par ? B.cid[1] : B.cid[0];
-  Box* __restrict__ cout = par ? B.cbox[0] : B.cbox[1];
-  int32_t* __restrict__ idout = par ? B.cid[0] : B.cid[1];
-  Node* __restrict__ nodes = B.nodes;
-  const uint32_t tiles = div_up(c, kPlocTile);
+template <int R>
+__device__ __forceinline__ void scatter_tiles(const PlocBufs& B, uint32_t c, uint32_t next, uint32_t tiles,
+                                              const Box* __restrict__ cin, const int32_t* __restrict__ idin,
+                                              Box* __restrict__ cout, int32_t* __restrict__ idout,
+                                              Node* __restrict__ nodes, unsigned long long* s_w) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const uint32_t base = tile * kPlocTile + w * (32 * kPlocRounds);
-    uint32_t mb[kPlocRounds], vb[kPlocRounds];
-    int32_t nj[kPlocRounds];
+    const uint32_t base = tile * (uint32_t)(kPlocThreads * R) + w * (32u * R);
+    uint32_t mb[R], vb[R];
+    int32_t nj[R];
     uint32_t tm = 0, tv = 0;
     // the ballots k_ploc_count stored; the partner of each merging cluster
-    const uint2* fl = B.flags + ((size_t)tile * (kPlocThreads / 32) + w) * kPlocRounds;
+    const uint2* fl = B.flags + ((size_t)tile * (kPlocThreads / 32) + w) * R;
 #pragma unroll
-    for (int r = 0; r < kPlocRounds; ++r) {
+    for (int r = 0; r < R; ++r) {
       const uint2 f = __ldcg(fl + r);
       mb[r] = f.x;
       vb[r] = f.y;
@@ -371,11 +398,11 @@ __global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
     uint32_t mpos = (uint32_t)(before >> 31), vpos = (uint32_t)(before & 0x7fffffffull);
     // two rounds at a time: both rounds' boxes and ids are loaded before either round stores
 #pragma unroll
-    for (int r0 = 0; r0 < kPlocRounds; r0 += 2) {
+    for (int r0 = 0; r0 < R; r0 += 2) {
       float4 lo[2], hi[2], jlo[2], jhi[2];
       int32_t id[2], jid[2];
 #pragma unroll
-      for (int g = 0; g < 2; ++g) {
+      for (int g = 0; g < 2 && r0 + g < R; ++g) {
         const int r = r0 + g;
         const uint32_t i = base + r * 32 + lane;
         const bool m = (mb[r] >> lane) & 1u, v = (vb[r] >> lane) & 1u;
@@ -395,7 +422,7 @@ __global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
         }
       }
 #pragma unroll
-      for (int g = 0; g < 2; ++g) {
+      for (int g = 0; g < 2 && r0 + g < R; ++g) {
         const int r = r0 + g;
         const bool m = (mb[r] >> lane) & 1u, v = (vb[r] >> lane) & 1u;
         float4 a = lo[g], b = hi[g];
@@ -420,6 +447,27 @@ __global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
         vpos += __popc(vb[r]);
       }
     }
+  }
+}
+
+__global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
+  __shared__ unsigned long long s_w[kPlocThreads / 32];
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const uint32_t next = __ldcg(B.ctrl + 1);
+  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
+  // selects, not an indexed parameter array (which would be copied to the stack)
+  const Box* __restrict__ cin = par ? B.cbox[1] : B.cbox[0];
+  const int32_t* __restrict__ idin = par ? B.cid[1] : B.cid[0];
+  Box* __restrict__ cout = par ? B.cbox[0] : B.cbox[1];
+  int32_t* __restrict__ idout = par ? B.cid[0] : B.cid[1];
+  Node* __restrict__ nodes = B.nodes;
+  const int R = ploc_rounds(c);
+  const uint32_t tiles = div_up(c, (uint32_t)(kPlocThreads * R));
+  switch (R) {
+    case 1: scatter_tiles<1>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
+    case 2: scatter_tiles<2>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
+    case 4: scatter_tiles<4>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
+    default: scatter_tiles<kPlocRounds>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
   }
 }
 
@@ -474,7 +522,10 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   // neighbours (cap) + per-tile merge totals / prefixes (64-bit) share one allocation
   // ... and the per-round ballots (8 B per 32 clusters)
   size_t desc_words = div_up(cap, kPlocTile) + 8;
-  size_t flag_words = (size_t)div_up(cap, kPlocTile) * (kPlocThreads / 32) * kPlocRounds;
+  // (smaller tiles in late iterations: at most one partial tile's worth more; never more tiles
+  // than the grid, so desc_words holds their totals)
+  size_t flag_words = (size_t)div_up(cap, kPlocTile) * (kPlocThreads / 32) * kPlocRounds +
+                      (kPlocThreads / 32) * kPlocRounds;
   if ((e = cudaMalloc(&ws.nbr, (size_t)cap * 4 + desc_words * 8 + flag_words * 8 + 64)) != cudaSuccess) return e;
   ws.ploc_cap = cap;
   return cudaSuccess;
