@@ -250,8 +250,35 @@ def cpu_baseline(name, mesh, budget_s=12.0):
         if time.perf_counter() - t0 > budget_s or reps >= 20:
             break
     dt = (time.perf_counter() - t0) / reps
-    return {"value": round(n_sample / dt / 1e6, 3), "unit": "Mtris/s", "cores": cores, "kind": "port",
-            "sample": f"first {n_sample:,} triangles of the workload, {reps} builds, oracle/bvh_oracle.c (OpenMP)"}
+    out = {"value": round(n_sample / dt / 1e6, 3), "unit": "Mtris/s", "cores": cores, "kind": "port",
+           "sample": f"first {n_sample:,} triangles of the workload, {reps} builds, oracle/bvh_oracle.c (OpenMP)"}
+    # the same build on one thread (a smaller sample), and the host evaluator (SAH + depth
+    # statistics, single-threaded as BVHEvaluator is) on an LBVH of the sample
+    n1 = min(n_sample, 250_000)
+    a1 = [a[:n1] for a in arrays]
+    try:
+        O.set_threads(1)
+        t1 = time.perf_counter()
+        if algo == "ploc":
+            O.ploc(a1, radius)
+        elif algo == "lbvh_plus":
+            O.lbvh_plus(a1, bits, treelet_rounds(name))
+        else:
+            O.lbvh(a1, bits)
+        dt1 = time.perf_counter() - t1
+    finally:
+        O.set_threads(cores)
+    out["one_thread"] = {"value": round(n1 / dt1 / 1e6, 3), "unit": "Mtris/s", "cores": 1,
+                         "sample": f"first {n1:,} triangles, 1 build"}
+    nodes, _, _ = O.lbvh(arrays, 30)
+    t2 = time.perf_counter()
+    O.sah(nodes)
+    O.depth_stats(nodes)
+    dt2 = time.perf_counter() - t2
+    out["evaluator"] = {"ms": round(dt2 * 1e3, 2), "nodes": int(nodes.shape[0]), "cores": 1,
+                        "what": "SAH + depth statistics (the restatement of BVHEvaluator, pinned bit-equal to it) "
+                                f"over an LBVH-30 of the first {n_sample:,} triangles"}
+    return out
 
 
 def run_ours(args):
