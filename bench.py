@@ -364,7 +364,10 @@ def run_ours(args):
                 "traffic_source": measured[1] if measured else "no capture of this stage at this workload",
                 "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": round(per_unit, 2),
                 "whole_build": {"bytes_per_tri": round(whole, 2), "achieved": round(build_gbs, 1),
-                                "frac": round(build_gbs / peak, 4), "median_build_ms": round(med[5], 4)}}
+                                "frac": round(build_gbs / peak, 4), "median_build_ms": round(med[5], 4)},
+                # secondary: the compulsory input and output alone (36 B in, 2 x 48 B nodes, 4 B index)
+                "io_floor": {"bytes_per_tri": 136, "achieved": round(136.0 * n / (med[5] / 1e3) / 1e9, 1),
+                             "frac": round(136.0 * n / (med[5] / 1e3) / 1e9 / peak, 4)}}
     if algo == "ploc":
         roofline["ploc"] = {"iterations": ploc_iters, "cluster_sum": ploc_csum}
     stage_ms = {k: round(v, 4) for k, v in shares.items()}
