@@ -53,6 +53,14 @@ WORKLOADS = {
                      "1,310,720-triangle displaced icosphere (0.05 fBm), LBVH+ 60-bit, 1 treelet pass"),
     "c2b_ploc25": ("strands", {"n_strands": 20000, "segments": 100, "seed": 3}, "ploc", 30, 25,
                    "2,000,000 thin triangles on 20,000 random-walk strands, PLOC radius 25"),
+    "c2a_ploc10": ("icosphere", {"levels": 8, "seed": 2}, "ploc", 30, 10,
+                   "1,310,720-triangle displaced icosphere (0.05 fBm), PLOC radius 10"),
+    "c2a_ploc100": ("icosphere", {"levels": 8, "seed": 2}, "ploc", 30, 100,
+                    "1,310,720-triangle displaced icosphere (0.05 fBm), PLOC radius 100"),
+    "c2b_ploc10": ("strands", {"n_strands": 20000, "segments": 100, "seed": 3}, "ploc", 30, 10,
+                   "2,000,000 thin triangles on 20,000 random-walk strands, PLOC radius 10"),
+    "c2b_ploc100": ("strands", {"n_strands": 20000, "segments": 100, "seed": 3}, "ploc", 30, 100,
+                    "2,000,000 thin triangles on 20,000 random-walk strands, PLOC radius 100"),
     "c2b_lbvhplus": ("strands", {"n_strands": 20000, "segments": 100, "seed": 3}, "lbvh_plus", 60, 0,
                      "2,000,000 thin triangles on 20,000 random-walk strands, LBVH+ 60-bit, 1 treelet pass"),
     "c3_batched": ("batch", {"meshes": 4096, "lo": 64, "hi": 262144}, "lbvh_batched", 30, 0,
@@ -286,7 +294,7 @@ def run_ours(args):
     import torch.distributed as dist
 
     import bvh_gb300
-    from bvh_gb300 import _capi as C
+    from bvh_gb300 import _capi as C, meshgen
 
     ws, rank, local = dist_info()
     if ws > 1:
@@ -399,6 +407,26 @@ def run_ours(args):
                         "trace_ms": round(tr_ms, 3), "trace_mrays_per_s": round(W * Hh / (tr_ms / 1e3) / 1e6, 1)})
         quality["sah"] = round(quality["sah"], 3)
         quality["avg_leaf_depth"] = round(quality["avg_leaf_depth"], 3)
+        if gen in ("icosphere", "strands"):
+            # surface-like meshes: 1M rays from a sphere around the mesh toward points in its box
+            ro, rd = meshgen.sphere_rays(mesh, 1_000_000, seed=7)
+            nr = ro.shape[0]
+            rays = [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                    for a in (ro[:, 0], ro[:, 1], ro[:, 2], rd[:, 0], rd[:, 1], rd[:, 2])]
+            sh = [torch.empty(nr, dtype=torch.float32, device=dev)] + \
+                 [torch.empty(nr, dtype=torch.int32, device=dev) for _ in range(4)]
+            rp, shp = [r.data_ptr() for r in rays], [h.data_ptr() for h in sh]
+            ctx.trace(tree.nodes, tree.n_nodes, ptrs, n, rp, nr, shp, s)
+            e0.record(stream)
+            for _ in range(3):
+                ctx.trace(tree.nodes, tree.n_nodes, ptrs, n, rp, nr, shp, s)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            sr_ms = e0.elapsed_time(e1) / 3
+            quality["sphere_rays"] = {"rays": nr, "avg_nodes_visited": round(float(sh[2].double().mean()), 3),
+                                      "hit_fraction": round(float((sh[1] >= 0).double().mean()), 4),
+                                      "trace_ms": round(sr_ms, 3),
+                                      "trace_mrays_per_s": round(nr / (sr_ms / 1e3) / 1e6, 1)}
 
     # --- end to end through the C ABI with pinned host buffers ----------------------------
     h_in = [torch.from_numpy(a).pin_memory() for a in mesh.arrays()]
