@@ -153,6 +153,20 @@ __global__ void __launch_bounds__(256, 4) k_fixrun_split_short(const uint32_t* _
   const uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
   unsigned long long hw[8];
   uint32_t v[8];
+  // one round trip: this thread's 4 keys and values; lane 31 also the next thread's 4 (the
+  // window's other half comes from the next lane), lane 0 the key before
+  unsigned long long edge_h[4] = {kNoH, kNoH, kNoH, kNoH};
+  uint32_t edge_v[4] = {0u, 0u, 0u, 0u};
+  unsigned long long hprev = kNoH;
+  if (lane == 31) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (p0 + 4 + j < n) {
+        edge_h[j] = hkeys[p0 + 4 + j];
+        edge_v[j] = vals[p0 + 4 + j];
+      }
+  }
+  if (lane == 0 && p0 > 0 && p0 - 1 < n) hprev = hkeys[p0 - 1];
   if (p0 + 4 <= n) {
     const uint4 a = *reinterpret_cast<const uint4*>(hkeys + p0);
     const uint4 c = *reinterpret_cast<const uint4*>(vals + p0);
@@ -179,31 +193,51 @@ __global__ void __launch_bounds__(256, 4) k_fixrun_split_short(const uint32_t* _
   if (lane == 31) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      hw[4 + j] = p0 + 4 + j < n ? (unsigned long long)hkeys[p0 + 4 + j] : kNoH;
-      v[4 + j] = p0 + 4 + j < n ? vals[p0 + 4 + j] : 0u;
+      hw[4 + j] = edge_h[j];
+      v[4 + j] = edge_v[j];
     }
   }
-  unsigned long long hprev = __shfl_up_sync(0xffffffffu, hw[3], 1);
-  if (lane == 0) hprev = (p0 > 0 && p0 - 1 < n) ? (unsigned long long)hkeys[p0 - 1] : kNoH;
+  {
+    const unsigned long long up = __shfl_up_sync(0xffffffffu, hw[3], 1);
+    if (lane != 0) hprev = up;
+  }
   if (DELTA) {
 #pragma unroll
     for (int j = 0; j < 4; ++j)
       if (p0 + j + 1 < n && hw[j] != hw[j + 1]) D[p0 + j] = delta_hi((uint32_t)hw[j], (uint32_t)hw[j + 1], lbits);
   }
+  // runs of 2+ equal high halves that start in this thread's positions: their lengths in the
+  // window (a run reaching the window's end may be longer: checked against position p0 + 8)
+  int rlen[4];
+  uint32_t need = 0;  // window slots whose low halves the runs read
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const unsigned long long hp = j == 0 ? hprev : hw[j - 1];
+    rlen[j] = 0;
     if (hw[j] == kNoH || hw[j] == hp || hw[j] != hw[j + 1]) continue;  // not the start of a run of 2+
-    const uint32_t s = p0 + j;
     int m = 2;
 #pragma unroll
     for (int q = j + 2; q < 8; ++q) m += (m == q - j && hw[q] == hw[j]) ? 1 : 0;
-    if (j + m == 8 && p0 + 8 < n && (unsigned long long)hkeys[p0 + 8] == hw[j]) {
+    rlen[j] = m;
+    need |= ((1u << m) - 1u) << j;
+  }
+  const bool at_end = ((need >> 7) & 1u) && p0 + 8 < n;
+  const unsigned long long h8 = at_end ? (unsigned long long)hkeys[p0 + 8] : kNoH;
+  // all needed low halves in one batch, before any store of this thread
+  uint32_t lw[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) lw[i] = ((need >> i) & 1u) ? __ldg(lows + v[i]) : 0u;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int m = rlen[j];
+    if (m == 0) continue;
+    const uint32_t s = p0 + j;
+    if (j + m == 8 && p0 + 8 < n && h8 == hw[j]) {
       long_list[atomicAdd(long_count, 1u)] = s;
       continue;
     }
     if (m == 2) {  // the common case: swap when out of order
-      const uint32_t la = __ldg(lows + v[j]), lb = __ldg(lows + v[j + 1]);
+      const uint32_t la = lw[j], lb = lw[j + 1];
       if (la > lb) {
         vals[s] = v[j + 1];
         vals[s + 1] = v[j];
@@ -213,7 +247,7 @@ __global__ void __launch_bounds__(256, 4) k_fixrun_split_short(const uint32_t* _
     }
     unsigned long long w[8];  // L in the window slots of the run (positions order the ties)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) w[i] = (i >= j && i < j + m) ? (unsigned long long)__ldg(lows + v[i]) : 0ull;
+    for (int i = 0; i < 8; ++i) w[i] = (i >= j && i < j + m) ? (unsigned long long)lw[i] : 0ull;
     uint32_t rk[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
