@@ -6,6 +6,8 @@
     its Release flags (-O3 --use_fast_math, CMakeLists.txt:41-45).
   - libref_eval.so: the reference's src/evaluator.cpp with ref_eval_shim.cpp (host only).
   - libref_loader.so: the reference's src/loader.cpp with ref_loader_shim.cpp (host only).
+  - libref_render_host.so: the reference's src/render_engine.cu, included by ref_render_shim.cu,
+    for its host post-processing (heatmap colormap, PPM bytes); used by CPU tests only.
 * Anywhere (GPU machine included): libref_runner.so from ref_runner.cu (our host code that loads the
   fatbins and replays the reference builders with CUB/Thrust).
 """
@@ -69,6 +71,13 @@ def build_loader():
           "-o", os.path.join(OUT, "libref_loader.so")])
 
 
+def build_render_host():
+    _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                             "-I" + os.path.join(REF_ROOT, "include"), "-I" + os.path.join(REF_ROOT, "src"),
+                             os.path.join(HERE, "ref_render_shim.cu"),
+                             "-o", os.path.join(OUT, "libref_render_host.so")])
+
+
 def build_runner():
     _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
                              os.path.join(HERE, "ref_runner.cu"), "-o", os.path.join(OUT, "libref_runner.so"),
@@ -85,6 +94,7 @@ def build(runner: bool = True):
         build_fatbins()
         build_eval()
         build_loader()
+        build_render_host()
     if runner and fatbins_present():
         build_runner()
 
