@@ -96,7 +96,10 @@ def bytes_per_tri(algo: str, bits: int, rounds: int = 0, cluster_sum_per_tri: fl
 
 
 def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, cluster_sum_per_tri: float = 0.0):
-    """Algorithmic bytes per triangle of one build stage (the split of B(K) above)."""
+    """Algorithmic bytes per triangle of one build stage: the split of B(K) above, except that the
+    Morton stage also counts the 32-byte triangle box it writes for the emission's gather (B(K)
+    counts that gather as 36 bytes of vertices inside the emission stage, as this split does too),
+    so the LBVH stages sum to B(K) + 32."""
     kb = 4 if bits == 30 else 8
     d = (bits + 7) // 8
     if stage == "scene_bounds":

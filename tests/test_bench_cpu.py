@@ -1,0 +1,41 @@
+"""bench.py's accounting: algorithmic bytes per triangle (the whole-build formula and its split by
+stage), launches per build, treelet passes per workload."""
+import pytest
+
+import bench
+
+
+@pytest.mark.parametrize("algo,bits,rounds,expected", [("lbvh", 30, 0, 352), ("lbvh", 60, 0, 492),
+                                                        ("lbvh", 63, 0, 492), ("lbvh_plus", 60, 1, 636),
+                                                        ("lbvh_plus", 60, 3, 924)])
+def test_whole_build_bytes(algo, bits, rounds, expected):
+    # LBVH: 276 + 3 kb + 2 D (kb + 4); LBVH+: B(60) + 144 per treelet pass (3 passes: 492 + 432)
+    assert bench.bytes_per_tri(algo, bits, rounds) == expected
+
+
+@pytest.mark.parametrize("bits", [30, 60, 63])
+def test_stage_split_sums_to_the_whole_build_plus_the_box_write(bits):
+    stages = ["scene_bounds", "morton_boxes_hist", "onesweep_sort", "emit_refit"]
+    total = sum(bench.stage_bytes_per_tri(s, "lbvh", bits) for s in stages)
+    assert total == bench.bytes_per_tri("lbvh", bits) + 32
+    plus = total + bench.stage_bytes_per_tri("treelet_or_ploc_loop", "lbvh_plus", bits, 3)
+    assert plus == bench.bytes_per_tri("lbvh_plus", bits, 3) + 32
+
+
+def test_ploc_bytes_follow_the_cluster_sum():
+    assert bench.bytes_per_tri("ploc", 30, cluster_sum_per_tri=9.84) == pytest.approx(264 + 160 * 9.84)
+    assert bench.stage_bytes_per_tri("treelet_or_ploc_loop", "ploc", 30, cluster_sum_per_tri=2.0) == 320
+
+
+def test_launches_per_build():
+    assert bench.kernels_per_build("lbvh", 63) == 10
+    assert bench.kernels_per_build("lbvh", 30) == 8
+    assert bench.kernels_per_build("lbvh_plus", 60, rounds=1, tree_height=40) == 10 + 5 + 3 * 40
+    assert bench.kernels_per_build("ploc", 30, ploc_iterations=103) == 8 + 4 * 103
+
+
+def test_treelet_passes_per_workload():
+    assert bench.treelet_rounds("c1_lbvhplus3") == 3
+    assert bench.treelet_rounds("c1_lbvhplus") == 1
+    assert bench.treelet_rounds("c1_lbvh63") == 0
+    assert bench.treelet_rounds("c1_ploc25") == 0
