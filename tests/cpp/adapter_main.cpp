@@ -21,7 +21,8 @@ int main(int argc, char** argv) {
     mesh.v1x[i] = x + 0.004f; mesh.v1y[i] = y; mesh.v1z[i] = z;
     mesh.v2x[i] = x; mesh.v2y[i] = y + 0.004f; mesh.v2z[i] = z + 0.002f;
   }
-  Gb300LBVHBuilder lbvh;
+  try {
+  Gb300LBVHBuilder lbvh;  // constructors throw when no context can be created (no GPU)
   Gb300LBVHPlusBuilder plus;
   Gb300PLOCBuilder ploc(25);
   BVHBuilder* builders[] = {&lbvh, &plus, &ploc};
@@ -48,6 +49,10 @@ int main(int argc, char** argv) {
       printf("%s error: %s\n", b->getName().c_str(), e.what());
       return 1;
     }
+  }
+  } catch (const std::exception& e) {
+    printf("error: %s\n", e.what());
+    return 1;
   }
   return 0;
 }
