@@ -3,7 +3,7 @@
 // Pipeline (one stream, no host synchronisation):
 //   k_bounds      scene AABB of all triangles (reference: kComputeBoundsAndCentroids_nt +
 //                 kReduceBounds_Step1/2_nt, src/cuda/lbvh_builder.cu:47-165), also zeroes the
-//                 sort scratch for this build.
+//                 sort scratch the current build uses.
 //   k_morton      per-triangle AABB (kept for the leaves), centroid, Morton code
 //                 (kComputeMortonCodes_nt :167-181 / kComputeMortonCodes_P, lbvh_plus_builder.cu:276-290)
 //                 and the digit histograms of every radix pass.
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) k_bounds(MeshPtrs m, uint32_t n, int vec4
                                                 ScratchLayout L) {
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t gsz = gridDim.x * blockDim.x;
-  // zero this build's histograms, tile counters and look-back descriptors
+  // zero the current build's histograms, tile counters and look-back descriptors
   {
     uint4* z = reinterpret_cast<uint4*>(scratch + L.zero_begin);
     size_t words4 = (L.zero_end - L.zero_begin) / 4;
@@ -611,7 +611,7 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
                                const ScratchLayout& L, int* final_buf) {
   uint32_t* lows = sizeof(K) == 8 ? split_lows(ws) : nullptr;
   const int vec4 = all_aligned16(m) && (reinterpret_cast<uintptr_t>(lows) & 15) == 0 ? 1 : 0;
-  // zero only the descriptors this build's passes use (the passes sort 32-bit keys)
+  // zero only the descriptors the current build's passes use (the passes sort 32-bit keys)
   ScratchLayout Lz = L;
   Lz.zero_end = L.desc + (size_t)4 * div_up(std::max<uint32_t>(n, 1),
                                              (uint32_t)sort_variant_tile(ws.sort_variant)) * 256;

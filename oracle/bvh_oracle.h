@@ -1,7 +1,7 @@
 /*
  * bvh_oracle.h -- CPU restatement of the reference BVH builders (TEST INFRASTRUCTURE).
  *
- * This library is the checker for the GPU library in bvh_gb300/: only the tests, the
+ * The tests compare the GPU library in bvh_gb300/ against this library: only the tests, the
  * smoke check and bench.py's CPU-baseline leg call it.  It is never linked into, or
  * called by, the product path.
  *

@@ -8,7 +8,7 @@
   - libref_loader.so: the reference's src/loader.cpp with ref_loader_shim.cpp (host only).
   - libref_render_host.so: the reference's src/render_engine.cu, included by ref_render_shim.cu,
     for its host post-processing (heatmap colormap, PPM bytes); used by CPU tests only.
-* Anywhere (GPU machine included): libref_runner.so from ref_runner.cu (our host code that loads the
+* Anywhere (GPU machines included): libref_runner.so from ref_runner.cu (our host code that loads the
   fatbins and replays the reference builders with CUB/Thrust).
 """
 from __future__ import annotations
