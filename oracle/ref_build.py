@@ -41,6 +41,14 @@ def _run(cmd):
         raise RuntimeError(" ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
+def _fresh(out, *inputs):
+    """True when `out` exists and is newer than every input (then its build step is skipped)."""
+    if not os.path.exists(out):
+        return False
+    t = os.path.getmtime(out)
+    return all(os.path.getmtime(i) <= t for i in inputs if os.path.exists(i))
+
+
 def have_reference() -> bool:
     return os.path.isdir(os.path.join(REF_ROOT, "src", "cuda"))
 
@@ -50,14 +58,20 @@ def build_fatbins():
     inc = ["-I" + os.path.join(REF_ROOT, "include")]
     for name, rel in FATBINS.items():
         src = os.path.join(REF_ROOT, rel)
-        jobs.append([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17"] + inc + [src, "-o", os.path.join(OUT, name + ".fatbin")])
-        jobs.append([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17", "-O3", "--use_fast_math"] + inc
-                    + [src, "-o", os.path.join(OUT, name + "_fast.fatbin")])
+        out, out_fast = os.path.join(OUT, name + ".fatbin"), os.path.join(OUT, name + "_fast.fatbin")
+        if not _fresh(out, src):
+            jobs.append([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17"] + inc + [src, "-o", out])
+        if not _fresh(out_fast, src):
+            jobs.append([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17", "-O3", "--use_fast_math"] + inc
+                        + [src, "-o", out_fast])
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(_run, jobs))
 
 
 def build_eval():
+    if _fresh(os.path.join(OUT, "libref_eval.so"), os.path.join(HERE, "ref_eval_shim.cpp"),
+              os.path.join(REF_ROOT, "src", "evaluator.cpp")):
+        return
     _run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
           "-I" + os.path.join(REF_ROOT, "include"), "-I/usr/local/cuda/include",
           os.path.join(HERE, "ref_eval_shim.cpp"), os.path.join(REF_ROOT, "src", "evaluator.cpp"),
@@ -65,6 +79,9 @@ def build_eval():
 
 
 def build_loader():
+    if _fresh(os.path.join(OUT, "libref_loader.so"), os.path.join(HERE, "ref_loader_shim.cpp"),
+              os.path.join(REF_ROOT, "src", "loader.cpp")):
+        return
     _run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC",
           "-I" + os.path.join(REF_ROOT, "include"), "-I/usr/local/cuda/include",
           os.path.join(HERE, "ref_loader_shim.cpp"), os.path.join(REF_ROOT, "src", "loader.cpp"),
@@ -72,6 +89,9 @@ def build_loader():
 
 
 def build_render_host():
+    if _fresh(os.path.join(OUT, "libref_render_host.so"), os.path.join(HERE, "ref_render_shim.cu"),
+              os.path.join(REF_ROOT, "src", "render_engine.cu")):
+        return
     _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off",
                              "-I" + os.path.join(REF_ROOT, "include"), "-I" + os.path.join(REF_ROOT, "src"),
                              os.path.join(HERE, "ref_render_shim.cu"),
@@ -79,6 +99,8 @@ def build_render_host():
 
 
 def build_runner():
+    if _fresh(os.path.join(OUT, "libref_runner.so"), os.path.join(HERE, "ref_runner.cu")):
+        return
     _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
                              os.path.join(HERE, "ref_runner.cu"), "-o", os.path.join(OUT, "libref_runner.so"),
                              "-lcuda"])
