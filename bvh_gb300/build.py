@@ -3,7 +3,9 @@
 Translation units are compiled in parallel and linked into bvh_gb300/libbvh_gb300.so.
 Device arithmetic is compiled with -fmad=false and host code with -ffp-contract=off, so every
 float operation rounds as written (the kernels use explicit FMAs where the reference's
-compiled code has them).
+compiled code has them).  trace.cu is the exception: it keeps nvcc's default -fmad=true so that
+the device tanf it calls (generateRay's tan(fov/2)) is compiled as the reference's is; every
+float operation written in that file is an explicitly rounded intrinsic, which is never fused.
 """
 from __future__ import annotations
 
@@ -20,8 +22,9 @@ OBJ_DIR = os.path.join(HERE, "_build")
 
 SOURCES = ["lbvh.cu", "treelet.cu", "ploc.cu", "trace.cu", "batched.cu", "capi.cu", "noalloc.cu", "serve.cu", "evaluate.cu", "fixrun.cu", "objload.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
               "--expt-relaxed-constexpr"]
+FMAD = {"trace.cu": "-fmad=true"}  # every other translation unit: -fmad=false
 
 
 def nvcc() -> str:
@@ -33,7 +36,8 @@ def nvcc() -> str:
 
 def _compile(src: str, extra) -> str:
     obj = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + list(extra) + ["-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + [FMAD.get(src, "-fmad=false")] + list(extra) + ["-c", os.path.join(CSRC, src),
+                                                                                         "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
@@ -67,7 +71,8 @@ def build_library(force: bool = False, extra=(), verbose: bool = False) -> str:
 
 def ptxas_report(src: str = "lbvh.cu") -> str:
     """Registers / spills / shared memory per kernel (-Xptxas -v)."""
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", os.devnull]
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + [FMAD.get(src, "-fmad=false"), "-Xptxas", "-v", "-c", os.path.join(CSRC, src),
+                                          "-o", os.devnull]
     r = subprocess.run(cmd, capture_output=True, text=True)
     return r.stdout + r.stderr
 

@@ -235,6 +235,14 @@ def load_obj(path: str, threads: int = 0) -> "TriangleMesh":
     return TriangleMesh(*arrays)
 
 
+def pinhole_rays(cam: C.Camera, width: int, height: int, ray_ptrs: Sequence[int], stream: int = 0):
+    """generateRay (src/render_engine.cu:155-188) for every pixel into six device arrays
+    (origin xyz, direction xyz; width * height floats each, row-major) -- bvh_pinhole_rays."""
+    lib = C.load_library()
+    C.check(lib.bvh_pinhole_rays(ctypes.byref(cam), width, height, *[ctypes.c_void_p(p) for p in ray_ptrs],
+                                 ctypes.c_void_p(stream)), "bvh_pinhole_rays")
+
+
 def auto_camera(root_node) -> C.Camera:
     """autoCamera (src/render_engine.cu:601-637) from a host root node (NODE_DTYPE record) or None."""
     lib = C.load_library()

@@ -562,29 +562,12 @@ extern "C" bvh_status bvh_trace(bvh_ctx* ctx, const bvh_node* nodes, uint32_t n_
                               rays->n, ho, reinterpret_cast<cudaStream_t>(stream)));
 }
 
-// Camera basis exactly as the CPU oracle computes it (orc_pinhole_rays): float arithmetic,
-// tan(fov/2) in double.  This file's host code is compiled with -ffp-contract=off.
-static void normalize3(float v[3]) {
-  float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
-  if (len < 1e-12f) { v[0] = v[1] = v[2] = 0.0f; return; }
-  float inv = 1.0f / len;
-  v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
-}
-
-static bool make_basis(const bvh_camera* cam, int32_t w, int32_t h, PinholeBasis* b) {
+// The camera as the kernels take it; generateRay's basis is derived on the device, per ray.
+static bool make_cam(const bvh_camera* cam, int32_t w, int32_t h, PinholeCam* b) {
   if (!cam || w <= 0 || h <= 0) return false;
   if ((uint64_t)w * (uint64_t)h > 0xffffffffull) return false;
-  float f[3] = {cam->look_at[0] - cam->eye[0], cam->look_at[1] - cam->eye[1], cam->look_at[2] - cam->eye[2]};
-  normalize3(f);
-  const float* up = cam->up;
-  float r[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
-  normalize3(r);
-  float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
-  float half_h = (float)tan((double)(cam->fov_y_deg * 3.14159265358979f / 180.0f) * 0.5);
-  float half_w = half_h * ((float)w / (float)h);
-  for (int k = 0; k < 3; ++k) { b->eye[k] = cam->eye[k]; b->f[k] = f[k]; b->r[k] = r[k]; b->u[k] = u[k]; }
-  b->half_w = half_w;
-  b->half_h = half_h;
+  for (int k = 0; k < 3; ++k) { b->eye[k] = cam->eye[k]; b->look[k] = cam->look_at[k]; b->up[k] = cam->up[k]; }
+  b->fov_deg = cam->fov_y_deg;
   b->width = w;
   b->height = h;
   return true;
@@ -597,8 +580,8 @@ extern "C" bvh_status bvh_trace_pinhole(bvh_ctx* ctx, const bvh_node* nodes, uin
   if (!hits->t || !hits->prim || !hits->nodes_visited || !hits->aabb_tests || !hits->tri_tests)
     return BVH_ERR_INVALID_ARG;
   if (n_nodes > 0 && !nodes) return BVH_ERR_INVALID_ARG;
-  PinholeBasis b;
-  if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
+  PinholeCam b;
+  if (!make_cam(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
   HitOut ho{hits->t, hits->prim, hits->nodes_visited, hits->aabb_tests, hits->tri_tests};
   return from_cuda(trace_pinhole(reinterpret_cast<const Node*>(nodes), (int)n_nodes, mesh_ptrs(mesh), mesh->n, b, ho,
@@ -607,8 +590,8 @@ extern "C" bvh_status bvh_trace_pinhole(bvh_ctx* ctx, const bvh_node* nodes, uin
 
 extern "C" bvh_status bvh_pinhole_rays(const bvh_camera* cam, int32_t width, int32_t height, float* ox, float* oy,
                                        float* oz, float* dx, float* dy, float* dz, void* stream) {
-  PinholeBasis b;
-  if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
+  PinholeCam b;
+  if (!make_cam(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
   if (!ox || !oy || !oz || !dx || !dy || !dz) return BVH_ERR_INVALID_ARG;
   return from_cuda(pinhole_rays(b, ox, oy, oz, dx, dy, dz, reinterpret_cast<cudaStream_t>(stream)));
 }
@@ -618,8 +601,8 @@ extern "C" bvh_status bvh_shade(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bv
                                 const float* light_dir, float* rgb, void* stream) {
   if (!ctx || !mesh_ok(mesh) || !hits || !hits->t || !hits->prim || !hits->nodes_visited || !rgb || !light_dir)
     return BVH_ERR_INVALID_ARG;
-  PinholeBasis b;
-  if (!make_basis(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
+  PinholeCam b;
+  if (!make_cam(cam, width, height, &b)) return BVH_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
   ShadeIn in{hits->t, hits->prim, hits->nodes_visited};
   return from_cuda(shade_pixels(b, mesh_ptrs(mesh), mesh->n, in, mode, scene_diag,
@@ -660,7 +643,7 @@ extern "C" bvh_status bvh_auto_camera(const bvh_node* root, bvh_camera* cam) {
   float diag = sqrtf((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2]);
   if (diag < 1e-6f) diag = 2.0f;
   float fov = cam->fov_y_deg * 3.14159265358979f / 180.0f;
-  float dist = (diag * 0.5f) / (float)tan((double)(fov * 0.5f)) * 1.2f;
+  float dist = (diag * 0.5f) / tanf(fov * 0.5f) * 1.2f;
   cam->eye[0] = c[0] + dist * 0.6f;
   cam->eye[1] = c[1] + dist * 0.3f;
   cam->eye[2] = c[2] + dist * 0.7f;

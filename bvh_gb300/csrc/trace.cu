@@ -3,8 +3,17 @@
 // Reference: traverseBVH (src/render_engine.cu:289-356) with intersectAABB (:194-214),
 // intersectTriangle (:220-273) and generateRay (:155-188).  Same visiting order (left child
 // first, 128-entry stack that silently drops pushes when full), same counters (a node counts as
-// visited before its box test), same closest-hit rule (strict <).  Every float operation is an
-// explicitly rounded intrinsic so that the CPU oracle reproduces the results bit for bit.
+// visited before its box test), same closest-hit rule (strict <).
+//
+// Rounding: every float operation is an explicitly rounded intrinsic, in the form nvcc gives the
+// reference's expressions under its default -fmad=true.  A two-product difference a*b - c*d is
+// fma(a, b, -(c*d)); a three-term dot product (a.x*b.x + a.y*b.y) + a.z*b.z is
+// fma(a.z, b.z, fma(a.x, b.x, a.y*b.y)); x + a*b is fma(a, b, x).  (The left product of a sum is
+// fused first, and a sum whose left operand is already fused takes the right product into a second
+// fma.)  Expressions with a division or subtraction between the multiply and the add
+// ((lo - o) * inv, (2(x + 0.5)/w - 1) * half_w) have nothing to contract.  The forms are pinned
+// against the reference's own traverseBVH and generateRay on the same rays.  The CPU oracle uses
+// the same forms (C fmaf), so it reproduces t, hit ids and counters bit for bit.
 #include <algorithm>
 
 #include "lbvh.cuh"
@@ -24,11 +33,13 @@ __device__ __forceinline__ bool hit_box(const float3 o, const float3 inv, const 
   return texit >= fmaxf(tenter, 0.0f) && tenter < tmax;
 }
 
+// d_dot (:122-124): (a*x + b*y) + c*z, contracted.
 __device__ __forceinline__ float dot3(float a, float b, float c, float x, float y, float z) {
-  return __fadd_rn(__fadd_rn(__fmul_rn(a, x), __fmul_rn(b, y)), __fmul_rn(c, z));
+  return __fmaf_rn(c, z, __fmaf_rn(a, x, __fmul_rn(b, y)));
 }
-__device__ __forceinline__ float cross_c(float a, float b, float c, float d) {  // a*b - c*d
-  return __fsub_rn(__fmul_rn(a, b), __fmul_rn(c, d));
+// a*b - c*d, contracted (d_cross :114-120 and the edge products of intersectTriangle).
+__device__ __forceinline__ float cross_c(float a, float b, float c, float d) {
+  return __fmaf_rn(a, b, -__fmul_rn(c, d));
 }
 
 __device__ __forceinline__ bool hit_tri(const float3 o, const float3 d, const MeshPtrs& m, uint32_t p, float& t_out) {
@@ -105,21 +116,35 @@ __global__ void __launch_bounds__(128) k_trace(const Node* __restrict__ nodes, i
   trace_one(o, d, nodes, n_nodes, m, n_tris, r, out);
 }
 
-// generateRay (src/render_engine.cu:155-188) per pixel from a host-computed basis.
-__device__ __forceinline__ float3 pinhole_dir(const PinholeBasis& c, int x, int y) {
-  const float uu = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn((float)x, 0.5f)), (float)c.width), 1.0f), c.half_w);
-  const float vv = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn((float)y, 0.5f)), (float)c.height), 1.0f), c.half_h);
-  float dx = __fsub_rn(__fadd_rn(c.f[0], __fmul_rn(uu, c.r[0])), __fmul_rn(vv, c.u[0]));
-  float dy = __fsub_rn(__fadd_rn(c.f[1], __fmul_rn(uu, c.r[1])), __fmul_rn(vv, c.u[1]));
-  float dz = __fsub_rn(__fadd_rn(c.f[2], __fmul_rn(uu, c.r[2])), __fmul_rn(vv, c.u[2]));
-  const float len = __fsqrt_rn(dot3(dx, dy, dz, dx, dy, dz));
+// d_normalize (:130-135): zero below length 1e-12, else each component times 1 / length.
+__device__ __forceinline__ float3 normalize3(float x, float y, float z) {
+  const float len = __fsqrt_rn(dot3(x, y, z, x, y, z));
   if (len < 1e-12f) return make_float3(0.f, 0.f, 0.f);
   const float inv = __fdiv_rn(1.0f, len);
-  return make_float3(__fmul_rn(dx, inv), __fmul_rn(dy, inv), __fmul_rn(dz, inv));
+  return make_float3(__fmul_rn(x, inv), __fmul_rn(y, inv), __fmul_rn(z, inv));
+}
+
+// generateRay (:155-188) for pixel (x, y): the camera basis and tan(fov/2) are computed per ray,
+// as the reference does, with the device's own tanf.
+__device__ __forceinline__ float3 pinhole_dir(const PinholeCam& c, int x, int y) {
+  const float3 f = normalize3(__fsub_rn(c.look[0], c.eye[0]), __fsub_rn(c.look[1], c.eye[1]),
+                              __fsub_rn(c.look[2], c.eye[2]));
+  const float3 rt = normalize3(cross_c(f.y, c.up[2], f.z, c.up[1]), cross_c(f.z, c.up[0], f.x, c.up[2]),
+                               cross_c(f.x, c.up[1], f.y, c.up[0]));
+  const float3 up = make_float3(cross_c(rt.y, f.z, rt.z, f.y), cross_c(rt.z, f.x, rt.x, f.z),
+                                cross_c(rt.x, f.y, rt.y, f.x));
+  const float fov = __fdiv_rn(__fmul_rn(c.fov_deg, 3.14159265358979f), 180.0f);
+  const float half_h = tanf(__fmul_rn(fov, 0.5f));
+  const float half_w = __fmul_rn(half_h, __fdiv_rn((float)c.width, (float)c.height));
+  const float uu = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn((float)x, 0.5f)), (float)c.width), 1.0f), half_w);
+  const float vv = __fmul_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn((float)y, 0.5f)), (float)c.height), 1.0f), half_h);
+  // forward + u*right - v*up, contracted: fma(-v, up, fma(u, right, forward))
+  return normalize3(__fmaf_rn(-vv, up.x, __fmaf_rn(uu, rt.x, f.x)), __fmaf_rn(-vv, up.y, __fmaf_rn(uu, rt.y, f.y)),
+                    __fmaf_rn(-vv, up.z, __fmaf_rn(uu, rt.z, f.z)));
 }
 
 __global__ void __launch_bounds__(128) k_trace_pinhole(const Node* __restrict__ nodes, int n_nodes, MeshPtrs m,
-                                                       uint32_t n_tris, PinholeBasis cam, HitOut out) {
+                                                       uint32_t n_tris, PinholeCam cam, HitOut out) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
   if (r >= total) return;
@@ -128,7 +153,7 @@ __global__ void __launch_bounds__(128) k_trace_pinhole(const Node* __restrict__ 
   trace_one(o, pinhole_dir(cam, x, y), nodes, n_nodes, m, n_tris, r, out);
 }
 
-__global__ void k_pinhole_rays(PinholeBasis cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz) {
+__global__ void k_pinhole_rays(PinholeCam cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
   if (r >= total) return;
@@ -145,14 +170,6 @@ __global__ void k_pinhole_rays(PinholeBasis cam, float* ox, float* oy, float* oz
 // ---------------------------------------------------------------------------------------
 constexpr float kBgR = 0.15f, kBgG = 0.15f, kBgB = 0.18f;  // a pixel without a hit (BG_R/G/B)
 
-// d_normalize (:130-135): zero below length 1e-12, else each component times 1 / length.
-__device__ __forceinline__ float3 normalize3(float x, float y, float z) {
-  const float len = __fsqrt_rn(dot3(x, y, z, x, y, z));
-  if (len < 1e-12f) return make_float3(0.f, 0.f, 0.f);
-  const float inv = __fdiv_rn(1.0f, len);
-  return make_float3(__fmul_rn(x, inv), __fmul_rn(y, inv), __fmul_rn(z, inv));
-}
-
 // Geometric normal of triangle p (intersectTriangle, :267-271): normalise(e1 x e2).
 __device__ __forceinline__ float3 tri_normal(const MeshPtrs& m, uint32_t p) {
   const float v0x = __ldg(m.v[0] + p), v0y = __ldg(m.v[1] + p), v0z = __ldg(m.v[2] + p);
@@ -163,7 +180,7 @@ __device__ __forceinline__ float3 tri_normal(const MeshPtrs& m, uint32_t p) {
   return normalize3(cross_c(e1y, e2z, e1z, e2y), cross_c(e1z, e2x, e1x, e2z), cross_c(e1x, e2y, e1y, e2x));
 }
 
-__global__ void __launch_bounds__(256) k_shade(PinholeBasis cam, MeshPtrs m, uint32_t n_tris, ShadeIn in, int mode,
+__global__ void __launch_bounds__(256) k_shade(PinholeCam cam, MeshPtrs m, uint32_t n_tris, ShadeIn in, int mode,
                                                float diag, float3 light, float* __restrict__ rgb) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
@@ -185,10 +202,11 @@ __global__ void __launch_bounds__(256) k_shade(PinholeBasis cam, MeshPtrs m, uin
     const float3 d = pinhole_dir(cam, (int)(r % (uint32_t)cam.width), (int)(r / (uint32_t)cam.width));
     if (dot3(n.x, n.y, n.z, d.x, d.y, d.z) > 0.0f) n = make_float3(-n.x, -n.y, -n.z);
     const float diffuse = fmaxf(0.0f, dot3(n.x, n.y, n.z, light.x, light.y, light.z));
-    const float shade = fminf(1.0f, __fadd_rn(0.15f, __fmul_rn(diffuse, 0.85f)));
-    cr = __fmul_rn(shade, __fadd_rn(0.7f, __fmul_rn(0.3f, fabsf(n.x))));
-    cg = __fmul_rn(shade, __fadd_rn(0.7f, __fmul_rn(0.3f, fabsf(n.y))));
-    cb = __fmul_rn(shade, __fadd_rn(0.7f, __fmul_rn(0.3f, fabsf(n.z))));
+    // ambient + diffuse*0.85 and 0.7 + 0.3*|n|, contracted
+    const float shade = fminf(1.0f, __fmaf_rn(diffuse, 0.85f, 0.15f));
+    cr = __fmul_rn(shade, __fmaf_rn(0.3f, fabsf(n.x), 0.7f));
+    cg = __fmul_rn(shade, __fmaf_rn(0.3f, fabsf(n.y), 0.7f));
+    cb = __fmul_rn(shade, __fmaf_rn(0.3f, fabsf(n.z), 0.7f));
   } else if (mode == 3) {  // raw node visits (the heatmap colours them afterwards)
     cr = cg = cb = (float)in.vis[r];
   } else {  // unknown mode: magenta
@@ -312,7 +330,7 @@ __global__ void __launch_bounds__(256) k_rgb8(const float* __restrict__ rgb, uin
   }
 }
 
-cudaError_t shade_pixels(const PinholeBasis& cam, const MeshPtrs& m, uint32_t n_tris, const ShadeIn& in, int mode,
+cudaError_t shade_pixels(const PinholeCam& cam, const MeshPtrs& m, uint32_t n_tris, const ShadeIn& in, int mode,
                          float diag, float3 light, float* rgb, cudaStream_t st) {
   const uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
   if (total == 0) return cudaSuccess;
@@ -354,7 +372,7 @@ cudaError_t trace_rays(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32
   return cudaGetLastError();
 }
 
-cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeBasis& cam,
+cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeCam& cam,
                           const HitOut& out, cudaStream_t st) {
   uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
   if (total == 0) return cudaSuccess;
@@ -362,7 +380,7 @@ cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uin
   return cudaGetLastError();
 }
 
-cudaError_t pinhole_rays(const PinholeBasis& cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz,
+cudaError_t pinhole_rays(const PinholeCam& cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz,
                          cudaStream_t st) {
   uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;
   if (total == 0) return cudaSuccess;

@@ -17,13 +17,13 @@ struct HitOut {
   int32_t* tri;
 };
 
-// Camera basis computed once on the host (generateRay, src/render_engine.cu:157-167).
-struct PinholeBasis {
+// Camera (include/render_engine.h:24-33) and image size; generateRay's basis
+// (src/render_engine.cu:157-167) is derived from it on the device, per ray.
+struct PinholeCam {
   float eye[3];
-  float f[3];
-  float r[3];
-  float u[3];
-  float half_w, half_h;
+  float look[3];
+  float up[3];
+  float fov_deg;
   int32_t width, height;
 };
 
@@ -35,12 +35,12 @@ struct ShadeIn {
 
 cudaError_t trace_rays(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const RayPtrs& rays,
                        uint32_t nr, const HitOut& out, cudaStream_t st);
-cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeBasis& cam,
+cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeCam& cam,
                           const HitOut& out, cudaStream_t st);
-cudaError_t pinhole_rays(const PinholeBasis& cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz,
+cudaError_t pinhole_rays(const PinholeCam& cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz,
                          cudaStream_t st);
 // kRenderKernel's shading of traced pinhole pixels (mode 0 normal, 1 depth, 2 diffuse, 3 visits).
-cudaError_t shade_pixels(const PinholeBasis& cam, const MeshPtrs& m, uint32_t n_tris, const ShadeIn& in, int mode,
+cudaError_t shade_pixels(const PinholeCam& cam, const MeshPtrs& m, uint32_t n_tris, const ShadeIn& in, int mode,
                          float diag, float3 light, float* rgb, cudaStream_t st);
 // applyHeatmapColormap on np visit counts with a 256-entry RGB colormap (device); scratch holds
 // heatmap_scratch_bytes().  fixed_max <= 0: the 99.9th-percentile normalisation.

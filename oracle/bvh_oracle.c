@@ -567,11 +567,22 @@ int orc_ploc(const orc_mesh* m, int radius, int max_iter, orc_node* nodes, uint3
   return rc;
 }
 
-/* ---- traversal: plain rounding of every operation (the GPU kernel uses __f*_rn) ---- */
+/* ---- traversal ----
+ * Every operation rounds as nvcc evaluates the reference's expressions under its default
+ * -fmad=true (pinned against the reference's own traverseBVH and generateRay on the GPU):
+ *   a*b - c*d              -> fmaf(a, b, -(c*d))
+ *   (a*x + b*y) + c*z      -> fmaf(c, z, fmaf(a, x, b*y))
+ *   x + a*b                -> fmaf(a, b, x)
+ * This file is compiled with -ffp-contract=off, so nothing else is fused. */
 #define TR_EPS 1e-6f
 #define TR_STACK 128
 
-/* intersectAABB, src/render_engine.cu:194-214. */
+static inline float tr_dot(float a, float b, float c, float x, float y, float z) {
+  return fmaf(c, z, fmaf(a, x, b * y));
+}
+static inline float tr_cross(float a, float b, float c, float d) { return fmaf(a, b, -(c * d)); }
+
+/* intersectAABB, src/render_engine.cu:194-214 (nothing to contract). */
 static inline int hit_box(const float o[3], const float inv[3], const orc_aabb* b, float tmax) {
   float t0[3], t1[3];
   for (int k = 0; k < 3; ++k) {
@@ -590,21 +601,21 @@ static inline int hit_tri(const float o[3], const float d[3], const orc_mesh* m,
   float v0x = m->v[0][p], v0y = m->v[1][p], v0z = m->v[2][p];
   float e1x = m->v[3][p] - v0x, e1y = m->v[4][p] - v0y, e1z = m->v[5][p] - v0z;
   float e2x = m->v[6][p] - v0x, e2y = m->v[7][p] - v0y, e2z = m->v[8][p] - v0z;
-  float px = d[1] * e2z - d[2] * e2y;
-  float py = d[2] * e2x - d[0] * e2z;
-  float pz = d[0] * e2y - d[1] * e2x;
-  float det = (e1x * px + e1y * py) + e1z * pz;
+  float px = tr_cross(d[1], e2z, d[2], e2y);
+  float py = tr_cross(d[2], e2x, d[0], e2z);
+  float pz = tr_cross(d[0], e2y, d[1], e2x);
+  float det = tr_dot(e1x, e1y, e1z, px, py, pz);
   if (fabsf(det) < TR_EPS) return 0;
   float inv_det = 1.0f / det;
   float tx = o[0] - v0x, ty = o[1] - v0y, tz = o[2] - v0z;
-  float u = ((tx * px + ty * py) + tz * pz) * inv_det;
+  float u = tr_dot(tx, ty, tz, px, py, pz) * inv_det;
   if (u < -1e-5f || u > 1.00001f) return 0;
-  float qx = ty * e1z - tz * e1y;
-  float qy = tz * e1x - tx * e1z;
-  float qz = tx * e1y - ty * e1x;
-  float v = ((d[0] * qx + d[1] * qy) + d[2] * qz) * inv_det;
+  float qx = tr_cross(ty, e1z, tz, e1y);
+  float qy = tr_cross(tz, e1x, tx, e1z);
+  float qz = tr_cross(tx, e1y, ty, e1x);
+  float v = tr_dot(d[0], d[1], d[2], qx, qy, qz) * inv_det;
   if (v < -1e-5f || u + v > 1.00001f) return 0;
-  float t = ((e2x * qx + e2y * qy) + e2z * qz) * inv_det;
+  float t = tr_dot(e2x, e2y, e2z, qx, qy, qz) * inv_det;
   if (t < TR_EPS) return 0;
   *out_t = t;
   return 1;
@@ -652,22 +663,25 @@ void orc_trace(const orc_node* nodes, uint32_t n_nodes, const orc_mesh* m, const
   }
 }
 
-/* generateRay, src/render_engine.cu:155-188, with the camera basis and tan(fov/2) computed
- * once on the host (the GPU kernel receives the same basis). */
+/* d_normalize, src/render_engine.cu:130-135. */
 static void normalize3(float v[3]) {
-  float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  float len = sqrtf(tr_dot(v[0], v[1], v[2], v[0], v[1], v[2]));
   if (len < 1e-12f) { v[0] = v[1] = v[2] = 0.0f; return; }
   float inv = 1.0f / len;
   v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
 }
+/* generateRay, src/render_engine.cu:155-188.  tan(fov/2) is the host's tanf, which may differ
+ * from the device's tanf in the last place; tests that need the GPU's exact rays take them from
+ * bvh_pinhole_rays, which is pinned bit for bit against the reference's generateRay. */
 void orc_pinhole_rays(const float eye[3], const float look[3], const float up[3], float fovy, int w, int h,
                       float* ro, float* rd) {
   float f[3] = {look[0] - eye[0], look[1] - eye[1], look[2] - eye[2]};
   normalize3(f);
-  float r[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+  float r[3] = {tr_cross(f[1], up[2], f[2], up[1]), tr_cross(f[2], up[0], f[0], up[2]),
+                tr_cross(f[0], up[1], f[1], up[0])};
   normalize3(r);
-  float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
-  float half_h = (float)tan((double)(fovy * 3.14159265358979f / 180.0f) * 0.5);
+  float u[3] = {tr_cross(r[1], f[2], r[2], f[1]), tr_cross(r[2], f[0], r[0], f[2]), tr_cross(r[0], f[1], r[1], f[0])};
+  float half_h = tanf(fovy * 3.14159265358979f / 180.0f * 0.5f);
   float half_w = half_h * ((float)w / (float)h);
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < (int64_t)w * h; ++p) {
@@ -675,7 +689,7 @@ void orc_pinhole_rays(const float eye[3], const float look[3], const float up[3]
     float uu = (2.0f * ((float)x + 0.5f) / (float)w - 1.0f) * half_w;
     float vv = (2.0f * ((float)y + 0.5f) / (float)h - 1.0f) * half_h;
     float d[3];
-    for (int k = 0; k < 3; ++k) d[k] = (f[k] + uu * r[k]) - vv * u[k];
+    for (int k = 0; k < 3; ++k) d[k] = fmaf(-vv, u[k], fmaf(uu, r[k], f[k]));
     normalize3(d);
     for (int k = 0; k < 3; ++k) { ro[3 * p + k] = eye[k]; rd[3 * p + k] = d[k]; }
   }
@@ -701,16 +715,16 @@ void orc_shade(const orc_mesh* m, const float* rd, const float* t, const int32_t
       float v0x = m->v[0][p], v0y = m->v[1][p], v0z = m->v[2][p];
       float e1x = m->v[3][p] - v0x, e1y = m->v[4][p] - v0y, e1z = m->v[5][p] - v0z;
       float e2x = m->v[6][p] - v0x, e2y = m->v[7][p] - v0y, e2z = m->v[8][p] - v0z;
-      float n[3] = {e1y * e2z - e1z * e2y, e1z * e2x - e1x * e2z, e1x * e2y - e1y * e2x};
+      float n[3] = {tr_cross(e1y, e2z, e1z, e2y), tr_cross(e1z, e2x, e1x, e2z), tr_cross(e1x, e2y, e1y, e2x)};
       normalize3(n);
       if (mode == 0) {
         for (int k = 0; k < 3; ++k) c[k] = (n[k] + 1.0f) * 0.5f;
       } else {
         const float* d = rd + 3 * i;
-        if ((n[0] * d[0] + n[1] * d[1]) + n[2] * d[2] > 0.0f) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
-        float diffuse = orc_fmax(0.0f, (n[0] * light[0] + n[1] * light[1]) + n[2] * light[2]);
-        float shade = orc_fmin(1.0f, 0.15f + diffuse * 0.85f);
-        for (int k = 0; k < 3; ++k) c[k] = shade * (0.7f + 0.3f * fabsf(n[k]));
+        if (tr_dot(n[0], n[1], n[2], d[0], d[1], d[2]) > 0.0f) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
+        float diffuse = orc_fmax(0.0f, tr_dot(n[0], n[1], n[2], light[0], light[1], light[2]));
+        float shade = orc_fmin(1.0f, fmaf(diffuse, 0.85f, 0.15f));
+        for (int k = 0; k < 3; ++k) c[k] = shade * fmaf(0.3f, fabsf(n[k]), 0.7f);
       }
     } else {
       c[0] = 1.0f; c[1] = 0.0f; c[2] = 1.0f;

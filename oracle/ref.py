@@ -76,6 +76,9 @@ class RefRunner:
         L.ref_render.argtypes = [c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_int, c_int, c_int, c_float, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
         L.ref_ploc_nn.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p]
+        L.ref_generate_rays.argtypes = [c_void_p, c_int, c_int, c_void_p]
+        L.ref_traverse.argtypes = [c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
         rc = L.ref_init(REF_DIR.encode(), b"_fast" if fast else b"")
         if rc:
             raise RuntimeError("ref_init: " + L.ref_error().decode())
@@ -135,6 +138,34 @@ class RefRunner:
                                         float(scene_diag), lt.ctypes.data, vis.ctypes.data, at.ctypes.data,
                                         tt.ctypes.data, rgb.ctypes.data, ms.ctypes.data), "ref_render")
         return vis, at, tt, rgb.reshape(-1, 3), float(ms[0])
+
+    def generate_rays(self, cam10, width, height):
+        """generateRay for every pixel (row-major): (origins (n, 3), directions (n, 3)) float32."""
+        cam = np.asarray(cam10, np.float32)
+        outs = [np.zeros(width * height, np.float32) for _ in range(6)]
+        arr = (c_void_p * 6)(*[a.ctypes.data for a in outs])
+        self._check(self.lib.ref_generate_rays(cam.ctypes.data, width, height, arr), "ref_generate_rays")
+        return np.stack(outs[:3], axis=1), np.stack(outs[3:], axis=1)
+
+    def traverse(self, nodes, arrays, ro, rd):
+        """traverseBVH on given rays: (t, prim, visits, aabb_tests, tri_tests, normal (n, 3), kernel_ms)."""
+        p, keep = _ptrs(arrays)
+        n = keep[0].shape[0]
+        nodes = np.ascontiguousarray(nodes)
+        rays = [np.ascontiguousarray(a[:, k], np.float32) for a in (ro, rd) for k in range(3)]
+        nr = rays[0].shape[0]
+        rp = (c_void_p * 6)(*[a.ctypes.data for a in rays])
+        t = np.zeros(nr, np.float32)
+        ints = [np.zeros(nr, np.int32) for _ in range(4)]
+        nrm = np.zeros(nr * 3, np.float32)
+        ms = np.zeros(1, np.float32)
+        self._check(self.lib.ref_traverse(nodes.ctypes.data, nodes.shape[0], p, n, rp, nr, t.ctypes.data,
+                                          *[a.ctypes.data for a in ints], nrm.ctypes.data, ms.ctypes.data),
+                    "ref_traverse")
+        return (t, *ints, nrm.reshape(-1, 3), float(ms[0]))
+
+    def trace_available(self) -> bool:
+        return os.path.exists(os.path.join(REF_DIR, "ref_trace.fatbin"))
 
     def ploc_nn(self, boxes_aabb, radius):
         boxes_aabb = np.ascontiguousarray(boxes_aabb)

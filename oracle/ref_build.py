@@ -8,6 +8,8 @@
   - libref_loader.so: the reference's src/loader.cpp with ref_loader_shim.cpp (host only).
   - libref_render_host.so: the reference's src/render_engine.cu, included by ref_render_shim.cu,
     for its host post-processing (heatmap colormap, PPM bytes); used by CPU tests only.
+  - ref_trace.fatbin: the reference's src/render_engine.cu, included by ref_trace_shim.cu, whose
+    two kernels run the reference's generateRay and traverseBVH on given rays (default flags).
 * Anywhere (GPU machines included): libref_runner.so from ref_runner.cu (our host code that loads the
   fatbins and replays the reference builders with CUB/Thrust).
 """
@@ -98,6 +100,15 @@ def build_render_host():
                              "-o", os.path.join(OUT, "libref_render_host.so")])
 
 
+def build_trace_shim():
+    out = os.path.join(OUT, "ref_trace.fatbin")
+    shim = os.path.join(HERE, "ref_trace_shim.cu")
+    if _fresh(out, shim, os.path.join(REF_ROOT, "src", "render_engine.cu")):
+        return
+    _run([_nvcc(), "-fatbin"] + ARCH + ["-std=c++17", "-I" + os.path.join(REF_ROOT, "include"),
+                                        "-I" + os.path.join(REF_ROOT, "src"), shim, "-o", out])
+
+
 def build_runner():
     if _fresh(os.path.join(OUT, "libref_runner.so"), os.path.join(HERE, "ref_runner.cu")):
         return
@@ -117,6 +128,7 @@ def build(runner: bool = True):
         build_eval()
         build_loader()
         build_render_host()
+        build_trace_shim()
     if runner and fatbins_present():
         build_runner()
 

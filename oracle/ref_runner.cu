@@ -60,7 +60,8 @@ struct BoxUnion {
 struct Mod {
   CUmodule m = nullptr;
 };
-Mod g_lbvh, g_plus, g_ploc, g_render;
+Mod g_lbvh, g_plus, g_ploc, g_render, g_trace;
+std::string g_dir;
 std::string g_err;
 
 #define CK(x)                                                               \
@@ -117,6 +118,7 @@ int ref_init(const char* dir, const char* suffix) {
   CK(cudaSetDevice(0));
   CK(cudaFree(nullptr));
   std::string d(dir), s(suffix ? suffix : "");
+  g_dir = d;
   if (load(g_lbvh, d + "/ref_lbvh" + s + ".fatbin")) return 1;
   if (load(g_plus, d + "/ref_lbvh_plus" + s + ".fatbin")) return 1;
   if (load(g_ploc, d + "/ref_ploc" + s + ".fatbin")) return 1;
@@ -468,6 +470,82 @@ int ref_render(const void* host_nodes, uint32_t n_nodes, const float* const* hv,
   cudaFree(dn);
   for (int k = 0; k < 9; ++k) cudaFree(dv[k]);
   cudaFree(drgb); cudaFree(dvis); cudaFree(dat); cudaFree(dtt);
+  return 0;
+}
+
+// generateRay (src/render_engine.cu:155-188) for every pixel of a width x height image, run by the
+// reference's own device code (ref_trace.fatbin, built from ref_trace_shim.cu).  Host outputs.
+int ref_generate_rays(const float* cam10, int width, int height, float* const* out6) {
+  if (load(g_trace, g_dir + "/ref_trace.fatbin")) return 1;
+  const size_t np = (size_t)width * height;
+  float* d[6];
+  for (int k = 0; k < 6; ++k) CK(cudaMalloc(&d[k], np * 4));
+  Cam cam;
+  cam.eye = F3{cam10[0], cam10[1], cam10[2]};
+  cam.look = F3{cam10[3], cam10[4], cam10[5]};
+  cam.up = F3{cam10[6], cam10[7], cam10[8]};
+  cam.fov = cam10[9];
+  DK(launch(fn(g_trace, "shim_generate_rays"), (unsigned)((np + 255) / 256), 256u, cam, width, height, d[0], d[1],
+            d[2], d[3], d[4], d[5]));
+  CK(cudaDeviceSynchronize());
+  for (int k = 0; k < 6; ++k) CK(cudaMemcpy(out6[k], d[k], np * 4, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 6; ++k) cudaFree(d[k]);
+  return 0;
+}
+
+// traverseBVH (src/render_engine.cu:289-356) on nr given rays (six host SoA arrays), run by the
+// reference's own device code.  Outputs per ray: t, prim (-1 on a miss), node visits, AABB tests,
+// triangle tests, and the hit normal (3 floats, 0 on a miss).  ms[0] = kernel time.
+int ref_traverse(const void* host_nodes, uint32_t n_nodes, const float* const* hv, uint32_t n,
+                 const float* const* rays6, uint32_t nr, float* t, int* prim, int* visits, int* aabb, int* tri,
+                 float* normal, float* ms) {
+  if (load(g_trace, g_dir + "/ref_trace.fatbin")) return 1;
+  Node* dn;
+  CK(cudaMalloc(&dn, (size_t)n_nodes * sizeof(Node) + 16));
+  CK(cudaMemcpy(dn, host_nodes, (size_t)n_nodes * sizeof(Node), cudaMemcpyHostToDevice));
+  Tris tr;
+  for (int k = 0; k < 9; ++k) {
+    CK(cudaMalloc(&tr.v[k], (size_t)n * 4 + 16));
+    CK(cudaMemcpy(tr.v[k], hv[k], (size_t)n * 4, cudaMemcpyHostToDevice));
+  }
+  float* dr[6];
+  for (int k = 0; k < 6; ++k) {
+    CK(cudaMalloc(&dr[k], (size_t)nr * 4 + 16));
+    CK(cudaMemcpy(dr[k], rays6[k], (size_t)nr * 4, cudaMemcpyHostToDevice));
+  }
+  float *dt, *dnorm;
+  int *dp, *dv, *da, *dtt;
+  CK(cudaMalloc(&dt, (size_t)nr * 4 + 16));
+  CK(cudaMalloc(&dp, (size_t)nr * 4 + 16));
+  CK(cudaMalloc(&dv, (size_t)nr * 4 + 16));
+  CK(cudaMalloc(&da, (size_t)nr * 4 + 16));
+  CK(cudaMalloc(&dtt, (size_t)nr * 4 + 16));
+  CK(cudaMalloc(&dnorm, (size_t)nr * 12 + 16));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const Node* cdn = dn;
+  const float *r0 = dr[0], *r1 = dr[1], *r2 = dr[2], *r3 = dr[3], *r4 = dr[4], *r5 = dr[5];
+  CK(cudaEventRecord(e0));
+  DK(launch(fn(g_trace, "shim_traverse"), (nr + 127) / 128, 128u, cdn, (int)n_nodes, tr, r0, r1, r2, r3, r4, r5,
+            (int)nr, dt, dp, dv, da, dtt, dnorm));
+  CK(cudaEventRecord(e1));
+  CK(cudaEventSynchronize(e1));
+  float a = 0;
+  CK(cudaEventElapsedTime(&a, e0, e1));
+  if (ms) ms[0] = a;
+  CK(cudaMemcpy(t, dt, (size_t)nr * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(prim, dp, (size_t)nr * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(visits, dv, (size_t)nr * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(aabb, da, (size_t)nr * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(tri, dtt, (size_t)nr * 4, cudaMemcpyDeviceToHost));
+  if (normal) CK(cudaMemcpy(normal, dnorm, (size_t)nr * 12, cudaMemcpyDeviceToHost));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(dn);
+  for (int k = 0; k < 9; ++k) cudaFree(tr.v[k]);
+  for (int k = 0; k < 6; ++k) cudaFree(dr[k]);
+  cudaFree(dt); cudaFree(dp); cudaFree(dv); cudaFree(da); cudaFree(dtt); cudaFree(dnorm);
   return 0;
 }
 

@@ -1,9 +1,10 @@
 """Device shading, heatmap and byte conversion (kRenderKernel's shading, applyHeatmapColormap,
-savePPM's conversion): bit-exact against the oracle, within a tolerance against the reference kernel."""
+savePPM's conversion): bit-exact against the oracle and against the reference's kRenderKernel."""
 import numpy as np
 import pytest
 
 from bvh_gb300 import Context, auto_camera, meshgen, _capi as C
+from bvh_gb300.builders import pinhole_rays
 from tests.gpu_util import build, stream
 
 pytestmark = pytest.mark.gpu
@@ -56,7 +57,10 @@ def test_shade_matches_oracle_bit_exact(ctx, gpu, oracle_lib, mode):
     gpu.cuda.synchronize()
     got = rgb.cpu().numpy().reshape(-1, 3)
     t, prim, vis = hts[0].cpu().numpy(), hts[1].cpu().numpy(), hts[2].cpu().numpy()
-    _, rd = O.pinhole_rays(list(cam.eye), list(cam.look_at), list(cam.up), cam.fov_y_deg, w, h)
+    rts = [gpu.empty(w * h, dtype=gpu.float32, device="cuda") for _ in range(6)]
+    pinhole_rays(cam, w, h, [x.data_ptr() for x in rts], stream(gpu))
+    gpu.cuda.synchronize()
+    rd = np.stack([x.cpu().numpy() for x in rts[3:]], axis=1)  # the GPU's rays (device tanf)
     exp = O.shade(m.arrays(), rd, t, prim, vis, mode, diag, LIGHT)
     assert (prim >= 0).sum() > 1000 and (prim < 0).sum() > 100  # hits and misses both present
     assert np.array_equal(got.view(np.uint32), exp.view(np.uint32))
@@ -64,9 +68,7 @@ def test_shade_matches_oracle_bit_exact(ctx, gpu, oracle_lib, mode):
 
 @pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_shade_vs_reference_render_kernel(ctx, gpu, mode):
-    """RGB against kRenderKernel on the reference's own LBVH. The reference's ray directions use
-    device tanf and its arithmetic may contract into FMAs, so values agree to 2e-5 on at least
-    99.9% of pixels (the node-visit mode exactly)."""
+    """RGB against kRenderKernel on the reference's own LBVH: bit-equal on every pixel."""
     from oracle import ref
     if not ref.runner_available():
         pytest.skip("reference fatbins not present")
@@ -83,9 +85,8 @@ def test_shade_vs_reference_render_kernel(ctx, gpu, mode):
               rgb.data_ptr(), stream(gpu))
     gpu.cuda.synchronize()
     got = rgb.cpu().numpy().reshape(-1, 3)
-    tol = 0.0 if mode == 3 else 2e-5
-    close = np.all(np.abs(got - rrgb) <= tol, axis=1)
-    assert close.mean() >= 0.999, close.mean()
+    same = np.all(got.view(np.uint32) == rrgb.view(np.uint32), axis=1)
+    assert same.all(), f"mode {mode}: {int((~same).sum())} pixels differ"
 
 
 @pytest.mark.parametrize("case", ["percentile", "fixed", "all_zero", "one_pixel", "large_counts"])
