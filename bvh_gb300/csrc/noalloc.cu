@@ -7,6 +7,11 @@
 // one file-scope __device__ array of fixed size, which every GPU that loads this library holds
 // until the process exits.  All calls share that array, so calls that overlap on the GPU (two
 // streams, two threads) race and corrupt each other's results; serialise them.
+// The call returns before its kernels finish and has no buffer of the caller's to report into,
+// so device-side errors go unreported: the radix sort's look-back waits are bounded and record a
+// timeout in the array's status word, which the context path reads, but this path does not.
+// (A look-back only waits on tiles that started before it, so the bound is a safety net; it is
+// not reached in normal operation.)
 #include <mutex>
 
 #include "../../include/bvh_gb300.h"
@@ -35,21 +40,23 @@ __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
-unsigned char* g_ptr[kMaxDevices] = {};  // device address of g_static_scratch, per device
+bool g_prepared[kMaxDevices] = {};  // kernel attributes set on this device
 
-// Once per device, with that device current: the array's device address (host code must not
-// use the symbol itself, which is only a host-side stand-in).
+// On every call, with the caller's device current: the array's device address (host code must
+// not use the symbol itself, which is only a host-side stand-in).  The lookup is cheap and is
+// not cached, so a module reloaded after cudaDeviceReset is found at its new address.  The
+// kernels' attributes are set once per device (allocates nothing).
 cudaError_t static_scratch(int device, unsigned char** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (!g_prepared[device]) {
+    e = prepare_kernels();
     if (e != cudaSuccess) return e;
-    e = prepare_kernels();  // kernel attributes only; allocates nothing
-    if (e != cudaSuccess) return e;
-    g_ptr[device] = static_cast<unsigned char*>(p);
+    g_prepared[device] = true;
   }
-  *out = g_ptr[device];
+  *out = static_cast<unsigned char*>(p);
   return cudaSuccess;
 }
 

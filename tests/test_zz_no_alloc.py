@@ -59,6 +59,30 @@ def test_static_build_equals_context_build_on_consecutive_calls(gpu):
     ctx.close()
 
 
+@pytest.mark.parametrize("bits", [30, 60, 63])
+def test_static_build_tiny_meshes(gpu, bits):
+    """The static path keeps the 60/63-bit run fix-up's low bits and scratch inside the caller's
+    node buffer, which is exactly 2n-1 nodes here: tiny meshes, and a dense cell (long runs of
+    equal high halves), against the context build."""
+    lib = C.load_library()
+    ctx = Context(0)
+    meshes = [meshgen.uniform_small(n, seed=30 + n) for n in (1, 2, 7, 9, 1025)]
+    one = meshgen.uniform_small(1, seed=29)
+    spread = meshgen.uniform_small(2000, seed=28)
+    for copies in (600, 2999):  # runs of equal codes ranked by counting (<= 1024) or block-sorted
+        same = [np.repeat(a, copies) for a in one.arrays()]
+        meshes.append(type(one)(*[np.concatenate([s, b[:1]]) for s, b in zip(same, spread.arrays())]))
+        meshes.append(type(one)(*[np.concatenate([s, b]) for s, b in zip(same, spread.arrays())]))
+    for mesh in meshes:
+        for _ in range(2):
+            status, nodes, idx = _static_build(gpu, lib, mesh, bits)
+            assert status == C.BVH_OK
+            ref_nodes, ref_idx = _ctx_build(gpu, ctx, mesh, bits)
+            assert np.array_equal(idx, ref_idx), mesh.size()
+            assert _same(nodes, ref_nodes), mesh.size()
+    ctx.close()
+
+
 def test_static_build_rejects_more_than_its_maximum(gpu):
     lib = C.load_library()
     status, _, _ = _static_build(gpu, lib, meshgen.uniform_small(MAX_TRIS + 1, seed=24), 30)
