@@ -27,6 +27,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+METRIC = "build Mtris/s (device-resident) + %HBM roofline; batched vs plain; serve p50/p99 ms"
 FALLBACK_HBM = 6800.0
 
 WORKLOADS = {
@@ -66,6 +67,9 @@ WORKLOADS = {
     "c3_batched": ("batch", {"meshes": 4096, "lo": 64, "hi": 262144}, "lbvh_batched", 30, 0,
                    "4,096 meshes, triangle counts logU[64, 262144], each built by LBVH-30 in one batched launch "
                    "sequence replayed as a CUDA graph"),
+    "c3_batched_ploc25": ("batch", {"meshes": 4096, "lo": 64, "hi": 262144}, "ploc_batched", 30, 25,
+                          "4,096 meshes, triangle counts logU[64, 262144], each built by PLOC r=25 in one batched "
+                          "build (one CUDA graph launch: keys, sort, clustering loop as a conditional node)"),
     "c4_serve": ("serve", {"rate": 2000.0, "duration_s": 3.0, "lo": 1000, "hi": 2_000_000, "rays": 65536,
                            "pool": 32, "budget_gb": 40, "slots": 16}, "serve", 30, 0,
                  "Poisson stream (2,000 req/s) of build+trace requests, meshes logU[1e3, 2e6] triangles, "
@@ -132,16 +136,21 @@ def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: in
     return n + (rounds * (5 + 3 * tree_height) if algo == "lbvh_plus" else 0)
 
 
-def batched_kernels_per_build(meshes: int) -> int:
+def batched_kernels_per_build(meshes: int, ploc_iterations: int = -1) -> int:
     """Launches in one batched build: per-mesh box init, bounds and Morton, ceil(K/8) onesweep
     passes over the K = 30 + mesh-bits keys (4 when K > 32, followed by the two run fix-up
-    kernels), delta + emission + frontier climb."""
+    kernels), then LBVH: delta + emission + frontier climb; PLOC (ploc_iterations >= 0): leaf and
+    cluster init, 5 per iteration (neighbours, tile counts + scan, per-mesh ranks, merge +
+    compaction, loop control) and the per-mesh root fix."""
     mbits = 1
     while mbits < 34 and (1 << mbits) < meshes:
         mbits += 1
     kbits = 30 + mbits
     passes = 4 if kbits > 32 else (kbits + 7) // 8
-    return 3 + passes + (2 if kbits > 32 else 0) + 3
+    prefix = 3 + passes + (2 if kbits > 32 else 0)
+    if ploc_iterations >= 0:
+        return prefix + 1 + 5 * ploc_iterations + 1
+    return prefix + 3
 
 
 STAGE_KERNELS = {
@@ -159,8 +168,8 @@ STAGE_KERNELS = {
 # the stage's traffic grows with the triangle count, so a launch over n triangles moves about
 # n times this.  Keyed by (algorithm, Morton bits, stage).
 MEASURED_TRAFFIC_PER_TRI = {
-    ("lbvh", 63, "emit_refit"): (191.6, "profiles/emit_fixrun_c1_4m.md: k_emit + k_emit_climb at 4M, "
-                                        "766 MB / 4M triangles, scaled by the triangle count"),
+    ("lbvh", 63, "emit_refit"): (191.6, "one ncu capture of k_emit + k_emit_climb on 4M triangles of the same "
+                                        "distribution: 766 MB / 4M triangles, scaled by the triangle count"),
 }
 
 
@@ -174,13 +183,17 @@ def hbm_peak():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms for as long as the sampler is
+    open; each sample is stamped with the host clock when it arrives, so any window (the timed
+    region, or the whole measurement phase around it) can be summarised afterwards."""
+
+    PERIOD_MS = 20
 
     def __init__(self, gpu_index: int = 0):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
-        self.skip = 0
+        self.samples = []  # (host time, csv line)
+        self.marks = {}
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -188,35 +201,42 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
-            # start the timed region only once nvidia-smi is producing samples (it takes a moment)
+            # measure only once nvidia-smi is producing samples (it takes a moment to start)
             t0 = time.perf_counter()
-            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+            while not self.samples and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
                 time.sleep(0.01)
-            self.skip = len(self.lines)  # samples taken before the timed region
         except Exception:
             self.proc = None
+        self.mark("open")
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.samples.append((time.perf_counter(), line.strip()))
+
+    def mark(self, name):
+        self.marks[name] = time.perf_counter()
 
     def __exit__(self, *a):
+        self.mark("close")
         if self.proc:
+            time.sleep(2.0 * self.PERIOD_MS / 1e3)  # the sample covering the last moments
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
+    def _summarise(self, t0, t1):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines[self.skip:]:
+        for ts, line in self.samples:
+            if ts < t0 or ts > t1:
+                continue
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 7:
                 continue
@@ -228,10 +248,24 @@ class ClockSampler:
             for nm, v in zip(names, parts[3:7]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
+        return sm, mx, reasons
+
+    def summary(self, start="timed_start", end="timed_end", fallback=("open", "close"), min_samples=3):
+        """Median SM clock, its maximum and the throttle reasons seen between two marks.  With
+        fewer than min_samples there (a short timed region), the fallback window -- the whole
+        phase of identical builds around it -- is summarised instead and named in `window`."""
+        t0, t1 = self.marks.get(start, 0.0), self.marks.get(end, 0.0)
+        sm, mx, reasons = self._summarise(t0, t1 + self.PERIOD_MS / 1e3)
+        window = "timed region"
+        if len(sm) < min_samples and fallback:
+            f0, f1 = self.marks.get(fallback[0], 0.0), self.marks.get(fallback[1], time.perf_counter())
+            sm, mx, reasons = self._summarise(f0, f1 + self.PERIOD_MS / 1e3)
+            window = (f"{fallback[0]}..{fallback[1]}: the timed region ({(t1 - t0) * 1e3:.0f} ms) and the "
+                      f"warm-up and stage-timing builds around it ({(f1 - f0) * 1e3:.0f} ms in all)")
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0, "window": window}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "window": window, "period_ms": self.PERIOD_MS}
 
 
 def dist_info():
@@ -326,7 +360,9 @@ def run_ours(args):
     tuning = None if args.no_autotune else ctx.autotune(n, s)
 
     # --- device-resident build throughput -------------------------------------------------
-    with torch.cuda.stream(stream):
+    # The clock sampler runs through the warm-up, the timed region and the stage-timing builds
+    # (all identical builds), so a short timed region still gets a clock record.
+    with torch.cuda.stream(stream), ClockSampler(local) as clk:
         for _ in range(args.warmup):
             ctx.build_device(ptrs, n, params, s)
         ctx.sync()
@@ -336,12 +372,13 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
         if ws > 1:
             dist.barrier()
-        with ClockSampler(local) as clk:
-            ev0.record(stream)
-            for _ in range(args.steps):
-                ctx.build_device(ptrs, n, params, s)
-            ev1.record(stream)
-            torch.cuda.synchronize(dev)
+        clk.mark("timed_start")
+        ev0.record(stream)
+        for _ in range(args.steps):
+            ctx.build_device(ptrs, n, params, s)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        clk.mark("timed_end")
         if ws > 1:
             dist.barrier()
         ctx.sync()
@@ -462,11 +499,55 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     e2e = {"value": round(n * ws / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
-           "d2h_bytes_per_step": 48 * (2 * n - 1) + 4 * n, "ms_per_step": round(e2e_ms, 3)}
+           "d2h_bytes_per_step": 48 * (2 * n - 1) + 4 * n, "ms_per_step": round(e2e_ms, 3),
+           "host_memory": "pinned (page-locked) input and output buffers"}
+    extras = {}
+    if args.workload == "c1_lbvh63" and not args.no_extras and ws == 1:
+        # the same call on ordinary pageable memory: what the BVHBuilder adapter hands over
+        # (std::vector / numpy arrays), so the speed-up a drop-in caller gets
+        p_in = mesh.arrays()
+        m_page = C.mesh_struct([a.ctypes.data for a in p_in], n)
+        p_nodes = np.empty((2 * n - 1) * 48, np.uint8)
+        p_idx = np.empty(n, np.uint32)
+
+        def e2e_pageable_once():
+            C.check(lib.bvh_build_host(ctx.handle, ctypes.byref(m_page), ctypes.byref(params), ctypes.c_void_p(s),
+                                       ctypes.c_void_p(p_nodes.ctypes.data), ctypes.c_void_p(p_idx.ctypes.data),
+                                       ctypes.byref(nn)), "bvh_build_host")
+
+        e2e_pageable_once()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_pageable_once()
+        torch.cuda.synchronize(dev)
+        pg_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        extras["e2e_pageable"] = {"value": round(n / (pg_ms / 1e3) / 1e6, 2), "unit": "Mtris/s",
+                                  "ms_per_step": round(pg_ms, 3), "steps": e2e_steps,
+                                  "h2d_bytes_per_step": 36 * n, "d2h_bytes_per_step": 48 * (2 * n - 1) + 4 * n,
+                                  "host_memory": "pageable numpy arrays (as a std::vector-backed TriangleMesh)"}
+        # the same mesh with the reference LBVH's own 30-bit codes: the same-configuration number
+        p30 = ctx.params(C.ALGO_LBVH, morton_bits=30)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                ctx.build_device(ptrs, n, p30, s)
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                ctx.build_device(ptrs, n, p30, s)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+        ms30 = e0.elapsed_time(e1) / args.steps
+        extras["lbvh30"] = {"value": round(n / (ms30 / 1e3) / 1e6, 2), "unit": "Mtris/s",
+                            "ms_per_step": round(ms30, 4), "steps": args.steps,
+                            "what": "the same 10M mesh, LBVH with 30-bit Morton codes (the configuration of the "
+                                    "reference's LBVHBuilderCUDA, which the reference arm times)"}
 
     # parity of the timed result against the oracle is covered by tests; record SAH here
     line = {
-        "metric": "build Mtris/s (device-resident) + %HBM roofline",
+        "metric": METRIC,
         "value": round(value, 2), "unit": "Mtris/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
@@ -483,15 +564,27 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, mesh)
+    ctx.close()
+    if extras:
+        line.update(extras)
+        del d_in, h_in, h_nodes, h_idx
+        torch.cuda.empty_cache()
+        # the metric's other halves: batched vs plain at equal trees (config 3), serving p50/p99
+        # (config 4, a shortened stream), each a measurement of its own
+        line["batched"] = measure_batched(max(3, min(args.steps, 10)), args.warmup, local, rank,
+                                          autotune=not args.no_autotune)
+        line["batched_ploc"] = measure_batched(3, args.warmup, local, rank, autotune=False, algo="ploc", radius=25)
+        line["serve"] = measure_serve(1.0, local, rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     if ws > 1:
         dist.destroy_process_group()
 
 
-def run_batched(args):
-    """Config 3: many meshes in one batched, graph-captured build vs a per-mesh loop of single builds."""
+def measure_batched(steps, warmup, local=0, rank=0, autotune=True, algo="lbvh", radius=25, check_meshes=16):
+    """Config 3: 4,096 meshes (counts logU[64, 262144]) in one batched, graph-replayed build vs a
+    per-mesh loop of single builds on the same GPU and the same device-resident data.  Also checks
+    that sampled meshes' trees equal their single builds bit for bit."""
     import ctypes
     import torch
 
@@ -499,49 +592,50 @@ def run_batched(args):
     from bvh_gb300 import _capi as C
     from bvh_gb300 import meshgen
 
-    ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    kw = WORKLOADS["c3_batched"][1]
     counts = meshgen.batch_counts(kw["meshes"], kw["lo"], kw["hi"], seed=4)
     mesh, offsets = meshgen.batch(counts, seed=5 + rank)
     n = mesh.size()
     count = offsets.shape[0] - 1
     ctx = bvh_gb300.Context(local)
-    params = ctx.params(C.ALGO_LBVH)
-    tuning = None if args.no_autotune else ctx.autotune(min(n, 1 << 26))
+    algo_id = C.ALGO_PLOC if algo == "ploc" else C.ALGO_LBVH
+    params = ctx.params(algo_id, ploc_radius=radius)
+    tuning = ctx.autotune(min(n, 1 << 26)) if autotune else None
     d_in = [torch.from_numpy(a).to(dev) for a in mesh.arrays()]
     ptrs = [t.data_ptr() for t in d_in]
     stream = torch.cuda.Stream(device=dev)
     s = stream.cuda_stream
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+    with torch.cuda.stream(stream), ClockSampler(local) as clk:
+        for _ in range(warmup):
             ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
         ctx.sync()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(dev)
-        with ClockSampler(local) as clk:
-            ev0.record(stream)
-            for _ in range(args.steps):
-                ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
-            ev1.record(stream)
-            torch.cuda.synchronize(dev)
-        ms = ev0.elapsed_time(ev1) / args.steps
+        clk.mark("timed_start")
+        ev0.record(stream)
+        for _ in range(steps):
+            ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        clk.mark("timed_end")
+        ms = ev0.elapsed_time(ev1) / steps
         # stage breakdown without the graph
-        ctx.build_batched(ptrs, offsets, params, s, use_graph=False)
+        tree = ctx.build_batched(ptrs, offsets, params, s, use_graph=False)
         t = ctx.last_timing()
+        iters, csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
         stages = {"seg_bounds": round(t.bounds_ms, 4), "seg_morton_hist": round(t.morton_ms, 4),
-                  "onesweep_sort": round(t.sort_ms, 4), "delta_emit_refit": round(t.emit_ms, 4)}
+                  "onesweep_sort": round(t.sort_ms, 4), "delta_emit_refit": round(t.emit_ms, 4),
+                  "ploc_loop": round(t.optimize_ms, 4)}
         # plain per-mesh loop of single-mesh builds on the same device-resident data
         single = bvh_gb300.Context(local)
-        single.reserve(int(counts.max()))
+        single.reserve(int(counts.max()), algo_id)
         single.set_tuning(ctx.tuning())
         loop_reps = 2
-        for _ in range(1):
-            for m in range(count):
-                a = int(offsets[m])
-                single.build_device([p + 4 * a for p in ptrs], int(counts[m]), params, s)
+        for m in range(count):
+            a = int(offsets[m])
+            single.build_device([p + 4 * a for p in ptrs], int(counts[m]), params, s)
         torch.cuda.synchronize(dev)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -553,25 +647,51 @@ def run_batched(args):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         loop_ms = e0.elapsed_time(e1) / loop_reps
+        # sampled meshes (the largest, the smallest, others spread over the batch) against their
+        # single builds, bit for bit; each mesh's part of the batched tree is read back alone
+        picks = sorted({int(np.argmax(counts)), int(np.argmin(counts))} |
+                       {int(x) for x in np.linspace(0, count - 1, max(2, check_meshes - 2)).astype(int)})
+        equal = True
+        for m in picks:
+            a, c = int(offsets[m]), int(counts[m])
+            first = 2 * a - m
+            sub = C.Tree()
+            sub.nodes = tree.nodes + 48 * first
+            sub.indices = tree.indices + 4 * a
+            sub.n_nodes, sub.n_prims = 2 * c - 1, c
+            bn = np.zeros(2 * c - 1, C.NODE_DTYPE)
+            bi = np.zeros(c, np.uint32)
+            C.check(ctx.lib.bvh_tree_download(ctx.handle, ctypes.byref(sub), ctypes.c_void_p(s),
+                                              ctypes.c_void_p(bn.ctypes.data), ctypes.c_void_p(bi.ctypes.data)))
+            one = single.build_device([p + 4 * a for p in ptrs], c, params, s)
+            single.sync()
+            sn, si = single.download(one, s)
+            same = (np.array_equal(bi, si) and np.array_equal(bn["left"], sn["left"])
+                    and np.array_equal(bn["right"], sn["right"])
+                    and np.array_equal(bn["min"].view(np.uint32), sn["min"].view(np.uint32))
+                    and np.array_equal(bn["max"].view(np.uint32), sn["max"].view(np.uint32)))
+            equal = equal and same
         single.close()
     value = n / (ms / 1e3) / 1e6
     loop_value = n / (loop_ms / 1e3) / 1e6
     peak, peak_kind = hbm_peak()
-    bpt = 444.0  # 42-bit segmented keys: B = 276 + 3*8 + 2*6*(8+4)
-    achieved = bpt * n / (ms / 1e3) / 1e9
+    # 42-bit segmented keys (kb = 8, D = 6): LBVH B = 276 + 3*8 + 2*6*(8+4) = 444; PLOC: its prefix
+    # with those keys (36 + 48 + 152) + leaf and cluster init 116 = 352, + 160 per live cluster
+    # per iteration
+    bpt = 444.0 if algo != "ploc" else 352.0 + 160.0 * csum / n
     # e2e: pinned host SoA -> device, batched build, nodes + indices back to pinned host memory
     h_in = [torch.from_numpy(a).pin_memory() for a in mesh.arrays()]
     n_nodes = 2 * n - count
     h_nodes = torch.empty(n_nodes * 48, dtype=torch.uint8).pin_memory()
     h_idx = torch.empty(n * 4, dtype=torch.uint8).pin_memory()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, min(steps, 5))
 
     def e2e_once():
         with torch.cuda.stream(stream):
             for d, h in zip(d_in, h_in):
                 d.copy_(h, non_blocking=True)
-            tree = ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
-            C.check(ctx.lib.bvh_tree_download(ctx.handle, ctypes.byref(tree), ctypes.c_void_p(s),
+            tr = ctx.build_batched(ptrs, offsets, params, s, use_graph=True)
+            C.check(ctx.lib.bvh_tree_download(ctx.handle, ctypes.byref(tr), ctypes.c_void_p(s),
                                               ctypes.c_void_p(h_nodes.data_ptr()), ctypes.c_void_p(h_idx.data_ptr())))
 
     e2e_once()
@@ -581,33 +701,58 @@ def run_batched(args):
         e2e_once()
     torch.cuda.synchronize(dev)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    ctx.close()
+    out = {"value": round(value, 2), "unit": "Mtris/s", "ms_per_step": round(ms, 4), "steps": steps,
+           "meshes": count, "triangles": n, "min_mesh": int(counts.min()), "max_mesh": int(counts.max()),
+           "algorithm": "PLOC r=%d" % radius if algo == "ploc" else "LBVH 30-bit",
+           "per_mesh_loop": {"value": round(loop_value, 2), "unit": "Mtris/s", "ms_per_step": round(loop_ms, 3)},
+           "speedup_batched_over_loop": round(value / loop_value, 2),
+           "equal_to_single_builds": {"meshes_checked": len(picks), "all_equal": bool(equal)},
+           "stage_ms": stages,
+           "e2e": {"value": round(n / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
+                   "d2h_bytes_per_step": 48 * n_nodes + 4 * n, "ms_per_step": round(e2e_ms, 3)},
+           "gpu_launches": steps * batched_kernels_per_build(count, iters if algo == "ploc" else -1),
+           "clocks": clk.summary(), "autotune": tuning}
+    if algo == "ploc":
+        out["ploc"] = {"iterations": iters, "cluster_sum": csum, "radius": radius}
+    if bpt:
+        achieved = bpt * n / (ms / 1e3) / 1e9
+        out["algorithmic_bytes_per_tri"] = round(bpt, 2)
+        out["roofline"] = {"bound": "hbm", "kernel": "whole batched build", "achieved": round(achieved, 1),
+                           "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                           "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": bpt}
+    return out
+
+
+def run_batched(args):
+    """Config 3 as its own bench line."""
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    b = measure_batched(args.steps, args.warmup, local, rank, autotune=not args.no_autotune,
+                        algo="ploc" if algo == "ploc_batched" else "lbvh", radius=radius or 25)
     line = {
         "metric": "batched build Mtris/s (device-resident) vs per-mesh loop",
-        "value": round(value * ws, 2), "unit": "Mtris/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+u64", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
-        "config": {"workload": args.workload, "description": desc, "meshes": count, "triangles": n,
-                   "min_mesh": int(counts.min()), "max_mesh": int(counts.max()), "parallelism": f"shards x{ws}",
+        "value": round(b["value"] * ws, 2), "unit": "Mtris/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
+        "config": {"workload": args.workload, "description": desc, "meshes": b["meshes"], "triangles": b["triangles"],
+                   "min_mesh": b["min_mesh"], "max_mesh": b["max_mesh"], "parallelism": f"replicas x{ws}",
                    "l2": "inputs (4.8 GB) exceed the 129 MB L2; no flush"},
-        "per_mesh_loop": {"value": round(loop_value, 2), "unit": "Mtris/s", "ms_per_step": round(loop_ms, 3),
-                          "speedup_batched_over_loop": round(value / loop_value, 2)},
-        "stage_ms": stages,
-        "roofline": {"bound": "hbm", "kernel": "whole batched build", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-                     "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_tri": bpt},
-        "e2e": {"value": round(n * ws / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * n,
-                "d2h_bytes_per_step": 48 * n_nodes + 4 * n, "ms_per_step": round(e2e_ms, 3)},
-        "gpu_launches": args.steps * batched_kernels_per_build(count),
-        "clocks": clk.summary(),
-        "autotune": tuning,
     }
+    for k in ("per_mesh_loop", "speedup_batched_over_loop", "equal_to_single_builds", "stage_ms", "roofline",
+              "e2e", "gpu_launches", "clocks", "autotune"):
+        if k in b:
+            line[k] = b[k]
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
-def run_serve(args):
-    """Config 4: continuously batched build+trace serving; p50/p99 latency and aggregate rates."""
+def measure_serve(duration_s=None, local=0, rank=0, **server_opts):
+    """Config 4: a Poisson stream (2,000 req/s) of build+trace requests (meshes logU[1e3, 2e6]
+    triangles from a pool of clustered and strand meshes, 65,536 rays each) through the server;
+    p50/p90/p99 latency from submission to completion, aggregate Mtris/s and Mrays/s."""
     import threading as th
 
     import torch
@@ -615,9 +760,9 @@ def run_serve(args):
     from bvh_gb300 import meshgen
     from bvh_gb300.serve import Server
 
-    ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    kw = dict(WORKLOADS["c4_serve"][1])
+    if duration_s:
+        kw["duration_s"] = duration_s
     g = np.random.default_rng(7 + rank)
     sizes = np.exp(g.uniform(np.log(kw["lo"]), np.log(kw["hi"]), kw["pool"])).astype(np.int64)
     pool = []
@@ -634,8 +779,10 @@ def run_serve(args):
     nr = kw["rays"]
     free_hits = [[torch.empty(nr, dtype=torch.float32).pin_memory()] +
                  [torch.empty(nr, dtype=torch.int32).pin_memory() for _ in range(4)] for _ in range(512)]
-    sv = Server(budget_bytes=kw["budget_gb"] << 30, slots=kw["slots"], morton_bits=30, device=local,
+    opts = dict(budget_bytes=kw["budget_gb"] << 30, slots=kw["slots"], morton_bits=30, device=local,
                 max_triangles=int(max(p[0] for p in pool)), max_rays=nr)
+    opts.update(server_opts)
+    sv = Server(**opts)
     results = []
     in_use = {}
     lock = th.Lock()
@@ -672,6 +819,7 @@ def run_serve(args):
     arrivals = np.cumsum(g.exponential(1.0 / kw["rate"], n_req))
     picks = g.integers(0, len(pool), n_req)
     with ClockSampler(local) as clk:
+        clk.mark("timed_start")
         t0 = time.perf_counter()
         for tag in range(n_req):
             delay = t0 + arrivals[tag] - time.perf_counter()
@@ -680,7 +828,7 @@ def run_serve(args):
             submit(tag, int(picks[tag]))
         while len(results) < n_req:
             time.sleep(0.005)
-        t1 = time.perf_counter()
+        clk.mark("timed_end")
     stop.set()
     pt.join(timeout=10)
     st = sv.stats()
@@ -691,17 +839,13 @@ def run_serve(args):
     rays = sum(r["rays"] for r in results)
     span = (max(r["t_done_ns"] for r in results) - min(r["t_submit_ns"] for r in results)) / 1e9
     ok = all(r["status"] == 0 for r in results)
-    line = {
-        "metric": "serve p50/p99 request latency (ms) + aggregate Mtris/s and Mrays/s",
-        "value": round(float(np.percentile(lat, 50)), 3), "unit": "ms (p50 latency)", "n_gpus": ws,
-        "steps": n_req, "warmup": len(pool), "ms_per_step": round(float(lat.mean()), 3),
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32",
-        "data": "synthetic (seeded pool of clustered/strand meshes, bvh_gb300/meshgen.py)",
-        "config": {"workload": args.workload, "description": desc, "requests": n_req, "rate_per_s": kw["rate"],
-                   "pool_meshes": len(pool), "slots": kw["slots"], "budget_gb": kw["budget_gb"],
-                   "rays_per_request": nr, "offered_mtris_per_s": round(float(np.mean(sizes)) * kw["rate"] / 1e6, 1)},
+    return {
+        "requests": n_req, "rate_per_s": kw["rate"], "duration_s": kw["duration_s"], "pool_meshes": len(pool),
+        "slots": opts["slots"], "budget_gb": kw["budget_gb"], "rays_per_request": nr,
+        "offered_mtris_per_s": round(float(np.mean(sizes)) * kw["rate"] / 1e6, 1),
         "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p90": round(float(np.percentile(lat, 90)), 3),
                        "p99": round(float(np.percentile(lat, 99)), 3), "max": round(float(lat.max()), 3),
+                       "mean": round(float(lat.mean()), 3),
                        "queue_p50": round(float(np.percentile(queue_ms, 50)), 3),
                        "queue_p99": round(float(np.percentile(queue_ms, 99)), 3)},
         "throughput": {"mtris_per_s": round(tris / span / 1e6, 1), "mrays_per_s": round(rays / span / 1e6, 1),
@@ -710,8 +854,29 @@ def run_serve(args):
         "e2e": {"value": round(tris / span / 1e6, 1), "unit": "Mtris/s",
                 "h2d_bytes_per_step": int(np.mean([36 * pool[k][0] + 24 * nr for k in picks])),
                 "d2h_bytes_per_step": 20 * nr},
-        "gpu_launches": n_req * 14,
         "clocks": clk.summary(),
+    }
+
+
+def run_serve(args):
+    """Config 4 as its own bench line."""
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
+    r = measure_serve(None, local, rank)
+    line = {
+        "metric": "serve p50/p99 request latency (ms) + aggregate Mtris/s and Mrays/s",
+        "value": r["latency_ms"]["p50"], "unit": "ms (p50 latency)", "n_gpus": ws,
+        "steps": r["requests"], "warmup": r["pool_meshes"], "ms_per_step": r["latency_ms"]["mean"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32",
+        "data": "synthetic (seeded pool of clustered/strand meshes, bvh_gb300/meshgen.py)",
+        "config": {"workload": args.workload, "description": desc, "requests": r["requests"],
+                   "rate_per_s": r["rate_per_s"], "pool_meshes": r["pool_meshes"], "slots": r["slots"],
+                   "budget_gb": r["budget_gb"], "rays_per_request": r["rays_per_request"],
+                   "offered_mtris_per_s": r["offered_mtris_per_s"], "parallelism": f"replicas x{ws}"},
+        "latency_ms": r["latency_ms"], "throughput": r["throughput"], "server": r["server"], "e2e": r["e2e"],
+        "gpu_launches": r["requests"] * 14, "clocks": r["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -728,17 +893,26 @@ def run_reference_batched(args, ref, sample_meshes: int = 256):
     k = min(sample_meshes, counts.shape[0])
     parts = [[a[offsets[m]:offsets[m + 1]] for a in arrays] for m in range(k)]
     R = ref.RefRunner(fast=True)
+    ploc = algo == "ploc_batched"
+
+    def one(part):  # (getLastBuildTimeMS, wall ms of build())
+        if ploc:
+            _, _, _, ms, _ = R.ploc(part, radius)
+            return float(ms[0]), float(ms[5])
+        _, _, ms = R.lbvh(part)
+        return float(ms[0]), float(ms[6])
+
     for m in range(min(8, k)):
-        R.lbvh(parts[m])
+        one(parts[m])
     tris = int(offsets[k])
     builds, walls = [], []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             b = w = 0.0
             for m in range(k):
-                _, _, ms = R.lbvh(parts[m])
-                b += float(ms[0])
-                w += float(ms[6])
+                bm, wm = one(parts[m])
+                b += bm
+                w += wm
             builds.append(b)
             walls.append(w)
     b = float(np.mean(builds))
@@ -750,8 +924,8 @@ def run_reference_batched(args, ref, sample_meshes: int = 256):
         "ms_per_step": round(b, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+u32", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
         "config": {"workload": args.workload, "description": desc, "meshes_sampled": k, "triangles_sampled": tris,
-                   "reference_builder": "LBVHBuilderCUDA (30-bit) once per mesh: the reference has no batched "
-                                        "builder",
+                   "reference_builder": (f"PLOCBuilderCUDA(r={radius})" if ploc else "LBVHBuilderCUDA (30-bit)")
+                                        + " once per mesh: the reference has no batched builder",
                    "how": "the reference's own kernels (its .cu files compiled unmodified, Release flags) "
                           "replayed in its host order; value from the sum of its getLastBuildTimeMS"},
         "e2e": {"value": round(tris / (w / 1e3) / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": 36 * tris,
@@ -777,7 +951,7 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving path (no request "
                           "queue, admission or overlapped builds); nothing of it can run this workload"}))
         return
-    if algo == "lbvh_batched":
+    if algo in ("lbvh_batched", "ploc_batched"):
         run_reference_batched(args, ref)
         return
     mesh = make_mesh(args.workload)
@@ -816,7 +990,7 @@ def run_reference(args):
         ref_algo += f"; the reference has no multi-pass LBVH+, so this is its 1-pass build, not the " \
                     f"workload's {treelet_rounds(args.workload)} passes"
     line = {
-        "impl": "reference", "metric": "build Mtris/s (device-resident) + %HBM roofline",
+        "impl": "reference", "metric": METRIC,
         "value": round(value, 2), "unit": "Mtris/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(b, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+u32", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
@@ -849,6 +1023,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c1_lbvh63")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: skip the pageable e2e, LBVH-30, batched and serving blocks")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default sort variants")
     ap.add_argument("--host-loops", action="store_true",
                     help="drive the PLOC / LBVH+ device loops from the host (for profilers; slower)")
@@ -857,7 +1033,7 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif WORKLOADS[args.workload][2] == "lbvh_batched":
+    elif WORKLOADS[args.workload][2] in ("lbvh_batched", "ploc_batched"):
         run_batched(args)
     elif WORKLOADS[args.workload][2] == "serve":
         run_serve(args)

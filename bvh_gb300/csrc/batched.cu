@@ -8,7 +8,8 @@
 //   k_seg_morton  key = mesh << 30 | code30, triangle boxes, radix histograms
 //   k_onesweep    ceil((30 + mesh bits) / 8) stable passes over the 64-bit keys
 //   k_delta/k_emit  segmented Karras emission: delta = -1 across meshes, node ids per mesh
-// The sequence has no host synchronisation and can be captured into a CUDA graph.
+// The sequence has no host synchronisation and can be captured into a CUDA graph.  Batched PLOC
+// (ploc.cu) shares everything up to the sort and then clusters all meshes at once.
 #include <algorithm>
 #include <cstring>
 
@@ -144,9 +145,11 @@ __global__ void __launch_bounds__(256) k_seg_morton(MeshPtrs m, const SegItem* _
   }
 }
 
-cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets, uint32_t count,
-                          const SegItem* d_items, uint32_t n_items, float* d_mbox, uint32_t* d_indices,
-                          cudaStream_t st, StageEvents* evs) {
+// The per-mesh boxes, keys and sort shared by the batched LBVH and PLOC: on return the sorted
+// (mesh, code30, index) order is in ws.vals[*fb] (global triangle indices) and ws.keys[*fb]
+// holds the high 32 bits of the keys.
+cudaError_t batched_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, uint32_t count, const SegItem* d_items,
+                           uint32_t n_items, float* d_mbox, cudaStream_t st, StageEvents* evs, BatchedSort* out) {
   cudaError_t e = workspace_reserve(ws, n, st);
   if (e != cudaSuccess) return e;
   ScratchLayout L = scratch_layout(ws.cap_n);
@@ -182,10 +185,25 @@ cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const ui
                                nullptr, st)) != cudaSuccess)
     return e;
   if (evs && evs->use) cudaEventRecord(evs->ev[3], st);
-  k_delta_seg_split<<<div_up(n, 256), 256, 0, st>>>(hkeys, ws.vals[fb], lows, d_offsets, shift0, ws.delta, n);
+  out->fb = fb;
+  out->shift0 = shift0;
+  out->lows = lows;
+  return cudaSuccess;
+}
+
+cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets, uint32_t count,
+                          const SegItem* d_items, uint32_t n_items, float* d_mbox, uint32_t* d_indices,
+                          cudaStream_t st, StageEvents* evs) {
+  BatchedSort bs;
+  cudaError_t e = batched_prefix(ws, m, n, count, d_items, n_items, d_mbox, st, evs, &bs);
+  if (e != cudaSuccess) return e;
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  const int fb = bs.fb;
+  const uint32_t* hkeys = reinterpret_cast<const uint32_t*>(ws.keys[fb]);
+  k_delta_seg_split<<<div_up(n, 256), 256, 0, st>>>(hkeys, ws.vals[fb], bs.lows, d_offsets, bs.shift0, ws.delta, n);
   uint32_t* fcount = ws.scratch + L.counters + kFrontierCounter;
   uint2* frontier = reinterpret_cast<uint2*>(ws.keys[fb ^ 1]);  // the sort's other key buffer
-  const SegBatch seg{hkeys, d_offsets, 30 - shift0};
+  const SegBatch seg{hkeys, d_offsets, 30 - bs.shift0};
   k_emit<SegBatch, false, kEmitTile><<<div_up(n, kEmitTile), kEmitTile, 0, st>>>(
       ws.delta, nullptr, ws.vals[fb], ws.boxes, ws.nodes, n, seg, d_indices, frontier, fcount, kEmitMaxSteps);
   k_emit_climb<SegBatch, false><<<std::min<uint32_t>(div_up(n, 256), 152 * 16), 256, 0, st>>>(

@@ -17,6 +17,7 @@ struct BatchGraph {
   cudaGraphExec_t exec = nullptr;
   const float* ptrs[9] = {};
   uint32_t n = 0, count = 0;
+  int32_t algo = -1, radius = 0, max_iter = 0;
   std::vector<uint32_t> offsets;
 };
 
@@ -214,6 +215,7 @@ static bvh_status check_status_word(bvh_ctx* ctx) {
   uint32_t s = *ctx->h_status;
   if (s & (kStatusSortTimeout | kStatusClimbTimeout)) return BVH_ERR_TIMEOUT;
   if (s & kStatusNoProgress) return BVH_ERR_NO_PROGRESS;
+  if (s & kStatusBadInput) return BVH_ERR_DEVICE;  // a kernel skipped an index outside its buffer
   return BVH_OK;
 }
 
@@ -390,12 +392,16 @@ static cudaError_t reserve_batch(Workspace& ws, uint32_t n, uint32_t count, size
 }
 
 static cudaError_t enqueue_batch(bvh_ctx* ctx, const MeshPtrs& m, uint32_t n, uint32_t count, size_t words,
-                                 cudaStream_t st, bool events) {
+                                 const bvh_params* params, cudaStream_t st, bool events) {
   Workspace& ws = ctx->ws;
   cudaError_t e = cudaMemcpyAsync(ws.bat_offsets, ws.bat_offsets_h, words * 4, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
   StageEvents none;
   const SegItem* items = reinterpret_cast<const SegItem*>(ws.bat_offsets + items_at(count));
+  if (params->algo == BVH_ALGO_PLOC)
+    return batched_ploc_build(ws, m, n, ws.bat_offsets, count, items, ws.bat_items, ws.bat_mbox, ws.bat_indices,
+                              params->ploc_radius, (uint32_t)params->max_iterations, st, events ? &ctx->evs : &none,
+                              params->reserved[1] == BVH_HOST_DRIVEN_LOOPS);
   return batched_build(ws, m, n, ws.bat_offsets, count, items, ws.bat_items, ws.bat_mbox, ws.bat_indices, st,
                        events ? &ctx->evs : &none);
 }
@@ -403,7 +409,9 @@ static cudaError_t enqueue_batch(bvh_ctx* ctx, const MeshPtrs& m, uint32_t n, ui
 extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_params* params, void* stream,
                                         bvh_tree* out) {
   if (!ctx || !batch || !out || !params || !mesh_ok(&batch->mesh) || !batch->offsets) return BVH_ERR_INVALID_ARG;
-  if (params->algo != BVH_ALGO_LBVH || params->morton_bits != 30) return BVH_ERR_UNSUPPORTED;
+  if (!valid_params(params)) return BVH_ERR_INVALID_ARG;
+  const bool ploc = params->algo == BVH_ALGO_PLOC;
+  if (!ploc && (params->algo != BVH_ALGO_LBVH || params->morton_bits != 30)) return BVH_ERR_UNSUPPORTED;
   const uint32_t n = batch->mesh.n, count = batch->count;
   if (count == 0 || count > n || count > (1u << 24) || batch->offsets[0] != 0 || batch->offsets[count] != n)
     return BVH_ERR_INVALID_ARG;
@@ -419,6 +427,13 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   const size_t words = items_at(count) + 4 * (size_t)n_items;
   cudaError_t e = reserve_batch(ws, n, count, words, st);
   if (e != cudaSuccess) return from_cuda(e);
+  if (ploc) {  // everything a capture may not do: allocations, kernel attributes
+    if ((e = workspace_reserve_ploc(ws, n)) != cudaSuccess) return from_cuda(e);
+    if ((e = ploc_prepare(params->ploc_radius)) != cudaSuccess) return from_cuda(e);
+    if (params->reserved[1] == BVH_HOST_DRIVEN_LOOPS && !ws.ploc_host &&
+        (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess)
+      return from_cuda(e);
+  }
   // the device copy reads the pinned staging buffer when it executes: rewrite it only when the
   // layout changed, after the work that may still read it has finished
   const bool changed = ws.bat_items != n_items ||
@@ -429,10 +444,13 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
     ws.bat_items = n_items;
   }
   MeshPtrs m = mesh_ptrs(&batch->mesh);
-  const bool use_graph = params->reserved[0] == BVH_BATCH_USE_GRAPH;
+  // (a host-driven PLOC loop reads the device between iterations, so it cannot be captured)
+  const bool use_graph = params->reserved[0] == BVH_BATCH_USE_GRAPH &&
+                         !(ploc && params->reserved[1] == BVH_HOST_DRIVEN_LOOPS);
   if (use_graph) {
     BatchGraph& g = ctx->bgraph;
-    bool same = g.exec && !changed && g.n == n && g.count == count && memcmp(g.ptrs, m.v, sizeof(g.ptrs)) == 0;
+    bool same = g.exec && !changed && g.n == n && g.count == count && memcmp(g.ptrs, m.v, sizeof(g.ptrs)) == 0 &&
+                g.algo == params->algo && g.radius == params->ploc_radius && g.max_iter == params->max_iterations;
     if (!same) {
       if (g.exec) cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -441,7 +459,7 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
       cudaGraph_t graph = nullptr;
       if ((e = cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return from_cuda(e);
-      cudaError_t e2 = enqueue_batch(ctx, m, n, count, words, ctx->capture_stream, false);
+      cudaError_t e2 = enqueue_batch(ctx, m, n, count, words, params, ctx->capture_stream, false);
       e = cudaStreamEndCapture(ctx->capture_stream, &graph);
       if (e2 != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return from_cuda(e2); }
       if (e != cudaSuccess) return from_cuda(e);
@@ -451,15 +469,20 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
       memcpy(g.ptrs, m.v, sizeof(g.ptrs));
       g.n = n;
       g.count = count;
+      g.algo = params->algo;
+      g.radius = params->ploc_radius;
+      g.max_iter = params->max_iterations;
     }
     cudaEventRecord(ctx->evs.ev[0], st);
     if ((e = cudaGraphLaunch(g.exec, st)) != cudaSuccess) return from_cuda(e);
     for (int k = 1; k <= 5; ++k) cudaEventRecord(ctx->evs.ev[k], st);
   } else {
-    if ((e = enqueue_batch(ctx, m, n, count, words, st, true)) != cudaSuccess) return from_cuda(e);
+    if ((e = enqueue_batch(ctx, m, n, count, words, params, st, true)) != cudaSuccess) return from_cuda(e);
   }
   ScratchLayout L = scratch_layout(ws.cap_n);
   cudaMemcpyAsync(ctx->h_status, ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
+  if (ploc)  // iterations and live-cluster sum, read at bvh_sync
+    cudaMemcpyAsync(ctx->h_status + 4, ws.scratch + L.ploc, 16 * 4, cudaMemcpyDeviceToHost, st);
   cudaEventRecord(ctx->evs.ev[6], st);
   ctx->last_stream = st;
   ctx->have_timing = true;

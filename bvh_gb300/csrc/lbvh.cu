@@ -545,6 +545,8 @@ void workspace_free(Workspace& ws) {
   cudaFree(ws.vals[0]); cudaFree(ws.vals[1]);
   cudaFree(ws.boxes); cudaFree(ws.nodes); cudaFree(ws.slots); cudaFree(ws.scratch); cudaFree(ws.delta);
   if (ws.ploc_exec) cudaGraphExecDestroy(ws.ploc_exec);
+  if (ws.ploc_seg_exec) cudaGraphExecDestroy(ws.ploc_seg_exec);
+  if (ws.aux_stream) cudaStreamDestroy(ws.aux_stream);
   if (ws.ploc_host) cudaFreeHost(ws.ploc_host);
   if (ws.tl_exec) cudaGraphExecDestroy(ws.tl_exec);
   cudaFree(ws.cbox[0]); cudaFree(ws.cbox[1]); cudaFree(ws.cid[0]); cudaFree(ws.cid[1]); cudaFree(ws.nbr);

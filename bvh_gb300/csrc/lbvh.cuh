@@ -41,6 +41,12 @@ struct Workspace {
   int ploc_key_r = 0;
   const void* ploc_key_nodes = nullptr;
   const void* ploc_key_scratch = nullptr;
+  cudaStream_t aux_stream = nullptr;  // a second stream for capturing loop bodies
+  // the batched PLOC loop graph and what it was made for
+  cudaGraphExec_t ploc_seg_exec = nullptr;
+  uint32_t ploc_seg_key_n = 0, ploc_seg_key_count = 0;
+  int ploc_seg_key_r = 0;
+  const void* ploc_seg_key[4] = {};
   // device-side mesh copy for host-pointer builds
   float* mesh_dev = nullptr;
   uint32_t mesh_cap = 0;
@@ -120,6 +126,8 @@ cudaError_t prepare_kernels();
 // Grow `ws` to hold n triangles (cudaMalloc; synchronising).
 cudaError_t workspace_reserve(Workspace& ws, uint32_t n, cudaStream_t st);
 cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n);
+// PLOC kernel attributes for a radius (shared memory of the neighbour search); before any capture.
+cudaError_t ploc_prepare(int radius);
 void workspace_free(Workspace& ws);
 
 // Tree statistics on the device (BVHEvaluator, src/evaluator.cpp:38-113).
@@ -160,6 +168,22 @@ struct SegItem {
   uint32_t mesh, begin, end, pad;
 };
 constexpr uint32_t kSegChunk = 16384;
+
+// The shared prefix of the batched builds: per-mesh boxes, keys mesh << 30 | code30, stable sort.
+struct BatchedSort {
+  int fb = 0;              // ping-pong buffer holding the sorted keys (high 32 bits) and indices
+  int shift0 = 0;          // key bits below the sorted high 32
+  uint32_t* lows = nullptr;  // those low bits by original index (inside the node buffer)
+};
+cudaError_t batched_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, uint32_t count, const SegItem* d_items,
+                           uint32_t n_items, float* d_mbox, cudaStream_t st, StageEvents* evs, BatchedSort* out);
+
+// Batched PLOC(radius) over the same layout: every mesh's tree equals its single build.  d_mbox
+// (8 words per mesh) holds the per-mesh loop state once the keys are made.
+cudaError_t batched_ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets,
+                               uint32_t count, const SegItem* d_items, uint32_t n_items, float* d_mbox,
+                               uint32_t* d_indices, int radius, uint32_t max_iter, cudaStream_t st,
+                               StageEvents* evs, bool host_loop);
 
 // Batched LBVH-30 over `count` meshes concatenated in one SoA (offsets and work items on the device).
 cudaError_t batched_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets, uint32_t count,

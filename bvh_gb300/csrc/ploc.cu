@@ -26,6 +26,7 @@ constexpr int kPlocTile = kPlocThreads * kPlocIpt;
 //   [0] live clusters  [1] next node id  [2] count ticket  [3] buffer parity
 //   [4] survivors (next iteration)  [5] next node id (next iteration)  [6] iterations  [7] cap
 //   [8..9] sum of live clusters over iterations (64-bit)  [10] go on (host-driven loop)
+//   [11] meshes (1 for a single build): the loop ends at one cluster per mesh
 struct PlocBufs {
   Box* cbox[2];
   int32_t* cid[2];
@@ -35,6 +36,17 @@ struct PlocBufs {
   Node* nodes;
   uint32_t* ctrl;
   uint32_t* status;
+};
+
+// Batched builds: per-mesh loop state.  seg[par * count + m] = position of mesh m's first live
+// cluster (a mesh's first cluster always survives: it is never the larger index of a pair);
+// id_base[m] = the mesh-local id of this iteration's first new node minus the global merge
+// rank of the mesh's first cluster, so a merge's local id is id_base[m] + its global rank.
+struct PlocSeg {
+  const uint32_t* offsets;  // count + 1 triangle offsets
+  uint32_t* seg;            // 2 * count (ping-pong with the cluster buffers' parity)
+  uint32_t* id_base;        // count
+  uint32_t count;
 };
 
 __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __restrict__ tri_boxes, PlocBufs B, uint32_t n,
@@ -49,6 +61,7 @@ __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __rest
     B.ctrl[7] = cap;
     B.ctrl[8] = 0;
     B.ctrl[9] = 0;
+    B.ctrl[11] = 1;
   }
   if (i >= n) return;
   uint32_t prim = __ldg(sidx + i);
@@ -81,7 +94,16 @@ __device__ __forceinline__ float pair_area(float4 xa, float4 xb, float4 ja, floa
                 __fsub_rn(fmaxf(xb.z, jb.z), fminf(xa.z, ja.z)));
 }
 
-template <int PER>
+// Batched builds keep each cluster's mesh in the w lane of its lo corner: a pair from two meshes
+// has no area (+inf never wins), which clips every window at its mesh's boundary exactly as a
+// single build's window ends at the ends of its cluster array.
+template <bool SEG>
+__device__ __forceinline__ float pair_d(float4 xa, float4 xb, float4 ja, float4 jb) {
+  if (SEG && __float_as_int(xa.w) != __float_as_int(ja.w)) return __int_as_float(0x7f800000);
+  return pair_area(xa, xb, ja, jb);
+}
+
+template <int PER, bool SEG>
 __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, const Box* __restrict__ cbox,
                                          float4* sw) {
   constexpr int TILE = kPlocThreads * PER;
@@ -130,7 +152,7 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
 #pragma unroll
           for (int kk = 0; kk < kNnKc; ++kk) {
             const int jw = xi + r + k0 + kk;
-            const float d = pair_area(xa[m], xb[m], s_lo[jw], s_hi[jw]);
+            const float d = pair_d<SEG>(xa[m], xb[m], s_lo[jw], s_hi[jw]);
             if (d < fd[m]) {
               fd[m] = d;
               fj[m] = (int)base + xi + k0 + kk;
@@ -146,7 +168,7 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
             const int kmax = min(kc, (int)c - 1 - ((int)base + xi) - k0 + 1);  // j = base + xi + k < c
             for (int kk = 0; kk < kmax; ++kk) {
               const int jw = xi + r + k0 + kk;
-              const float d = pair_area(xa[m], xb[m], s_lo[jw], s_hi[jw]);
+              const float d = pair_d<SEG>(xa[m], xb[m], s_lo[jw], s_hi[jw]);
               if (d < fd[m]) {  // increasing j: the first of equal areas stays
                 fd[m] = d;
                 fj[m] = (int)base + xi + k0 + kk;
@@ -164,7 +186,7 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
           const int h = (int)base + p - k;  // the halo cluster; p is the tile-relative target
           if (h >= 0) {
             const int hw = p - k + r;
-            sD[kk * TILE + p] = pair_area(s_lo[hw], s_hi[hw], s_lo[p + r], s_hi[p + r]);
+            sD[kk * TILE + p] = pair_d<SEG>(s_lo[hw], s_hi[hw], s_lo[p + r], s_hi[p + r]);
           }
         }
       }
@@ -210,6 +232,7 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
   }
 }
 
+template <bool SEG>
 __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   extern __shared__ float4 sw[];
   const uint32_t c = __ldcg(B.ctrl + 0);
@@ -218,9 +241,9 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   // one tile's latency: smaller tiles (2 or 1 clusters per thread) then spread it over more
   // blocks.  The result does not depend on the tiling.
   const uint32_t g = gridDim.x * (uint32_t)kPlocThreads;
-  if (c > 2u * g) nn_tiles<kNnPer>(B, r, c, cbox, sw);
-  else if (c > g) nn_tiles<2>(B, r, c, cbox, sw);
-  else nn_tiles<1>(B, r, c, cbox, sw);
+  if (c > 2u * g) nn_tiles<kNnPer, SEG>(B, r, c, cbox, sw);
+  else if (c > g) nn_tiles<2, SEG>(B, r, c, cbox, sw);
+  else nn_tiles<1, SEG>(B, r, c, cbox, sw);
 }
 
 // Merge mutual pairs (i < j keeps position i, :211-264) and compact the survivors (:267-293),
@@ -252,7 +275,7 @@ __device__ __forceinline__ void ploc_step(PlocBufs B, cudaGraphConditionalHandle
   B.ctrl[0] = nc;
   B.ctrl[1] = B.ctrl[5];
   B.ctrl[3] ^= 1u;
-  bool go = nc > 1;
+  bool go = nc > B.ctrl[11];
   if (go && (nc >= c || it >= cap)) {  // no mutual pair anywhere, or the cap: stop and report
     atomicOr(B.status, kStatusNoProgress);
     go = false;
@@ -297,12 +320,13 @@ __device__ __forceinline__ void ploc_scan_tiles(PlocBufs B, uint32_t tiles, unsi
 // Rounds of 32 clusters per warp in a merge tile (8 at most, 2048 clusters per tile): the fewest
 // whose tiles still fill the grid, so that late iterations (few clusters) spread over all blocks.
 // k_ploc_count and k_ploc_scatter run on the same grid and agree on it.
-__device__ __forceinline__ int ploc_rounds(uint32_t c) {
+__device__ __forceinline__ int ploc_rounds(uint32_t c, uint32_t grid) {
 #pragma unroll
   for (int r = 1; r < kPlocRounds; r <<= 1)
-    if (div_up(c, (uint32_t)(kPlocThreads * r)) <= gridDim.x) return r;
+    if (div_up(c, (uint32_t)(kPlocThreads * r)) <= grid) return r;
   return kPlocRounds;
 }
+__device__ __forceinline__ int ploc_rounds(uint32_t c) { return ploc_rounds(c, gridDim.x); }
 
 template <int R>
 __device__ __forceinline__ void count_tiles(const PlocBufs& B, uint32_t c, uint32_t tiles, unsigned long long* s_w) {
@@ -365,11 +389,12 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_count(PlocBufs B) {
   if (threadIdx.x == 0) B.ctrl[2] = 0;
 }
 
-template <int R>
+template <int R, bool SEG>
 __device__ __forceinline__ void scatter_tiles(const PlocBufs& B, uint32_t c, uint32_t next, uint32_t tiles,
                                               const Box* __restrict__ cin, const int32_t* __restrict__ idin,
                                               Box* __restrict__ cout, int32_t* __restrict__ idout,
-                                              Node* __restrict__ nodes, unsigned long long* s_w) {
+                                              Node* __restrict__ nodes, unsigned long long* s_w,
+                                              const PlocSeg& S) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -428,13 +453,29 @@ __device__ __forceinline__ void scatter_tiles(const PlocBufs& B, uint32_t c, uin
         float4 a = lo[g], b = hi[g];
         int32_t nid = id[g];
         if (m) {
-          a = make_float4(fminf(a.x, jlo[g].x), fminf(a.y, jlo[g].y), fminf(a.z, jlo[g].z), 0.f);
+          // a batched cluster keeps its mesh in lo.w; nodes get 0 there
+          a = make_float4(fminf(a.x, jlo[g].x), fminf(a.y, jlo[g].y), fminf(a.z, jlo[g].z), SEG ? a.w : 0.f);
           b = make_float4(fmaxf(b.x, jhi[g].x), fmaxf(b.y, jhi[g].y), fmaxf(b.z, jhi[g].z), 0.f);
-          nid = (int32_t)(next + mpos + __popc(mb[r] & lt));
-          float4* np = reinterpret_cast<float4*>(nodes + nid);
-          np[0] = a;
-          np[1] = b;
-          reinterpret_cast<int4*>(np + 2)[0] = make_int4(id[g], jid[g], 0, 0);
+          float4* np;
+          np = nullptr;
+          if constexpr (SEG) {
+            const uint32_t mesh = (uint32_t)__float_as_int(a.w);
+            const uint32_t local = mesh < S.count ? __ldcg(S.id_base + mesh) + mpos + __popc(mb[r] & lt) : ~0u;
+            nid = (int32_t)local;  // children and cluster ids are mesh-local
+            if (mesh < S.count) {
+              const uint32_t off = __ldg(S.offsets + mesh), nm = __ldg(S.offsets + mesh + 1) - off;
+              if (local < 2 * nm - 1) np = reinterpret_cast<float4*>(nodes + (2 * (size_t)off - mesh) + local);
+            }
+            if (!np) atomicOr(B.status, kStatusBadInput);  // outside its mesh's range: skipped
+          } else {
+            nid = (int32_t)(next + mpos + __popc(mb[r] & lt));
+            np = reinterpret_cast<float4*>(nodes + nid);
+          }
+          if (np) {
+            np[0] = make_float4(a.x, a.y, a.z, 0.f);
+            np[1] = b;
+            reinterpret_cast<int4*>(np + 2)[0] = make_int4(id[g], jid[g], 0, 0);
+          }
         }
         if (v) {
           const uint32_t o = vpos + __popc(vb[r] & lt);
@@ -450,7 +491,8 @@ __device__ __forceinline__ void scatter_tiles(const PlocBufs& B, uint32_t c, uin
   }
 }
 
-__global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
+template <bool SEG>
+__global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B, PlocSeg S) {
   __shared__ unsigned long long s_w[kPlocThreads / 32];
   const uint32_t c = __ldcg(B.ctrl + 0);
   const uint32_t next = __ldcg(B.ctrl + 1);
@@ -464,10 +506,95 @@ __global__ void __launch_bounds__(kPlocThreads, 3) k_ploc_scatter(PlocBufs B) {
   const int R = ploc_rounds(c);
   const uint32_t tiles = div_up(c, (uint32_t)(kPlocThreads * R));
   switch (R) {
-    case 1: scatter_tiles<1>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
-    case 2: scatter_tiles<2>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
-    case 4: scatter_tiles<4>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
-    default: scatter_tiles<kPlocRounds>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w); break;
+    case 1: scatter_tiles<1, SEG>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w, S); break;
+    case 2: scatter_tiles<2, SEG>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w, S); break;
+    case 4: scatter_tiles<4, SEG>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w, S); break;
+    default: scatter_tiles<kPlocRounds, SEG>(B, c, next, tiles, cin, idin, cout, idout, nodes, s_w, S); break;
+  }
+}
+
+// Batched builds, between k_ploc_count (whose last block has scanned the tile totals) and
+// k_ploc_scatter: per mesh, the global merge and survivor ranks of its first live cluster, from
+// its tile's prefix and the stored ballots before it in the tile (at most 64 words).  From them
+// the mesh's id base (a merge's local id = id_base + its global rank) and the position of its
+// first cluster after the compaction.  mg_grid = the grid of k_ploc_count / k_ploc_scatter,
+// which fixes their tiling.
+__global__ void __launch_bounds__(256) k_ploc_seg(PlocBufs B, PlocSeg S, uint32_t mg_grid) {
+  const uint32_t c = __ldcg(B.ctrl + 0);
+  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
+  const int R = ploc_rounds(c, mg_grid);
+  const uint32_t per_tile = (uint32_t)kPlocThreads * (uint32_t)R, per_warp = 32u * (uint32_t)R;
+  const uint32_t* seg_in = S.seg + (size_t)par * S.count;
+  uint32_t* seg_out = S.seg + (size_t)(par ^ 1u) * S.count;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < S.count; m += gridDim.x * blockDim.x) {
+    const uint32_t p = seg_in[m];
+    const uint32_t pe = m + 1 < S.count ? seg_in[m + 1] : c;
+    if (p >= c || pe > c || pe <= p) {  // inconsistent loop state: no ranks for this mesh
+      atomicOr(B.status, kStatusBadInput);
+      S.id_base[m] = ~0u;
+      seg_out[m] = p;
+      continue;
+    }
+    const uint32_t nm = __ldg(S.offsets + m + 1) - __ldg(S.offsets + m);
+    const uint32_t tile = p / per_tile, o = p - tile * per_tile;
+    const uint32_t w = o / per_warp, rr = (o % per_warp) >> 5, lane = o & 31u;
+    const uint2* fl = B.flags + (size_t)tile * (kPlocThreads / 32) * R;
+    uint32_t mc = 0, vc = 0;
+    for (uint32_t k = 0; k < w * (uint32_t)R + rr; ++k) {  // whole rounds before p's round
+      const uint2 f = __ldcg(fl + k);
+      mc += __popc(f.x);
+      vc += __popc(f.y);
+    }
+    const uint2 f = __ldcg(fl + w * (uint32_t)R + rr);
+    const uint32_t below = (1u << lane) - 1u;
+    mc += __popc(f.x & below);
+    vc += __popc(f.y & below);
+    const unsigned long long pre = __ldcg(B.desc + tile);
+    const uint32_t G = (uint32_t)(pre >> 31) + mc, V = (uint32_t)(pre & 0x7fffffffull) + vc;
+    // local id of the next new node = n_m + merges so far = 2 n_m - live clusters
+    S.id_base[m] = 2u * nm - (pe - p) - G;
+    seg_out[m] = V;
+  }
+}
+
+// Batched builds: leaves and clusters from the sorted order of all meshes (positions
+// [offsets[m], offsets[m+1]) hold mesh m's triangles in its own Morton order).  Mesh m's tree
+// starts at node 2 offsets[m] - m; its leaves are nodes 0 .. n_m - 1 of that range (mesh-local
+// ids, as a single build numbers them); indices get mesh-local triangle numbers.
+__global__ void __launch_bounds__(256) k_ploc_init_seg(const uint32_t* __restrict__ sidx,
+                                                       const Box* __restrict__ tri_boxes, PlocBufs B, PlocSeg S,
+                                                       const SegItem* __restrict__ items, uint32_t n_items,
+                                                       uint32_t n, uint32_t cap, uint32_t* __restrict__ d_indices) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    B.ctrl[0] = n;
+    B.ctrl[1] = n;
+    B.ctrl[2] = 0;
+    B.ctrl[3] = 0;
+    B.ctrl[6] = 0;
+    B.ctrl[7] = cap;
+    B.ctrl[8] = 0;
+    B.ctrl[9] = 0;
+    B.ctrl[11] = S.count;
+  }
+  for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const SegItem w = items[it];
+    const uint32_t off = __ldg(S.offsets + w.mesh);
+    const size_t base = 2 * (size_t)off - w.mesh;
+    if (w.begin == off && threadIdx.x == 0) S.seg[w.mesh] = off;
+    for (uint32_t p = w.begin + threadIdx.x; p < w.end; p += blockDim.x) {
+      const uint32_t prim = __ldg(sidx + p);
+      const float4* bp = reinterpret_cast<const float4*>(tri_boxes + prim);
+      const float4 lo = __ldg(bp), hi = __ldg(bp + 1);
+      float4* cb = reinterpret_cast<float4*>(B.cbox[0] + p);
+      cb[0] = make_float4(lo.x, lo.y, lo.z, __int_as_float((int)w.mesh));
+      cb[1] = hi;
+      B.cid[0][p] = (int32_t)(p - off);
+      float4* np = reinterpret_cast<float4*>(B.nodes + base + (p - off));
+      np[0] = make_float4(lo.x, lo.y, lo.z, 0.f);
+      np[1] = hi;
+      reinterpret_cast<int4*>(np + 2)[0] = make_int4((int32_t)((prim - off) | kLeafBit), -1, 0, 0);
+      d_indices[p] = prim - off;
+    }
   }
 }
 
@@ -505,12 +632,55 @@ __global__ void k_ploc_root(Node* __restrict__ nodes, uint32_t total, const uint
   }
 }
 
+// Batched builds: each mesh's root (its last node) moves to the start of its range, as in
+// k_ploc_root; work items split the node ranges evenly.
+__global__ void __launch_bounds__(256) k_ploc_root_seg(Node* __restrict__ nodes, const SegItem* __restrict__ items,
+                                                       uint32_t n_items, PlocSeg S, const uint32_t* __restrict__ ctrl) {
+  if (__ldcg(ctrl + 0) != S.count) return;
+  for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const SegItem w = items[it];
+    const uint32_t off = __ldg(S.offsets + w.mesh), nm = __ldg(S.offsets + w.mesh + 1) - off;
+    Node* mn = nodes + (2 * (size_t)off - w.mesh);
+    const uint32_t R = 2 * nm - 2;
+    auto fix = [&](int32_t c) -> int32_t {
+      if (c < 0) return c;
+      if (c == 0) return (int32_t)R;
+      if (c == (int32_t)R) return 0;
+      return c;
+    };
+    const uint32_t k0 = 2 * (w.begin - off), k1 = min(2 * (w.end - off), 2 * nm - 1);
+    for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      if (k == 0) {
+        Node a = mn[0], b = mn[R];
+        if (b.left >= 0) { b.left = fix(b.left); b.right = fix(b.right); }
+        if (a.left >= 0) { a.left = fix(a.left); a.right = fix(a.right); }
+        mn[0] = b;
+        mn[R] = a;
+      } else if (k != R) {
+        int2 ch = *reinterpret_cast<int2*>(&mn[k].left);
+        if (ch.x >= 0) {
+          int2 nc = make_int2(fix(ch.x), fix(ch.y));
+          if (nc.x != ch.x || nc.y != ch.y) *reinterpret_cast<int2*>(&mn[k].left) = nc;
+        }
+      }
+    }
+  }
+}
+
 cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
+  if (!ws.aux_stream) {  // captures the batched loop body while a batch is being captured
+    cudaError_t e = cudaStreamCreateWithFlags(&ws.aux_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+  }
   if (n <= ws.ploc_cap && ws.nbr) return cudaSuccess;
   uint32_t cap = std::max<uint32_t>(n, 1024);
   if (ws.ploc_exec) {
     cudaGraphExecDestroy(ws.ploc_exec);
     ws.ploc_exec = nullptr;
+  }
+  if (ws.ploc_seg_exec) {  // both loop graphs hold the cluster buffers' addresses
+    cudaGraphExecDestroy(ws.ploc_seg_exec);
+    ws.ploc_seg_exec = nullptr;
   }
   cudaFree(ws.cbox[0]); cudaFree(ws.cbox[1]); cudaFree(ws.cid[0]); cudaFree(ws.cid[1]); cudaFree(ws.nbr);
   ws.cbox[0] = ws.cbox[1] = nullptr; ws.cid[0] = ws.cid[1] = nullptr; ws.nbr = nullptr; ws.ploc_cap = 0;
@@ -533,9 +703,27 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
 
 static size_t nn_smem(int radius) { return 32 * (kNnTile + 2 * (size_t)radius) + 4 * (size_t)kNnKc * kNnTile; }
 
-// The loop as a graph: WHILE(cond) { nn; merge; step }.  Grids are persistent (sized for n), the
-// kernels read the live cluster count from the control words.
-static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n, int radius, cudaGraphExec_t* out) {
+static uint32_t nn_grid_for(uint32_t n) { return std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3)); }
+static uint32_t mg_grid_for(uint32_t n) { return std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8)); }
+
+// One clustering iteration: neighbours, tile counts + scan, (batched: per-mesh ranks), merge +
+// compaction, loop control.  Grids are persistent (sized for n); the kernels read the live
+// cluster count from the control words.
+template <bool SEG, bool GRAPH>
+static void enqueue_iteration(const PlocBufs& B, const PlocSeg& S, uint32_t n, int radius, cudaStream_t st,
+                              cudaGraphConditionalHandle handle) {
+  const uint32_t mg_grid = mg_grid_for(n);
+  k_ploc_nn<SEG><<<nn_grid_for(n), kPlocThreads, nn_smem(radius), st>>>(B, radius);
+  k_ploc_count<<<mg_grid, kPlocThreads, 0, st>>>(B);
+  if constexpr (SEG) k_ploc_seg<<<std::max<uint32_t>(1, std::min<uint32_t>(div_up(S.count, 256), 152 * 4)), 256, 0,
+                                  st>>>(B, S, mg_grid);
+  k_ploc_scatter<SEG><<<mg_grid, kPlocThreads, 0, st>>>(B, S);
+  k_ploc_step<GRAPH><<<1, 32, 0, st>>>(B, handle);
+}
+
+// The loop as a graph: WHILE(cond) { one iteration }.
+template <bool SEG>
+static cudaError_t make_loop_graph(const PlocBufs& B, const PlocSeg& S, uint32_t n, int radius, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
   if (e != cudaSuccess) return e;
@@ -555,12 +743,7 @@ static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n,
     if ((e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
       break;
-    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3));
-    const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
-    k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), cs>>>(B, radius);
-    k_ploc_count<<<mg_grid, kPlocThreads, 0, cs>>>(B);
-    k_ploc_scatter<<<mg_grid, kPlocThreads, 0, cs>>>(B);
-    k_ploc_step<true><<<1, 32, 0, cs>>>(B, handle);
+    enqueue_iteration<SEG, true>(B, S, n, radius, cs, handle);
     cudaGraph_t captured = nullptr;
     cudaError_t e2 = cudaGetLastError();
     e = cudaStreamEndCapture(cs, &captured);
@@ -573,12 +756,7 @@ static cudaError_t make_loop_graph(Workspace& ws, const PlocBufs& B, uint32_t n,
   return e;
 }
 
-cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter, cudaStream_t st,
-                       StageEvents* evs, uint32_t** out_indices, bool host_loop) {
-  cudaError_t e = workspace_reserve(ws, n, st);
-  if (e != cudaSuccess) return e;
-  if ((e = workspace_reserve_ploc(ws, n)) != cudaSuccess) return e;
-  ScratchLayout L = scratch_layout(ws.cap_n);
+static PlocBufs ploc_bufs(Workspace& ws, const ScratchLayout& L) {
   PlocBufs B;
   B.cbox[0] = ws.cbox[0];
   B.cbox[1] = ws.cbox[1];
@@ -591,11 +769,29 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   B.nodes = ws.nodes;
   B.ctrl = ws.scratch + L.ploc;
   B.status = ws.scratch + L.status;
-  if (nn_smem(radius) > 48 * 1024) {
-    if ((e = cudaFuncSetAttribute(k_ploc_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem(radius))) !=
-        cudaSuccess)
-      return e;
-  }
+  return B;
+}
+
+template <bool SEG>
+static cudaError_t set_nn_smem(int radius) {
+  if (nn_smem(radius) <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(k_ploc_nn<SEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem(radius));
+}
+
+cudaError_t ploc_prepare(int radius) {
+  cudaError_t e = set_nn_smem<false>(radius);
+  return e == cudaSuccess ? set_nn_smem<true>(radius) : e;
+}
+
+cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter, cudaStream_t st,
+                       StageEvents* evs, uint32_t** out_indices, bool host_loop) {
+  cudaError_t e = workspace_reserve(ws, n, st);
+  if (e != cudaSuccess) return e;
+  if ((e = workspace_reserve_ploc(ws, n)) != cudaSuccess) return e;
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  const PlocBufs B = ploc_bufs(ws, L);
+  const PlocSeg none{};
+  if ((e = set_nn_smem<false>(radius)) != cudaSuccess) return e;
   // every iteration that makes progress removes at least one cluster, so n bounds the loop
   const uint32_t cap = max_iter > 0 ? (uint32_t)max_iter : n;
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
@@ -605,7 +801,7 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
     if (!same) {
       if (ws.ploc_exec) cudaGraphExecDestroy(ws.ploc_exec);
       ws.ploc_exec = nullptr;
-      if ((e = make_loop_graph(ws, B, n, radius, &ws.ploc_exec)) != cudaSuccess) return e;
+      if ((e = make_loop_graph<false>(B, none, n, radius, &ws.ploc_exec)) != cudaSuccess) return e;
       ws.ploc_key_n = n;
       ws.ploc_key_r = radius;
       ws.ploc_key_nodes = ws.nodes;
@@ -619,13 +815,8 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap);
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
   if (n > 1 && host_loop) {
-    const uint32_t nn_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3));
-    const uint32_t mg_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8));
     for (uint32_t it = 0; it < cap; ++it) {
-      k_ploc_nn<<<nn_grid, kPlocThreads, nn_smem(radius), st>>>(B, radius);
-      k_ploc_count<<<mg_grid, kPlocThreads, 0, st>>>(B);
-      k_ploc_scatter<<<mg_grid, kPlocThreads, 0, st>>>(B);
-      k_ploc_step<false><<<1, 32, 0, st>>>(B, cudaGraphConditionalHandle{});
+      enqueue_iteration<false, false>(B, none, n, radius, st, cudaGraphConditionalHandle{});
       if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
           (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return e;
@@ -636,6 +827,104 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
     if ((e = cudaGraphLaunch(ws.ploc_exec, st)) != cudaSuccess) return e;
     k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
   }
+  if (evs && evs->use) cudaEventRecord(evs->ev[5], st);
+  return cudaGetLastError();
+}
+
+// Batched PLOC: the batched prefix (per-mesh boxes and keys, one sort), then every mesh's
+// clustering in the same iterations -- windows clipped at mesh boundaries, merges numbered per
+// mesh -- until each mesh has one cluster, then each mesh's root fix.  Mesh m's result equals its
+// single build: the same leaves, the same neighbours in every iteration, the same node ids
+// relative to its range [2 offsets[m] - m, 2 offsets[m+1] - m - 1).  A mesh that has finished
+// keeps its one cluster, which has no neighbour.  The loop is a CUDA graph WHILE node (or a
+// host loop); the iteration count is the largest of the meshes' own.
+cudaError_t batched_ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, const uint32_t* d_offsets,
+                               uint32_t count, const SegItem* d_items, uint32_t n_items, float* d_mbox,
+                               uint32_t* d_indices, int radius, uint32_t max_iter, cudaStream_t st,
+                               StageEvents* evs, bool host_loop) {
+  cudaError_t e = workspace_reserve(ws, n, st);
+  if (e != cudaSuccess) return e;
+  if ((e = workspace_reserve_ploc(ws, n)) != cudaSuccess) return e;
+  ScratchLayout L = scratch_layout(ws.cap_n);
+  const PlocBufs B = ploc_bufs(ws, L);
+  PlocSeg S;
+  S.offsets = d_offsets;
+  S.seg = reinterpret_cast<uint32_t*>(d_mbox);  // the mesh boxes are dead once the keys are made
+  S.id_base = S.seg + 2 * (size_t)count;
+  S.count = count;
+  if ((e = set_nn_smem<true>(radius)) != cudaSuccess) return e;
+  const uint32_t cap = max_iter > 0 ? max_iter : n;
+  if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
+  const bool loop = n > count;  // some mesh has two or more triangles
+  cudaStreamCaptureStatus cst0 = cudaStreamCaptureStatusNone;
+  if ((e = cudaStreamIsCapturing(st, &cst0)) != cudaSuccess) return e;
+  if (loop && !host_loop && cst0 == cudaStreamCaptureStatusNone) {
+    const bool same = ws.ploc_seg_exec && ws.ploc_seg_key_n == n && ws.ploc_seg_key_count == count &&
+                      ws.ploc_seg_key_r == radius && ws.ploc_seg_key[0] == ws.nodes &&
+                      ws.ploc_seg_key[1] == ws.scratch && ws.ploc_seg_key[2] == d_offsets &&
+                      ws.ploc_seg_key[3] == d_mbox;
+    if (!same) {
+      if (ws.ploc_seg_exec) cudaGraphExecDestroy(ws.ploc_seg_exec);
+      ws.ploc_seg_exec = nullptr;
+      if ((e = make_loop_graph<true>(B, S, n, radius, &ws.ploc_seg_exec)) != cudaSuccess) return e;
+      ws.ploc_seg_key_n = n;
+      ws.ploc_seg_key_count = count;
+      ws.ploc_seg_key_r = radius;
+      ws.ploc_seg_key[0] = ws.nodes;
+      ws.ploc_seg_key[1] = ws.scratch;
+      ws.ploc_seg_key[2] = d_offsets;
+      ws.ploc_seg_key[3] = d_mbox;
+    }
+  }
+  BatchedSort bs;
+  if ((e = batched_prefix(ws, m, n, count, d_items, n_items, d_mbox, st, evs, &bs)) != cudaSuccess) return e;
+  const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(n_items, 152 * 8));
+  k_ploc_init_seg<<<grid, 256, 0, st>>>(ws.vals[bs.fb], ws.boxes, B, S, d_items, n_items, n, cap, d_indices);
+  if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
+  if (loop && host_loop) {
+    for (uint32_t it = 0; it < cap; ++it) {
+      enqueue_iteration<true, false>(B, S, n, radius, st, cudaGraphConditionalHandle{});
+      if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+      if (!*ws.ploc_host) break;
+    }
+  } else if (loop) {
+    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edata = nullptr;
+    size_t nd = 0;
+    if ((e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &cg, &deps, &edata, &nd)) != cudaSuccess) return e;
+    if (cst == cudaStreamCaptureStatusActive) {
+      // the batch is being captured into one graph: the loop becomes a conditional node of it
+      cudaGraphConditionalHandle h;
+      if ((e = cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node;
+      if ((e = cudaGraphAddNode(&node, cg, deps, edata, nd, &cp)) != cudaSuccess) return e;
+      cudaStream_t aux = ws.aux_stream;
+      if (!aux) return cudaErrorInvalidResourceHandle;  // made by workspace_reserve_ploc, before any capture
+      if ((e = cudaStreamBeginCaptureToGraph(aux, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return e;
+      enqueue_iteration<true, true>(B, S, n, radius, aux, h);
+      cudaGraph_t body = nullptr;
+      const cudaError_t e2 = cudaGetLastError();
+      if ((e = cudaStreamEndCapture(aux, &body)) != cudaSuccess) return e;
+      if (e2 != cudaSuccess) return e2;
+      if ((e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+          cudaSuccess)
+        return e;
+    } else if ((e = cudaGraphLaunch(ws.ploc_seg_exec, st)) != cudaSuccess) {
+      return e;
+    }
+  }
+  if (loop) k_ploc_root_seg<<<grid, 256, 0, st>>>(ws.nodes, d_items, n_items, S, B.ctrl);
   if (evs && evs->use) cudaEventRecord(evs->ev[5], st);
   return cudaGetLastError();
 }

@@ -184,10 +184,13 @@ bvh_status bvh_last_timing(bvh_ctx* ctx, bvh_timing* out);
 /* Wait for the last build and report device-side errors (bounded waits that gave up). */
 bvh_status bvh_sync(bvh_ctx* ctx);
 
-/* Build every mesh of a batch (LBVH, 30-bit Morton).  Result: 2*mesh.n - count nodes; mesh m's
- * tree occupies nodes [2*offsets[m] - m, 2*offsets[m+1] - m - 1) with its root first and child
- * indices relative to that first node, and indices [offsets[m], offsets[m+1]) hold mesh-local
- * original triangle indices -- each mesh's part equals bvh_build_device of that mesh alone.
+/* Build every mesh of a batch: LBVH with 30-bit Morton codes, or PLOC(ploc_radius) (other
+ * combinations: BVH_ERR_UNSUPPORTED).  Result: 2*mesh.n - count nodes; mesh m's tree occupies
+ * nodes [2*offsets[m] - m, 2*offsets[m+1] - m - 1) with its root first and child indices relative
+ * to that first node, and indices [offsets[m], offsets[m+1]) hold mesh-local original triangle
+ * indices -- each mesh's part equals bvh_build_device of that mesh alone.  PLOC clusters all
+ * meshes in the same iterations (as many as the slowest mesh needs; bvh_last_timing reports
+ * them).  With BVH_BATCH_USE_GRAPH the whole build, PLOC's loop included, is one graph launch.
  * Asynchronous on `stream`. */
 bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_params* params, void* stream,
                              bvh_tree* out);
@@ -208,8 +211,11 @@ bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
  * fixed __device__ array inside the library (about 17 MB per GPU that loads it, held until
  * exit), so n may be at most 262,144 (BVH_ERR_INVALID_ARG beyond).  morton_bits: 30, 60 or 63;
  * the result equals bvh_build_device's.  Asynchronous on `stream`.  The first call on a device
- * looks up the array's device address; make that first call before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race, so serialise them. */
+ * also sets kernel attributes; make that first call before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race, so serialise them.  Device-side errors go
+ * unreported here: BVH_OK means the kernels were launched.  (The radix sort's bounded look-back
+ * wait, a safety net that normal operation never reaches, reports through bvh_sync on the
+ * context path only.) */
 bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t morton_bits, bvh_node* nodes, uint32_t* indices,
                                  void* stream);
 
