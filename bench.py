@@ -74,6 +74,10 @@ WORKLOADS = {
                            "pool": 32, "budget_gb": 40, "slots": 16}, "serve", 30, 0,
                  "Poisson stream (2,000 req/s) of build+trace requests, meshes logU[1e3, 2e6] triangles, "
                  "65,536 rays each, 40 GB HBM budget"),
+    "c4_serve_batched": ("serve", {"rate": 2000.0, "duration_s": 3.0, "lo": 1000, "hi": 2_000_000, "rays": 65536,
+                                   "pool": 32, "budget_gb": 40, "slots": 4}, "serve_batched", 30, 0,
+                         "config 4's stream served in batched ticks: every waiting request that fits joins one "
+                         "gather + batched LBVH build + traversal + scatter launch sequence"),
     "c0_lbvh30": ("uniform_small", {"n": 100_000, "seed": 0}, "lbvh", 30, 0,
                   "100k uniform triangles, LBVH 30-bit"),
 }
@@ -389,6 +393,12 @@ def run_ours(args):
             stages.append((t.bounds_ms, t.morton_ms, t.sort_ms, t.emit_ms, t.optimize_ms, t.total_ms))
             ploc_iters, ploc_csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
             tree_height = int(t.tree_height)
+        # a short timed region gets few clock samples: keep building (untimed, the same build)
+        # until the sampled window around it spans at least 150 ms
+        while time.perf_counter() - clk.marks["open"] < 0.15:
+            for _ in range(8):
+                ctx.build_device(ptrs, n, params, s)
+            torch.cuda.synchronize(dev)
     elapsed_ms = ev0.elapsed_time(ev1)
     if ws > 1:
         tt = torch.tensor([elapsed_ms], device=dev)
@@ -575,27 +585,45 @@ def run_ours(args):
                                           autotune=not args.no_autotune)
         line["batched_ploc"] = measure_batched(3, args.warmup, local, rank, autotune=False, algo="ploc", radius=25)
         line["serve"] = measure_serve(1.0, local, rank)
+        for k in ("latencies_ms", "span_s", "tris", "rays"):
+            line["serve"].pop(k)
+        line["serve"]["mode"] = "per-request slots (16 streams, one build + trace per request)"
+        line["serve_batched"] = measure_serve(1.0, local, rank, batched=True, slots=4)
+        for k in ("latencies_ms", "span_s", "tris", "rays"):
+            line["serve_batched"].pop(k)
+        line["serve_batched"]["mode"] = ("batched ticks (4 slots; each batch: one gather, one batched LBVH build, "
+                                         "one traversal launch, one scatter)")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
 
 
-def measure_batched(steps, warmup, local=0, rank=0, autotune=True, algo="lbvh", radius=25, check_meshes=16):
+def measure_batched(steps, warmup, local=0, rank=0, autotune=True, algo="lbvh", radius=25, check_meshes=16,
+                    world=1, barrier=None):
     """Config 3: 4,096 meshes (counts logU[64, 262144]) in one batched, graph-replayed build vs a
     per-mesh loop of single builds on the same GPU and the same device-resident data.  Also checks
-    that sampled meshes' trees equal their single builds bit for bit."""
+    that sampled meshes' trees equal their single builds bit for bit.  With world > 1 ranks the
+    batch has 4,096 x world meshes, shared out by shard.assign (balanced by triangle count, no
+    collective on the data path); this rank builds its share, and `barrier` brackets the timed
+    region."""
     import ctypes
     import torch
 
     import bvh_gb300
     from bvh_gb300 import _capi as C
-    from bvh_gb300 import meshgen
+    from bvh_gb300 import meshgen, shard
 
     dev = torch.device("cuda", local)
     kw = WORKLOADS["c3_batched"][1]
-    counts = meshgen.batch_counts(kw["meshes"], kw["lo"], kw["hi"], seed=4)
-    mesh, offsets = meshgen.batch(counts, seed=5 + rank)
+    if world > 1:
+        all_counts = meshgen.batch_counts(kw["meshes"] * world, kw["lo"], kw["hi"], seed=4)
+        mine = shard.assign(all_counts, world)[rank]
+        counts = all_counts[mine]
+        mesh, offsets = meshgen.batch_subset(all_counts, mine, seed=5)
+    else:
+        counts = meshgen.batch_counts(kw["meshes"], kw["lo"], kw["hi"], seed=4)
+        mesh, offsets = meshgen.batch(counts, seed=5)
     n = mesh.size()
     count = offsets.shape[0] - 1
     ctx = bvh_gb300.Context(local)
@@ -613,6 +641,8 @@ def measure_batched(steps, warmup, local=0, rank=0, autotune=True, algo="lbvh", 
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(dev)
+        if barrier:
+            barrier()
         clk.mark("timed_start")
         ev0.record(stream)
         for _ in range(steps):
@@ -620,6 +650,8 @@ def measure_batched(steps, warmup, local=0, rank=0, autotune=True, algo="lbvh", 
         ev1.record(stream)
         torch.cuda.synchronize(dev)
         clk.mark("timed_end")
+        if barrier:
+            barrier()
         ms = ev0.elapsed_time(ev1) / steps
         # stage breakdown without the graph
         tree = ctx.build_batched(ptrs, offsets, params, s, use_graph=False)
@@ -725,20 +757,37 @@ def measure_batched(steps, warmup, local=0, rank=0, autotune=True, algo="lbvh", 
 
 
 def run_batched(args):
-    """Config 3 as its own bench line."""
+    """Config 3 as its own bench line.  Under torchrun: 4,096 meshes per rank, shared out by
+    shard.assign; value = all ranks' triangles / the slowest rank's time."""
     import torch
+    import torch.distributed as dist
     ws, rank, local = dist_info()
     torch.cuda.set_device(local)
+    barrier = None
+    if ws > 1:
+        dist.init_process_group("nccl")
+        barrier = dist.barrier
     gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
     b = measure_batched(args.steps, args.warmup, local, rank, autotune=not args.no_autotune,
-                        algo="ploc" if algo == "ploc_batched" else "lbvh", radius=radius or 25)
+                        algo="ploc" if algo == "ploc_batched" else "lbvh", radius=radius or 25, world=ws,
+                        barrier=barrier)
+    ms, tris, meshes = b["ms_per_step"], b["triangles"], b["meshes"]
+    if ws > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        u = torch.tensor([tris, meshes], dtype=torch.float64, device="cuda")
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        tris, meshes = int(u[0].item()), int(u[1].item())
     line = {
         "metric": "batched build Mtris/s (device-resident) vs per-mesh loop",
-        "value": round(b["value"] * ws, 2), "unit": "Mtris/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "value": round(tris / (ms / 1e3) / 1e6, 2), "unit": "Mtris/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic (seeded generator, bvh_gb300/meshgen.py)",
-        "config": {"workload": args.workload, "description": desc, "meshes": b["meshes"], "triangles": b["triangles"],
-                   "min_mesh": b["min_mesh"], "max_mesh": b["max_mesh"], "parallelism": f"replicas x{ws}",
+        "config": {"workload": args.workload, "description": desc, "meshes": meshes, "triangles": tris,
+                   "min_mesh": b["min_mesh"], "max_mesh": b["max_mesh"],
+                   "parallelism": f"shards x{ws} (shard.assign: 4,096 meshes per rank, balanced by triangles)"
+                   if ws > 1 else "1 GPU",
                    "l2": "inputs (4.8 GB) exceed the 129 MB L2; no flush"},
     }
     for k in ("per_mesh_loop", "speedup_batched_over_loop", "equal_to_single_builds", "stage_ms", "roofline",
@@ -747,23 +796,27 @@ def run_batched(args):
             line[k] = b[k]
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
 
 
-def measure_serve(duration_s=None, local=0, rank=0, **server_opts):
+def measure_serve(duration_s=None, local=0, rank=0, world=1, barrier=None, **server_opts):
     """Config 4: a Poisson stream (2,000 req/s) of build+trace requests (meshes logU[1e3, 2e6]
     triangles from a pool of clustered and strand meshes, 65,536 rays each) through the server;
-    p50/p90/p99 latency from submission to completion, aggregate Mtris/s and Mrays/s."""
+    p50/p90/p99 latency from submission to completion, aggregate Mtris/s and Mrays/s.  With
+    world > 1 ranks the stream carries 2,000 x world req/s and shard.stream_share gives each rank
+    its balanced share (no collective on the data path); `barrier` aligns the ranks' clocks."""
     import threading as th
 
     import torch
 
-    from bvh_gb300 import meshgen
+    from bvh_gb300 import meshgen, shard
     from bvh_gb300.serve import Server
 
     kw = dict(WORKLOADS["c4_serve"][1])
     if duration_s:
         kw["duration_s"] = duration_s
-    g = np.random.default_rng(7 + rank)
+    g = np.random.default_rng(7)  # the same pool and stream on every rank
     sizes = np.exp(g.uniform(np.log(kw["lo"]), np.log(kw["hi"]), kw["pool"])).astype(np.int64)
     pool = []
     for k, n in enumerate(sizes):
@@ -815,17 +868,21 @@ def measure_serve(duration_s=None, local=0, rank=0, **server_opts):
     while len(results) < len(pool):
         time.sleep(0.01)
     results.clear()
-    n_req = int(kw["rate"] * kw["duration_s"])
-    arrivals = np.cumsum(g.exponential(1.0 / kw["rate"], n_req))
-    picks = g.integers(0, len(pool), n_req)
+    n_all = int(kw["rate"] * world * kw["duration_s"])
+    arrivals = np.cumsum(g.exponential(1.0 / (kw["rate"] * world), n_all))
+    picks = g.integers(0, len(pool), n_all)
+    mine = shard.stream_share(sizes[picks], world, rank) if world > 1 else np.arange(n_all)
+    n_req = len(mine)
+    if barrier:
+        barrier()
     with ClockSampler(local) as clk:
         clk.mark("timed_start")
         t0 = time.perf_counter()
-        for tag in range(n_req):
-            delay = t0 + arrivals[tag] - time.perf_counter()
+        for tag, q in enumerate(mine):
+            delay = t0 + arrivals[q] - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
-            submit(tag, int(picks[tag]))
+            submit(tag, int(picks[q]))
         while len(results) < n_req:
             time.sleep(0.005)
         clk.mark("timed_end")
@@ -840,6 +897,7 @@ def measure_serve(duration_s=None, local=0, rank=0, **server_opts):
     span = (max(r["t_done_ns"] for r in results) - min(r["t_submit_ns"] for r in results)) / 1e9
     ok = all(r["status"] == 0 for r in results)
     return {
+        "latencies_ms": lat, "span_s": span, "tris": tris, "rays": rays,
         "requests": n_req, "rate_per_s": kw["rate"], "duration_s": kw["duration_s"], "pool_meshes": len(pool),
         "slots": opts["slots"], "budget_gb": kw["budget_gb"], "rays_per_request": nr,
         "offered_mtris_per_s": round(float(np.mean(sizes)) * kw["rate"] / 1e6, 1),
@@ -852,19 +910,39 @@ def measure_serve(duration_s=None, local=0, rank=0, **server_opts):
                        "requests_per_s": round(n_req / span, 1), "all_ok": ok},
         "server": {k: int(v) for k, v in st.items()},
         "e2e": {"value": round(tris / span / 1e6, 1), "unit": "Mtris/s",
-                "h2d_bytes_per_step": int(np.mean([36 * pool[k][0] + 24 * nr for k in picks])),
+                "h2d_bytes_per_step": int(np.mean([36 * pool[int(picks[q])][0] + 24 * nr for q in mine])),
                 "d2h_bytes_per_step": 20 * nr},
         "clocks": clk.summary(),
     }
 
 
 def run_serve(args):
-    """Config 4 as its own bench line."""
+    """Config 4 as its own bench line.  Under torchrun: 2,000 req/s per rank, the stream shared
+    out by shard.stream_share; latencies are gathered from every rank."""
     import torch
+    import torch.distributed as dist
     ws, rank, local = dist_info()
     torch.cuda.set_device(local)
+    barrier = None
+    if ws > 1:
+        dist.init_process_group("nccl")
+        barrier = dist.barrier
     gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
-    r = measure_serve(None, local, rank)
+    r = measure_serve(None, local, rank, world=ws, barrier=barrier, batched=algo == "serve_batched",
+                      slots=kw["slots"])
+    if ws > 1:  # every rank's latencies and totals
+        parts = [None] * ws
+        dist.all_gather_object(parts, (list(r["latencies_ms"]), r["span_s"], r["tris"], r["rays"], r["requests"]))
+        lat = np.concatenate([np.asarray(p[0]) for p in parts])
+        span = max(p[1] for p in parts)
+        r["latency_ms"].update({"p50": round(float(np.percentile(lat, 50)), 3),
+                                "p90": round(float(np.percentile(lat, 90)), 3),
+                                "p99": round(float(np.percentile(lat, 99)), 3), "max": round(float(lat.max()), 3),
+                                "mean": round(float(lat.mean()), 3)})
+        r["throughput"]["mtris_per_s"] = round(sum(p[2] for p in parts) / span / 1e6, 1)
+        r["throughput"]["mrays_per_s"] = round(sum(p[3] for p in parts) / span / 1e6, 1)
+        r["requests"] = sum(p[4] for p in parts)
+        r["e2e"]["value"] = r["throughput"]["mtris_per_s"]
     line = {
         "metric": "serve p50/p99 request latency (ms) + aggregate Mtris/s and Mrays/s",
         "value": r["latency_ms"]["p50"], "unit": "ms (p50 latency)", "n_gpus": ws,
@@ -874,12 +952,15 @@ def run_serve(args):
         "config": {"workload": args.workload, "description": desc, "requests": r["requests"],
                    "rate_per_s": r["rate_per_s"], "pool_meshes": r["pool_meshes"], "slots": r["slots"],
                    "budget_gb": r["budget_gb"], "rays_per_request": r["rays_per_request"],
-                   "offered_mtris_per_s": r["offered_mtris_per_s"], "parallelism": f"replicas x{ws}"},
+                   "offered_mtris_per_s": r["offered_mtris_per_s"],
+                   "parallelism": f"shards x{ws} (shard.stream_share: 2,000 req/s per rank)" if ws > 1 else "1 GPU"},
         "latency_ms": r["latency_ms"], "throughput": r["throughput"], "server": r["server"], "e2e": r["e2e"],
         "gpu_launches": r["requests"] * 14, "clocks": r["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
 
 
 def run_reference_batched(args, ref, sample_meshes: int = 256):
@@ -947,7 +1028,7 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref fatbins) not built"}))
         return
     gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
-    if algo == "serve":
+    if algo in ("serve", "serve_batched"):
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving path (no request "
                           "queue, admission or overlapped builds); nothing of it can run this workload"}))
         return
@@ -1035,7 +1116,7 @@ def main():
         run_reference(args)
     elif WORKLOADS[args.workload][2] in ("lbvh_batched", "ploc_batched"):
         run_batched(args)
-    elif WORKLOADS[args.workload][2] == "serve":
+    elif WORKLOADS[args.workload][2] in ("serve", "serve_batched"):
         run_serve(args)
     else:
         run_ours(args)

@@ -71,6 +71,7 @@ class Batch(ctypes.Structure):
 
 BATCH_USE_GRAPH = 1
 HOST_DRIVEN_LOOPS = 1  # bvh_params.reserved[1]: PLOC / LBVH+ loops driven from the host
+SERVE_BATCHED = 1  # bvh_serve_config.reserved[0]: batched ticks
 
 
 class Camera(ctypes.Structure):
@@ -120,6 +121,7 @@ SIGNATURES = {
     "bvh_tree_download": (c_int, [c_void_p, POINTER(Tree), c_void_p, c_void_p, c_void_p]),
     "bvh_last_timing": (c_int, [c_void_p, POINTER(Timing)]),
     "bvh_sync": (c_int, [c_void_p]),
+    "bvh_selftest_bounded_wait": (c_int, [c_int, c_uint32]),
     "bvh_trace": (c_int, [c_void_p, c_void_p, c_uint32, POINTER(MeshSoA), POINTER(Rays), POINTER(Hits), c_void_p]),
     "bvh_trace_pinhole": (c_int, [c_void_p, c_void_p, c_uint32, POINTER(MeshSoA), POINTER(Camera), c_int32, c_int32,
                                   POINTER(Hits), c_void_p]),

@@ -168,6 +168,7 @@ cudaError_t batched_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, uint32_
   unsigned long long* run_scratch = reinterpret_cast<unsigned long long*>(
       reinterpret_cast<unsigned char*>(ws.nodes) + (((size_t)n * 4 + 15) & ~(size_t)15));
   if (evs && evs->use) cudaEventRecord(evs->ev[0], st);
+  if ((e = epoch_tick(ws, st)) != cudaSuccess) return e;
   k_seg_init<<<152 * 4, 256, 0, st>>>(d_mbox, count, ws.scratch, L);
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(n_items, 152 * 8));
   k_seg_bounds<<<grid, 256, 0, st>>>(m, d_items, n_items, d_mbox);

@@ -219,6 +219,18 @@ static bvh_status check_status_word(bvh_ctx* ctx) {
   return BVH_OK;
 }
 
+extern "C" bvh_status bvh_selftest_bounded_wait(int device, uint32_t polls) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count || polls == 0 ||
+      polls > kSpinLimit)
+    return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(device);
+  uint32_t status = 0;
+  cudaError_t e = wait_selftest(polls, &status);
+  if (e != cudaSuccess) return from_cuda(e);
+  return (status & kStatusSortTimeout) ? BVH_ERR_TIMEOUT : BVH_ERR_DEVICE;
+}
+
 extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
   if (!ctx) return BVH_ERR_INVALID_ARG;
   if (!ctx->have_timing) return BVH_OK;
@@ -474,6 +486,7 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
       g.max_iter = params->max_iterations;
     }
     cudaEventRecord(ctx->evs.ev[0], st);
+    if ((e = epoch_tick(ws, st)) != cudaSuccess) return from_cuda(e);  // the graph bumps the epoch
     if ((e = cudaGraphLaunch(g.exec, st)) != cudaSuccess) return from_cuda(e);
     for (int k = 1; k <= 5; ++k) cudaEventRecord(ctx->evs.ev[k], st);
   } else {

@@ -154,10 +154,10 @@ __device__ __forceinline__ uint32_t warp_match_bits(uint32_t d) {
 
 // Decoupled look-back over tiles (Merrill & Garland): descriptor words hold a 2-bit flag and the
 // value in one word, so relaxed loads suffice.  Predecessors are read W at a time to shorten the
-// dependent chain; an unpublished word (flag 0) is polled again, at most kSpinLimit times.
+// dependent chain; an unpublished word (flag 0) is polled again, at most `limit` times.
 template <int W, typename T>
 __device__ __forceinline__ T lookback(const T* desc, size_t stride, int64_t tile, T flag_mask, T flag_inc,
-                                      uint32_t* status, uint32_t status_bit) {
+                                      uint32_t* status, uint32_t status_bit, uint32_t limit = kSpinLimit) {
   T excl = 0;
   int64_t j = tile - 1;
   uint32_t spins = 0;
@@ -177,7 +177,7 @@ __device__ __forceinline__ T lookback(const T* desc, size_t stride, int64_t tile
     if (done) break;
     if (k < W) {
       j -= k;
-      if (++spins > kSpinLimit) {
+      if (++spins > limit) {
         atomicOr(status, status_bit);
         break;
       }

@@ -538,6 +538,34 @@ cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms)
 }
 
 // ---------------------------------------------------------------------------------------
+// self-test of the bounded device wait
+// ---------------------------------------------------------------------------------------
+// The sort's look-back waits only on tiles that started before its own, so in a build it always
+// ends.  To show that the bound works, one thread of tile 1 looks back at a tile 0 whose
+// descriptor is never published, with a short poll limit: it must give up, set the timeout bit
+// and return.  Words 0-31: descriptors (zero = unpublished); word 32: the status word.
+__device__ uint32_t g_wait_selftest[64];
+
+__global__ void k_wait_selftest(uint32_t limit) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int k = 0; k < 64; ++k) g_wait_selftest[k] = 0;
+  __threadfence();
+  lookback<1, uint32_t>(g_wait_selftest, 1, 1, ~kValMask, kFlagInc, g_wait_selftest + 32, kStatusSortTimeout, limit);
+}
+
+cudaError_t wait_selftest(uint32_t limit, uint32_t* status_out) {
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  k_wait_selftest<<<1, 32, 0, st>>>(limit);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(status_out, g_wait_selftest, 4, 32 * 4, cudaMemcpyDeviceToHost, st);
+  const cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return e != cudaSuccess ? e : e2;
+}
+
+// ---------------------------------------------------------------------------------------
 // workspace
 // ---------------------------------------------------------------------------------------
 void workspace_free(Workspace& ws) {
@@ -559,6 +587,16 @@ void workspace_free(Workspace& ws) {
 // enqueued on `st`, the stream the next build runs on, so that it is ordered before that build's
 // kernels even when `st` is a non-blocking stream (a synchronous cudaMemset would run on the
 // legacy stream, unordered with respect to non-blocking streams).
+cudaError_t epoch_tick(Workspace& ws, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cs);
+  if (e != cudaSuccess || cs != cudaStreamCaptureStatusNone) return e;
+  if (ws.epoch_builds > 0 && ws.epoch_builds % kEpochCycle == 0 && ws.slots && ws.cap_n)
+    e = cudaMemsetAsync(ws.slots, 0, (size_t)ws.cap_n * 8, st);  // no stale tag can match again
+  ws.epoch_builds++;
+  return e;
+}
+
 cudaError_t workspace_reserve(Workspace& ws, uint32_t n, cudaStream_t st) {
   if (n <= ws.cap_n && ws.scratch) return cudaSuccess;
   uint32_t cap = std::max<uint32_t>(n, 1024);
@@ -617,6 +655,8 @@ static cudaError_t lbvh_prefix(Workspace& ws, const MeshPtrs& m, uint32_t n, cud
   ScratchLayout Lz = L;
   Lz.zero_end = L.desc + (size_t)4 * div_up(std::max<uint32_t>(n, 1),
                                              (uint32_t)sort_variant_tile(ws.sort_variant)) * 256;
+  cudaError_t et = epoch_tick(ws, st);
+  if (et != cudaSuccess) return et;
   k_bounds<<<kBoundsBlocks, 256, 0, st>>>(m, n, vec4, ws.scratch, Lz);
   rec(evs, 1, st);
   const uint32_t work = vec4 ? div_up(n, 4) : n;

@@ -42,6 +42,7 @@ struct Workspace {
   const void* ploc_key_nodes = nullptr;
   const void* ploc_key_scratch = nullptr;
   cudaStream_t aux_stream = nullptr;  // a second stream for capturing loop bodies
+  uint64_t epoch_builds = 0;           // builds that bumped this workspace's epoch (epoch_tick)
   // the batched PLOC loop graph and what it was made for
   cudaGraphExec_t ploc_seg_exec = nullptr;
   uint32_t ploc_seg_key_n = 0, ploc_seg_key_count = 0;
@@ -65,6 +66,9 @@ struct Workspace {
 
 // First epoch value; every build adds kEpochStride (emission uses E, treelet round r uses E+1+r).
 constexpr uint32_t kEpochStride = 64;
+// The 32-bit epoch repeats after this many builds (it wraps to kEpochStride); the build that
+// reuses an epoch first clears the rendezvous slots (epoch_tick).
+constexpr uint64_t kEpochCycle = (1ull << 26) - 1;
 
 // Scratch layout (32-bit words, offsets from Workspace::scratch).
 struct ScratchLayout {
@@ -120,8 +124,17 @@ constexpr int kPlocSumWord = 8;
 cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStream_t st, StageEvents* evs,
                           uint32_t** sorted_idx);
 
+// Runs the sort's bounded look-back wait against a predecessor that never publishes, giving up
+// after `limit` polls; *status_out = the status word it left (kStatusSortTimeout expected).
+cudaError_t wait_selftest(uint32_t limit, uint32_t* status_out);
+
 // Kernel attributes (dynamic shared memory limits), set once per device before any capture.
 cudaError_t prepare_kernels();
+
+// Count one build that bumps the epoch; before the build that would reuse an old epoch, clear the
+// rendezvous slots on `st`.  Not counted while `st` is being captured: each launch of the graph
+// counts instead (call it before cudaGraphLaunch).
+cudaError_t epoch_tick(Workspace& ws, cudaStream_t st);
 
 // Grow `ws` to hold n triangles (cudaMalloc; synchronising).
 cudaError_t workspace_reserve(Workspace& ws, uint32_t n, cudaStream_t st);

@@ -40,7 +40,8 @@ __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
-bool g_prepared[kMaxDevices] = {};  // kernel attributes set on this device
+bool g_prepared[kMaxDevices] = {};          // kernel attributes set on this device
+uint64_t g_epoch_builds[kMaxDevices] = {};  // builds on this device's array (clears its slots on epoch reuse)
 
 // On every call, with the caller's device current: the array's device address (host code must
 // not use the symbol itself, which is only a host-side stand-in).  The lookup is cheap and is
@@ -98,6 +99,11 @@ extern "C" bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t mo
   ws.scratch_words = kScratchBytes / 4;
   if (scratch_layout(kStaticMaxTris).total > ws.scratch_words) return BVH_ERR_DEVICE;  // layout guard
   uint32_t* out_idx = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    ws.epoch_builds = g_epoch_builds[device];
+    g_epoch_builds[device] = ws.epoch_builds + 1;
+  }
   cudaError_t e = lbvh_build(ws, m, n, morton_bits, 0, reinterpret_cast<cudaStream_t>(stream), nullptr, &out_idx);
   if (e != cudaSuccess) return BVH_ERR_DEVICE;
   return out_idx == indices ? BVH_OK : BVH_ERR_DEVICE;

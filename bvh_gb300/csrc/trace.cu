@@ -372,6 +372,66 @@ cudaError_t trace_rays(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(128) k_trace_seg(const Node* __restrict__ nodes, MeshPtrs m, RayPtrs rays,
+                                                   uint32_t nr, const RaySeg* __restrict__ segs, uint32_t count,
+                                                   HitOut out) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nr) return;
+  uint32_t lo = 0, hi = count;  // the last segment whose first ray is <= r
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&segs[mid].ray_begin) <= r) lo = mid;
+    else hi = mid;
+  }
+  const RaySeg g = segs[lo];
+  MeshPtrs mm;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) mm.v[k] = m.v[k] + g.tri_base;
+  const float3 o = make_float3(__ldg(rays.o[0] + r), __ldg(rays.o[1] + r), __ldg(rays.o[2] + r));
+  const float3 d = make_float3(__ldg(rays.d[0] + r), __ldg(rays.d[1] + r), __ldg(rays.d[2] + r));
+  trace_one(o, d, nodes + g.node_base, g.n_tris ? (int)(2 * g.n_tris - 1) : 0, mm, g.n_tris, r, out);
+}
+
+cudaError_t trace_rays_batched(const Node* nodes, const MeshPtrs& m, const RayPtrs& rays, uint32_t nr,
+                               const RaySeg* segs, uint32_t count, const HitOut& out, cudaStream_t st) {
+  if (nr == 0 || count == 0) return cudaSuccess;
+  k_trace_seg<<<div_up(nr, 128), 128, 0, st>>>(nodes, m, rays, nr, segs, count, out);
+  return cudaGetLastError();
+}
+
+// One piece (64 KB) per block iteration; 16-byte accesses where both sides allow.
+__global__ void __launch_bounds__(256) k_copy_many(const CopyDesc* __restrict__ descs, uint32_t count,
+                                                   uint32_t total_pieces) {
+  for (uint32_t q = blockIdx.x; q < total_pieces; q += gridDim.x) {
+    uint32_t lo = 0, hi = count;  // the last descriptor whose first piece is <= q
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(&descs[mid].first_piece) <= q) lo = mid;
+      else hi = mid;
+    }
+    const CopyDesc c = descs[lo];
+    const uint32_t b = (q - c.first_piece) * kCopyPiece;
+    if (b >= c.n) continue;
+    const uint32_t len = min(c.n - b, kCopyPiece);
+    const float* src = c.src + b;
+    float* dst = c.dst + b;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+      const uint32_t n4 = len >> 2;
+      for (uint32_t i = threadIdx.x; i < n4; i += blockDim.x)
+        reinterpret_cast<float4*>(dst)[i] = reinterpret_cast<const float4*>(src)[i];
+      for (uint32_t i = (n4 << 2) + threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i];
+    } else {
+      for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i];
+    }
+  }
+}
+
+cudaError_t copy_many(const CopyDesc* d_descs, uint32_t count, uint32_t total_pieces, cudaStream_t st) {
+  if (count == 0 || total_pieces == 0) return cudaSuccess;
+  k_copy_many<<<std::min<uint32_t>(total_pieces, 152 * 8), 256, 0, st>>>(d_descs, count, total_pieces);
+  return cudaGetLastError();
+}
+
 cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeCam& cam,
                           const HitOut& out, cudaStream_t st) {
   uint32_t total = (uint32_t)cam.width * (uint32_t)cam.height;

@@ -35,6 +35,29 @@ struct ShadeIn {
 
 cudaError_t trace_rays(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const RayPtrs& rays,
                        uint32_t nr, const HitOut& out, cudaStream_t st);
+
+// Rays of many requests traced in one launch against a batched build (each request's tree at
+// node_base, its triangles at tri_base of the concatenated mesh, child and primitive indices
+// local to them).  segs: count + 1 entries on the device, ray_begin ascending, the last entry's
+// ray_begin = the total ray count.
+struct RaySeg {
+  uint32_t ray_begin, node_base, tri_base, n_tris;
+};
+cudaError_t trace_rays_batched(const Node* nodes, const MeshPtrs& m, const RayPtrs& rays, uint32_t nr,
+                               const RaySeg* segs, uint32_t count, const HitOut& out, cudaStream_t st);
+
+// Many float copies in one launch: each descriptor moves n floats from src to dst (either side
+// may be host memory the device can address, e.g. page-locked buffers).  The work is cut into
+// pieces of kCopyPiece floats; first_piece = the pieces of all earlier descriptors (ascending).
+constexpr uint32_t kCopyPiece = 16384;
+struct CopyDesc {
+  const float* src;
+  float* dst;
+  uint32_t n;
+  uint32_t first_piece;
+};
+inline uint32_t copy_pieces(uint32_t n) { return (n + kCopyPiece - 1) / kCopyPiece; }
+cudaError_t copy_many(const CopyDesc* d_descs, uint32_t count, uint32_t total_pieces, cudaStream_t st);
 cudaError_t trace_pinhole(const Node* nodes, int n_nodes, const MeshPtrs& m, uint32_t n_tris, const PinholeCam& cam,
                           const HitOut& out, cudaStream_t st);
 cudaError_t pinhole_rays(const PinholeCam& cam, float* ox, float* oy, float* oz, float* dx, float* dy, float* dz,

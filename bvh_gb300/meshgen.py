@@ -175,6 +175,31 @@ def batch(counts, seed: int = 5):
     return TriangleMesh.from_vertices(*arrs), offsets.astype(np.uint32)
 
 
+def batch_subset(counts, meshes, seed: int = 5):
+    """The selected meshes of a batch, concatenated: (TriangleMesh, offsets[len(meshes)+1]).  Mesh k
+    is drawn from its own generator (seed, k) as in batch() -- centroids U[0,1]^3, vertex offsets
+    U[-0.005,0.005]^3, scale logU[0.1, 10], shift U[-10, 10]^3 -- so any subset (one rank's share)
+    is reproducible on its own."""
+    counts = np.asarray(counts, np.int64)
+    meshes = np.asarray(meshes, np.int64)
+    total = int(counts[meshes].sum())
+    arrs = [np.empty((total, 3), np.float32) for _ in range(3)]
+    offsets = np.zeros(len(meshes) + 1, np.int64)
+    o = 0
+    for j, k in enumerate(meshes):
+        g = np.random.default_rng([seed, int(k)])
+        c = int(counts[k])
+        scale = np.float32(np.exp(g.uniform(np.log(0.1), np.log(10.0))))
+        off = g.uniform(-10, 10, 3).astype(np.float32)
+        cen = g.random((c, 3), dtype=np.float32)
+        for a in arrs:
+            v = cen + (g.random((c, 3), dtype=np.float32) - np.float32(0.5)) * np.float32(0.01)
+            a[o:o + c] = v * scale + off
+        o += c
+        offsets[j + 1] = o
+    return TriangleMesh.from_vertices(*arrs), offsets.astype(np.uint32)
+
+
 def scene_box(mesh: TriangleMesh):
     lo = np.array([min(mesh.v0x.min(), mesh.v1x.min(), mesh.v2x.min()),
                    min(mesh.v0y.min(), mesh.v1y.min(), mesh.v2y.min()),

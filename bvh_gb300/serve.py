@@ -16,7 +16,11 @@ from . import _capi as C
 
 class Server:
     def __init__(self, budget_bytes: int = 40 << 30, slots: int = 8, morton_bits: int = 30, device: int = 0,
-                 max_triangles: int = 0, max_rays: int = 0):
+                 max_triangles: int = 0, max_rays: int = 0, batched: bool = False, batch_requests: int = 0,
+                 batch_triangles: int = 0):
+        """batched=True: batched ticks (one gather, build, trace and scatter launch sequence for all
+        requests admitted together); otherwise one slot per request.  batch_requests and
+        batch_triangles bound a batch (0: the library's defaults)."""
         self.lib = C.load_library()
         cfg = self.lib.bvh_serve_default_config()
         cfg.hbm_budget_bytes = int(budget_bytes)
@@ -25,6 +29,9 @@ class Server:
         cfg.device = int(device)
         cfg.max_triangles = int(max_triangles)
         cfg.max_rays = int(max_rays)
+        cfg.reserved[0] = C.SERVE_BATCHED if batched else 0
+        cfg.reserved[1] = int(batch_requests)
+        cfg.reserved[2] = int(batch_triangles)
         h = ctypes.c_void_p()
         C.check(self.lib.bvh_serve_open(ctypes.byref(cfg), ctypes.byref(h)), "bvh_serve_open")
         self.handle = h

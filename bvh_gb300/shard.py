@@ -35,3 +35,9 @@ def shard_offsets(counts: Sequence[int], meshes: np.ndarray) -> np.ndarray:
     off = np.zeros(len(c) + 1, np.int64)
     np.cumsum(c, out=off[1:])
     return off.astype(np.uint32)
+
+
+def stream_share(sizes: Sequence[int], world_size: int, rank: int) -> np.ndarray:
+    """The requests of one serving stream that `rank` serves (indices in arrival order): the
+    same balanced partition by request size as assign(), so every rank derives its share alone."""
+    return assign(sizes, world_size)[rank]

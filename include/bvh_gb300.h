@@ -179,6 +179,13 @@ bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_para
 bvh_status bvh_tree_download(bvh_ctx* ctx, const bvh_tree* tree, void* stream, bvh_node* host_nodes,
                              uint32_t* host_indices);
 
+/* Self-test of the device-side bounded wait (no reference counterpart): the radix sort's
+ * look-back wait is run on `device` against a predecessor that never publishes, giving up after
+ * `polls` polls (1 .. 16,777,216).  Returns BVH_ERR_TIMEOUT -- the expected outcome: the wait
+ * ended and reported it, and the device is still usable -- or BVH_ERR_DEVICE / another error if
+ * it did not.  Synchronous; allocates nothing. */
+bvh_status bvh_selftest_bounded_wait(int device, uint32_t polls);
+
 /* Timing of the last build; waits for it to finish.  Also reports device-side errors. */
 bvh_status bvh_last_timing(bvh_ctx* ctx, bvh_timing* out);
 /* Wait for the last build and report device-side errors (bounded waits that gave up). */
@@ -220,23 +227,34 @@ bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t morton_bits, 
                                  void* stream);
 
 /* ---- serving (no reference counterpart) ----------------------------------------------------
- * A continuously batched build+trace server: requests are admitted oldest-first whenever a slot
- * is free and their device-memory estimate fits the HBM budget beside everything in flight;
- * admitted requests run concurrently (one stream and workspace per slot).  Each request uploads
- * its host mesh and rays, builds an LBVH, traces the rays and downloads the hits into the
- * caller's host buffers, which must stay valid until its result is polled (pinned buffers let
- * uploads and downloads overlap other requests).  A request's result does not depend on what
- * else is in flight. */
+ * A continuously batched build+trace server.  Each request carries a host mesh, host rays and
+ * host hit buffers (which must stay valid until its result is polled); it gets an LBVH of its
+ * mesh and the closest hits of its rays.  Requests are admitted oldest first whenever a slot is
+ * free and the memory fits the budget; admitted work overlaps on the GPU.  A request's result
+ * does not depend on what else is in flight.
+ *   per-request slots (reserved[0] = 0): each request runs alone on a slot's stream (upload,
+ *     build, trace, download); morton_bits 30, 60 or 63.
+ *   batched ticks (reserved[0] = BVH_SERVE_BATCHED): when a slot is free, every waiting request
+ *     that fits joins one batch -- one gather kernel reads all meshes and rays from the callers'
+ *     buffers (page-locked buffers, or any host memory where the GPU reads pageable memory;
+ *     others are copied), one batched LBVH build, one traversal launch, one scatter kernel writes
+ *     all hits back; requests arriving meanwhile form the next batch on another slot.  30-bit
+ *     codes only.  reserved[1] = requests per batch at most (0: 64); reserved[2] = triangles per
+ *     batch at most (0: 8,388,608; a larger single request still runs, alone).
+ * hbm_budget_bytes bounds the device memory all slots hold together, busy or idle: a slot that
+ * must grow first takes memory back from idle slots, and requests wait while it cannot. */
 typedef struct bvh_server bvh_server;
 
+#define BVH_SERVE_BATCHED 1
+
 typedef struct bvh_serve_config {
-  uint64_t hbm_budget_bytes; /* admission budget for all requests in flight */
-  int32_t slots;             /* requests in flight at most */
-  int32_t morton_bits;       /* LBVH keys: 30, 60 or 63 */
+  uint64_t hbm_budget_bytes; /* device memory all slots hold together, at most */
+  int32_t slots;             /* requests (per-request mode) or batches (batched mode) in flight at most */
+  int32_t morton_bits;       /* LBVH keys: 30, 60 or 63 (batched mode: 30) */
   int32_t device;
   uint32_t max_triangles;    /* per-slot buffers allocated up front for this size (0: grow on demand) */
   uint32_t max_rays;
-  int32_t reserved[3];
+  int32_t reserved[3];       /* [0] mode, [1] requests per batch, [2] triangles per batch (see above) */
 } bvh_serve_config;
 
 typedef struct bvh_serve_request {

@@ -1,25 +1,53 @@
 // Builds meshes through the C++ BVHBuilder adapters and prints node checksums (test program).
 // Compiled either against the reference's headers (drop-in check) or standalone.
+// Argument: a triangle count (a seeded random mesh) or the path of a mesh file (nine float32
+// arrays v0x..v2z of n entries each, back to back).
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <random>
+#include <string>
 
 #ifndef BVH_GB300_STANDALONE
 #include "evaluator.h"
 #endif
 #include "bvh_gb300_builder.hpp"
 
-int main(int argc, char** argv) {
-  const size_t n = argc > 1 ? (size_t)atol(argv[1]) : 10000;
-  TriangleMesh mesh;
+static bool load_mesh(const char* path, TriangleMesh& mesh) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  const long bytes = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  const size_t n = (size_t)bytes / 36;
   mesh.resize(n);
-  std::mt19937 g(1234);
-  std::uniform_real_distribution<float> u(0.0f, 1.0f);
-  for (size_t i = 0; i < n; ++i) {
-    float x = u(g), y = u(g), z = u(g);
-    mesh.v0x[i] = x; mesh.v0y[i] = y; mesh.v0z[i] = z;
-    mesh.v1x[i] = x + 0.004f; mesh.v1y[i] = y; mesh.v1z[i] = z;
-    mesh.v2x[i] = x; mesh.v2y[i] = y + 0.004f; mesh.v2z[i] = z + 0.002f;
+  std::vector<float>* arrays[9] = {&mesh.v0x, &mesh.v0y, &mesh.v0z, &mesh.v1x, &mesh.v1y,
+                                   &mesh.v1z, &mesh.v2x, &mesh.v2y, &mesh.v2z};
+  bool ok = true;
+  for (auto* a : arrays) ok = ok && fread(a->data(), 4, n, f) == n;
+  fclose(f);
+  return ok;
+}
+
+int main(int argc, char** argv) {
+  TriangleMesh mesh;
+  const std::string arg = argc > 1 ? argv[1] : "10000";
+  if (arg.find_first_not_of("0123456789") != std::string::npos) {
+    if (!load_mesh(arg.c_str(), mesh)) {
+      printf("error: cannot read %s\n", arg.c_str());
+      return 1;
+    }
+  } else {
+    const size_t n = (size_t)atol(arg.c_str());
+    mesh.resize(n);
+    std::mt19937 g(1234);
+    std::uniform_real_distribution<float> u(0.0f, 1.0f);
+    for (size_t i = 0; i < n; ++i) {
+      float x = u(g), y = u(g), z = u(g);
+      mesh.v0x[i] = x; mesh.v0y[i] = y; mesh.v0z[i] = z;
+      mesh.v1x[i] = x + 0.004f; mesh.v1y[i] = y; mesh.v1z[i] = z;
+      mesh.v2x[i] = x; mesh.v2y[i] = y + 0.004f; mesh.v2z[i] = z + 0.002f;
+    }
   }
   try {
   Gb300LBVHBuilder lbvh;  // constructors throw when no context can be created (no GPU)

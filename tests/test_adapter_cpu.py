@@ -9,7 +9,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIBDIR = os.path.join(ROOT, "bvh_gb300")
-REF = os.environ.get("REF_ROOT", "/root/reference")
+from oracle.ref_build import REF_ROOT as REF  # the reference tree the build recipe reads (skip if absent)
 
 
 def _build_and_run(tmp_path, flags, sources=()):

@@ -50,3 +50,44 @@ def test_two_gloo_ranks_agree_on_the_partition():
         p.join(120)
     assert all(p.exitcode == 0 for p in procs)
     assert list(out) == [1, 1]
+
+
+def _worker_shares(rank, world, port, out):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import torch
+    ok = True
+    # a serving stream: every request served by exactly one rank, loads balanced by size
+    g = np.random.default_rng(7)
+    sizes = np.exp(g.uniform(np.log(1000), np.log(2e6), 32)).astype(np.int64)
+    picks = g.integers(0, 32, 4000)
+    mine = shard.stream_share(sizes[picks], world, rank)
+    t = torch.zeros(4000, dtype=torch.int64)
+    t[torch.from_numpy(mine)] = 1
+    dist.all_reduce(t)
+    ok = ok and bool((t == 1).all())
+    # a rank's share of a batch, generated alone, equals those meshes generated together
+    counts = meshgen.batch_counts(64 * world, 64, 3000, seed=4)
+    part = shard.assign(counts, world)[rank]
+    m, offs = meshgen.batch_subset(counts, part, seed=5)
+    whole, woffs = meshgen.batch_subset(counts, np.arange(len(counts)), seed=5)
+    for j, k in enumerate(part):
+        for a, b in zip(m.arrays(), whole.arrays()):
+            ok = ok and np.array_equal(a[offs[j]:offs[j + 1]], b[woffs[k]:woffs[k + 1]])
+    ok = ok and int(offs[-1]) == int(counts[part].sum())
+    out[rank] = 1 if ok else 0
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_share_the_stream_and_the_batch():
+    ctx = mp.get_context("spawn")
+    out = ctx.Array("i", [0, 0])
+    port = 30000 + os.getpid() % 1000
+    procs = [ctx.Process(target=_worker_shares, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+    assert all(p.exitcode == 0 for p in procs)
+    assert list(out) == [1, 1]
