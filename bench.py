@@ -75,7 +75,7 @@ WORKLOADS = {
                  "Poisson stream (2,000 req/s) of build+trace requests, meshes logU[1e3, 2e6] triangles, "
                  "65,536 rays each, 40 GB HBM budget"),
     "c4_serve_batched": ("serve", {"rate": 2000.0, "duration_s": 3.0, "lo": 1000, "hi": 2_000_000, "rays": 65536,
-                                   "pool": 32, "budget_gb": 40, "slots": 4}, "serve_batched", 30, 0,
+                                   "pool": 32, "budget_gb": 40, "slots": 8}, "serve_batched", 30, 0,
                          "config 4's stream served in batched ticks: every waiting request that fits joins one "
                          "gather + batched LBVH build + traversal + scatter launch sequence"),
     "c0_lbvh30": ("uniform_small", {"n": 100_000, "seed": 0}, "lbvh", 30, 0,
@@ -588,11 +588,11 @@ def run_ours(args):
         for k in ("latencies_ms", "span_s", "tris", "rays"):
             line["serve"].pop(k)
         line["serve"]["mode"] = "per-request slots (16 streams, one build + trace per request)"
-        line["serve_batched"] = measure_serve(1.0, local, rank, batched=True, slots=4)
+        line["serve_batched"] = measure_serve(1.0, local, rank, batched=True, slots=8, batch_requests=8)
         for k in ("latencies_ms", "span_s", "tris", "rays"):
             line["serve_batched"].pop(k)
-        line["serve_batched"]["mode"] = ("batched ticks (4 slots; each batch: one gather, one batched LBVH build, "
-                                         "one traversal launch, one scatter)")
+        line["serve_batched"]["mode"] = ("batched ticks (8 slots, up to 8 requests per batch; each batch: one "
+                                         "gather, one batched LBVH build, one traversal launch, one scatter)")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -928,8 +928,8 @@ def run_serve(args):
         dist.init_process_group("nccl")
         barrier = dist.barrier
     gen, kw, algo, bits, radius, desc = WORKLOADS[args.workload]
-    r = measure_serve(None, local, rank, world=ws, barrier=barrier, batched=algo == "serve_batched",
-                      slots=kw["slots"])
+    extra = dict(batched=True, batch_requests=8) if algo == "serve_batched" else {}
+    r = measure_serve(None, local, rank, world=ws, barrier=barrier, slots=kw["slots"], **extra)
     if ws > 1:  # every rank's latencies and totals
         parts = [None] * ws
         dist.all_gather_object(parts, (list(r["latencies_ms"]), r["span_s"], r["tris"], r["rays"], r["requests"]))

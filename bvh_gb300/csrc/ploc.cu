@@ -27,6 +27,8 @@ constexpr int kPlocTile = kPlocThreads * kPlocIpt;
 //   [4] survivors (next iteration)  [5] next node id (next iteration)  [6] iterations  [7] cap
 //   [8..9] sum of live clusters over iterations (64-bit)  [10] go on (host-driven loop)
 //   [11] meshes (1 for a single build): the loop ends at one cluster per mesh
+//   [12] hand-over size: the loop stops at this many live clusters and k_ploc_tail finishes
+//        (0: no hand-over)
 struct PlocBufs {
   Box* cbox[2];
   int32_t* cid[2];
@@ -50,7 +52,7 @@ struct PlocSeg {
 };
 
 __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __restrict__ tri_boxes, PlocBufs B, uint32_t n,
-                            uint32_t cap) {
+                            uint32_t cap, uint32_t tail) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     B.ctrl[0] = n;
@@ -62,6 +64,7 @@ __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __rest
     B.ctrl[8] = 0;
     B.ctrl[9] = 0;
     B.ctrl[11] = 1;
+    B.ctrl[12] = tail;
   }
   if (i >= n) return;
   uint32_t prim = __ldg(sidx + i);
@@ -278,6 +281,8 @@ __device__ __forceinline__ void ploc_step(PlocBufs B, cudaGraphConditionalHandle
   bool go = nc > B.ctrl[11];
   if (go && (nc >= c || it >= cap)) {  // no mutual pair anywhere, or the cap: stop and report
     atomicOr(B.status, kStatusNoProgress);
+    go = false;
+  } else if (go && nc <= B.ctrl[12]) {  // few enough for k_ploc_tail, which finishes the loop
     go = false;
   }
   if constexpr (GRAPH) cudaGraphSetConditional(handle, go ? 1u : 0u);
@@ -575,6 +580,7 @@ __global__ void __launch_bounds__(256) k_ploc_init_seg(const uint32_t* __restric
     B.ctrl[8] = 0;
     B.ctrl[9] = 0;
     B.ctrl[11] = S.count;
+    B.ctrl[12] = 0;
   }
   for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
     const SegItem w = items[it];
@@ -602,6 +608,162 @@ __global__ void __launch_bounds__(256) k_ploc_init_seg(const uint32_t* __restric
 template <bool GRAPH>
 __global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
   if (threadIdx.x == 0 && blockIdx.x == 0) ploc_step<GRAPH>(B, handle);
+}
+
+// The last iterations in one block.  Once the live clusters fit in shared memory (at most
+// kTailMax, and few enough that their 2r pairs per cluster are cheap), an iteration over many
+// blocks costs mostly launch latency; this kernel runs the remaining iterations in one block of
+// kTailThreads, with the same rules and results as the kernels above: neighbour = smallest union
+// area in [x-r, x+r], smallest j on ties, +inf and NaN never winning; mutual pairs merge into
+// the smaller index, new node ids in ascending cluster order, survivors compacted in order; the
+// same stop (one cluster), no-progress and cap rules, iteration count and live-cluster sum.
+constexpr int kTailThreads = 1024;
+constexpr uint32_t kTailMax = 2048;
+constexpr uint32_t kTailPairs = 100000;  // pair areas per iteration at the hand-over, at most
+
+uint32_t ploc_tail_threshold(int radius) {
+  const uint32_t t = kTailPairs / (2u * (uint32_t)std::max(radius, 1));
+  return std::min<uint32_t>(kTailMax, std::max<uint32_t>(t, 64));
+}
+static size_t tail_smem() { return (size_t)kTailMax * (4 * 16 + 3 * 4) + 2 * 32 * 4; }
+
+__global__ void __launch_bounds__(kTailThreads, 1) k_ploc_tail(PlocBufs B, int r) {
+  extern __shared__ float4 tsm[];
+  float4* s_lo[2] = {tsm, tsm + 2 * kTailMax};
+  float4* s_hi[2] = {tsm + kTailMax, tsm + 3 * kTailMax};
+  int32_t* s_id[2] = {reinterpret_cast<int32_t*>(tsm + 4 * kTailMax),
+                      reinterpret_cast<int32_t*>(tsm + 4 * kTailMax) + kTailMax};
+  int32_t* s_nbr = s_id[1] + kTailMax;
+  uint32_t* s_w = reinterpret_cast<uint32_t*>(s_nbr + kTailMax);  // 2 x 32 warp sums
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  uint32_t c = __ldcg(B.ctrl + 0);
+  // nothing left, or the loop stopped without handing over (too many clusters, an error)
+  if (c <= 1 || c > kTailMax || (__ldcg(B.status) & kStatusNoProgress)) return;
+  const uint32_t par = __ldcg(B.ctrl + 3) & 1u;
+  const Box* cin = par ? B.cbox[1] : B.cbox[0];
+  const int32_t* idin = par ? B.cid[1] : B.cid[0];
+  for (uint32_t x = tid; x < c; x += kTailThreads) {
+    const float4* bp = reinterpret_cast<const float4*>(cin + x);
+    s_lo[0][x] = __ldcg(bp);
+    s_hi[0][x] = __ldcg(bp + 1);
+    s_id[0][x] = __ldcg(idin + x);
+  }
+  uint32_t next = __ldcg(B.ctrl + 1), it = __ldcg(B.ctrl + 6);
+  const uint32_t cap = __ldcg(B.ctrl + 7);
+  unsigned long long sum = (unsigned long long)__ldcg(B.ctrl + 9) << 32 | __ldcg(B.ctrl + 8);
+  int cur = 0;
+  bool no_progress = false;
+  const float kInf = __int_as_float(0x7f800000);
+  __syncthreads();
+  while (true) {
+    sum += c;
+    ++it;
+    const float4* lo = s_lo[cur];
+    const float4* hi = s_hi[cur];
+    // neighbours: ascending j with a strict < keeps the smallest j of equal areas
+    for (uint32_t x = tid; x < c; x += kTailThreads) {
+      const float4 xa = lo[x], xb = hi[x];
+      const uint32_t j0 = x > (uint32_t)r ? x - (uint32_t)r : 0u, j1 = min(c - 1, x + (uint32_t)r);
+      float best = kInf;
+      int32_t bj = -1;
+      for (uint32_t j = j0; j <= j1; ++j) {
+        if (j == x) continue;
+        const float d = pair_area(xa, xb, lo[j], hi[j]);
+        if (d < best) {
+          best = d;
+          bj = (int32_t)j;
+        }
+      }
+      s_nbr[x] = bj;
+    }
+    __syncthreads();
+    // merge and survivor flags of this thread's clusters x = 2 tid, 2 tid + 1 (ascending)
+    uint32_t mk = 0, vk = 0;
+    bool m2[2], v2[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t x = 2u * (uint32_t)tid + (uint32_t)q;
+      bool mm = false, vv = false;
+      if (x < c) {
+        const int32_t j = s_nbr[x];
+        const bool mutual = j >= 0 && s_nbr[j] == (int32_t)x;
+        mm = mutual && (int32_t)x < j;
+        vv = !(mutual && j < (int32_t)x);
+      }
+      m2[q] = mm;
+      v2[q] = vv;
+      mk += mm;
+      vk += vv;
+    }
+    // block exclusive scan of (merges, survivors), packed 16 + 16 bits (c <= 2048)
+    uint32_t packed = mk << 16 | vk, x = packed;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      uint32_t t = s_w[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      s_w[32 + lane] = t;  // inclusive warp totals
+    }
+    __syncthreads();
+    const uint32_t before = (wid ? s_w[32 + wid - 1] : 0u) + x - packed;
+    const uint32_t total = s_w[32 + 31];
+    uint32_t mpos = before >> 16, vpos = before & 0xffffu;
+    const int nb = cur ^ 1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t xi = 2u * (uint32_t)tid + (uint32_t)q;
+      if (xi >= c) continue;
+      float4 a = lo[xi], b = hi[xi];
+      int32_t nid = s_id[cur][xi];
+      if (m2[q]) {
+        const int32_t j = s_nbr[xi];
+        const float4 ja = lo[j], jb = hi[j];
+        a = make_float4(fminf(a.x, ja.x), fminf(a.y, ja.y), fminf(a.z, ja.z), 0.f);
+        b = make_float4(fmaxf(b.x, jb.x), fmaxf(b.y, jb.y), fmaxf(b.z, jb.z), 0.f);
+        const int32_t id_new = (int32_t)(next + mpos);
+        float4* np = reinterpret_cast<float4*>(B.nodes + id_new);
+        np[0] = a;
+        np[1] = b;
+        reinterpret_cast<int4*>(np + 2)[0] = make_int4(nid, s_id[cur][j], 0, 0);
+        nid = id_new;
+        ++mpos;
+      }
+      if (v2[q]) {
+        s_lo[nb][vpos] = a;
+        s_hi[nb][vpos] = b;
+        s_id[nb][vpos] = nid;
+        ++vpos;
+      }
+    }
+    const uint32_t nc = total & 0xffffu, merges = total >> 16;
+    next += merges;
+    __syncthreads();  // the next buffer is complete; this iteration's buffers are free
+    cur = nb;
+    const uint32_t prev = c;
+    c = nc;
+    if (c <= 1) break;
+    if (c >= prev || it >= cap) {  // no mutual pair anywhere, or the cap
+      no_progress = true;
+      break;
+    }
+  }
+  if (tid == 0) {
+    B.ctrl[0] = c;
+    B.ctrl[1] = next;
+    B.ctrl[6] = it;
+    B.ctrl[8] = (uint32_t)sum;
+    B.ctrl[9] = (uint32_t)(sum >> 32);
+    if (no_progress) atomicOr(B.status, kStatusNoProgress);
+  }
 }
 
 // Move the root (last node) to index 0 and swap every reference to 0 and the root
@@ -778,9 +940,14 @@ static cudaError_t set_nn_smem(int radius) {
   return cudaFuncSetAttribute(k_ploc_nn<SEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem(radius));
 }
 
+static cudaError_t set_tail_smem() {
+  return cudaFuncSetAttribute(k_ploc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem());
+}
+
 cudaError_t ploc_prepare(int radius) {
   cudaError_t e = set_nn_smem<false>(radius);
-  return e == cudaSuccess ? set_nn_smem<true>(radius) : e;
+  if (e == cudaSuccess) e = set_nn_smem<true>(radius);
+  return e == cudaSuccess ? set_tail_smem() : e;
 }
 
 cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter, cudaStream_t st,
@@ -792,10 +959,13 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   const PlocBufs B = ploc_bufs(ws, L);
   const PlocSeg none{};
   if ((e = set_nn_smem<false>(radius)) != cudaSuccess) return e;
+  if ((e = set_tail_smem()) != cudaSuccess) return e;
   // every iteration that makes progress removes at least one cluster, so n bounds the loop
   const uint32_t cap = max_iter > 0 ? (uint32_t)max_iter : n;
+  const uint32_t tail = ploc_tail_threshold(radius);
+  const bool loop = n > tail;  // else k_ploc_tail runs every iteration
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
-  if (n > 1 && !host_loop) {
+  if (loop && !host_loop) {
     const bool same = ws.ploc_exec && ws.ploc_key_n == n && ws.ploc_key_r == radius && ws.ploc_key_nodes == ws.nodes &&
                       ws.ploc_key_scratch == ws.scratch;
     if (!same) {
@@ -812,9 +982,9 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   uint32_t* sidx = nullptr;
   if ((e = prefix_sort30(ws, m, n, st, evs, &sidx)) != cudaSuccess) return e;
   *out_indices = sidx;
-  k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap);
+  k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap, tail);
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
-  if (n > 1 && host_loop) {
+  if (loop && host_loop) {
     for (uint32_t it = 0; it < cap; ++it) {
       enqueue_iteration<false, false>(B, none, n, radius, st, cudaGraphConditionalHandle{});
       if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
@@ -822,9 +992,11 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
         return e;
       if (!*ws.ploc_host) break;
     }
-    k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
-  } else if (n > 1) {
+  } else if (loop) {
     if ((e = cudaGraphLaunch(ws.ploc_exec, st)) != cudaSuccess) return e;
+  }
+  if (n > 1) {
+    k_ploc_tail<<<1, kTailThreads, tail_smem(), st>>>(B, radius);
     k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
   }
   if (evs && evs->use) cudaEventRecord(evs->ev[5], st);

@@ -537,10 +537,18 @@ extern "C" bvh_status bvh_serve_open(const bvh_serve_config* cfg, bvh_server** o
     }
   }
   if (cfg->max_triangles || cfg->max_rays) {
-    const uint32_t n = cfg->max_triangles ? cfg->max_triangles : 1024;
+    // per-request slots: room for the largest request; batched slots: for a full batch of them
+    // (growing later would free buffers, which synchronises the whole device mid-stream)
+    uint64_t n = cfg->max_triangles ? cfg->max_triangles : 1024, nr = cfg->max_rays, count = 1;
+    if (batched) {
+      count = sv->max_batch_requests;
+      n = std::min<uint64_t>(std::max<uint64_t>(n * count, 1024), std::max<uint64_t>(sv->max_batch_triangles, n));
+      nr = std::min<uint64_t>(nr * count, 0xffffffffull);
+    }
     for (Slot& s : sv->slots) {
-      if (held_total(sv) + need_bytes(sv, n, cfg->max_rays, 1) > cfg->hbm_budget_bytes) break;  // grow later
-      if (grow(sv, s, n, cfg->max_rays, 1, meta_layout(1, div_up(n, kSegChunk)).total) != cudaSuccess) {
+      if (held_total(sv) + need_bytes(sv, n, nr, count) > cfg->hbm_budget_bytes) break;  // grow later
+      if (grow(sv, s, (uint32_t)n, (uint32_t)nr, (uint32_t)count,
+               meta_layout((uint32_t)count, (uint32_t)(count + n / kSegChunk)).total) != cudaSuccess) {
         release_slots(sv);
         delete sv;
         return BVH_ERR_OUT_OF_MEMORY;
