@@ -361,7 +361,9 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     s = stream.cuda_stream
     ctx.reserve(n, algo_id)
-    tuning = None if args.no_autotune else ctx.autotune(n, s)
+    # launch shapes for this algorithm and size (the tree is checked to stay the same); choices
+    # that change the tree (radius, treelet passes, Morton bits) come back with their SAH
+    tuning = None if args.no_autotune else ctx.autotune_build(ptrs, n, params, s)
 
     # --- device-resident build throughput -------------------------------------------------
     # The clock sampler runs through the warm-up, the timed region and the stage-timing builds

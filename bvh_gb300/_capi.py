@@ -135,6 +135,9 @@ SIGNATURES = {
     "bvh_autotune": (c_int, [c_void_p, c_uint32, c_void_p, c_char_p, ctypes.c_size_t]),
     "bvh_tuning_get": (c_int, [c_void_p, POINTER(c_int32)]),
     "bvh_tuning_set": (c_int, [c_void_p, c_int32]),
+    "bvh_autotune_build": (c_int, [c_void_p, POINTER(MeshSoA), POINTER(Params), c_void_p, c_char_p, ctypes.c_size_t]),
+    "bvh_tuning_export": (c_int, [c_void_p, c_char_p, ctypes.c_size_t]),
+    "bvh_tuning_import": (c_int, [c_void_p, c_char_p]),
     "bvh_build_lbvh_static": (c_int, [POINTER(MeshSoA), c_int32, c_void_p, c_void_p, c_void_p]),
     "bvh_evaluate": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p, POINTER(EvalStats)]),
     "bvh_load_obj": (c_int, [ctypes.c_char_p, c_int32, c_int32, POINTER(ObjMesh)]),

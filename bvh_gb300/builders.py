@@ -145,6 +145,26 @@ class Context:
         C.check(self.lib.bvh_autotune(self.handle, n, ctypes.c_void_p(stream), buf, len(buf)), "bvh_autotune")
         return json.loads(buf.value.decode())
 
+    def autotune_build(self, ptrs: Sequence[int], n: int, params: C.Params, stream: int = 0) -> dict:
+        """bvh_autotune_build: time every launch shape on this mesh (device SoA), keep the fastest
+        in the context's tuning table, report tree-changing choices with their SAH."""
+        import json
+        m = C.mesh_struct(ptrs, n)
+        buf = ctypes.create_string_buffer(1 << 16)
+        C.check(self.lib.bvh_autotune_build(self.handle, ctypes.byref(m), ctypes.byref(params), ctypes.c_void_p(stream),
+                                            buf, len(buf)), "bvh_autotune_build")
+        return json.loads(buf.value.decode())
+
+    def tuning_export(self) -> str:
+        """The context's tuning table as JSON (bvh_tuning_export), e.g. to write to a file."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        C.check(self.lib.bvh_tuning_export(self.handle, buf, len(buf)), "bvh_tuning_export")
+        return buf.value.decode()
+
+    def tuning_import(self, text: str) -> None:
+        """Replace the tuning table with one bvh_tuning_export wrote (bvh_tuning_import)."""
+        C.check(self.lib.bvh_tuning_import(self.handle, text.encode()), "bvh_tuning_import")
+
     def tuning(self) -> int:
         """The sort variant this context uses (bvh_tuning_get)."""
         a = ctypes.c_int32()

@@ -17,13 +17,27 @@ struct BatchGraph {
   cudaGraphExec_t exec = nullptr;
   const float* ptrs[9] = {};
   uint32_t n = 0, count = 0;
-  int32_t algo = -1, radius = 0, max_iter = 0;
+  int32_t algo = -1, radius = 0, max_iter = 0, sort_variant = -1;
+  uint32_t shape = 0;
   std::vector<uint32_t> offsets;
+};
+
+// Launch shapes for one (algorithm, size bucket) -- bvh_autotune_build's choice.  None of them
+// changes the tree.  algo: bvh_algo, +256 for batched builds; bucket: floor(log2(triangles)).
+struct TuneEntry {
+  int32_t algo = -1, bucket = -1;
+  int32_t sort_variant = 0;
+  uint32_t tail_pairs = 100000;
+  int32_t nn_bps = 3, mg_bps = 8;
 };
 
 struct bvh_ctx {
   int device = 0;
   Workspace ws;
+  TuneEntry base;                 // shapes where no table entry matches (bvh_tuning_set sets its sort variant)
+  std::vector<TuneEntry> table;   // bvh_autotune_build / bvh_tuning_import
+  bool tuning_locked = false;     // bvh_autotune_build sets the shapes itself
+  unsigned long long* hash_buf = nullptr;  // device word for tree_hash
   BatchGraph bgraph;
   cudaStream_t capture_stream = nullptr;  // for CUDA graph capture (never the legacy stream)
   void* eval_buf = nullptr;               // bvh_evaluate scratch
@@ -108,6 +122,7 @@ extern "C" bvh_status bvh_ctx_destroy(bvh_ctx* ctx) {
   cudaFree(ctx->heat_buf);
   for (int k = 0; k < 8; ++k) cudaEventDestroy(ctx->evs.ev[k]);
   cudaFreeHost(ctx->h_status);
+  cudaFree(ctx->hash_buf);
   delete ctx;
   return BVH_OK;
 }
@@ -165,9 +180,31 @@ static bool mesh_ok(const bvh_mesh_soa* m) {
   return true;
 }
 
+static int size_bucket(uint32_t n) { return n ? 31 - __builtin_clz(n) : 0; }
+
+static void set_shapes(Workspace& ws, const TuneEntry& t) {
+  ws.sort_variant = t.sort_variant;
+  ws.ploc_tail_pairs = t.tail_pairs;
+  ws.ploc_nn_bps = t.nn_bps;
+  ws.ploc_mg_bps = t.mg_bps;
+}
+
+// The table entry for this algorithm and size, else the base shapes.
+static void apply_tuning(bvh_ctx* ctx, int32_t algo_key, uint32_t n) {
+  if (ctx->tuning_locked) return;
+  const int b = size_bucket(n);
+  for (const TuneEntry& t : ctx->table)
+    if (t.algo == algo_key && t.bucket == b) {
+      set_shapes(ctx->ws, t);
+      return;
+    }
+  set_shapes(ctx->ws, ctx->base);
+}
+
 static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, cudaStream_t st,
                              bvh_tree* out) {
   const uint32_t n = mesh->n;
+  apply_tuning(ctx, params->algo, n);
   ctx->have_timing = false;
   ctx->last = bvh_timing{};
   ctx->last_algo = params->algo;
@@ -435,6 +472,7 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   ctx->have_timing = false;
   ctx->last = bvh_timing{};
   ctx->last_algo = params->algo;
+  apply_tuning(ctx, params->algo + 256, n);
   const uint32_t n_items = count_items(batch->offsets, count);
   const size_t words = items_at(count) + 4 * (size_t)n_items;
   cudaError_t e = reserve_batch(ws, n, count, words, st);
@@ -462,7 +500,8 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   if (use_graph) {
     BatchGraph& g = ctx->bgraph;
     bool same = g.exec && !changed && g.n == n && g.count == count && memcmp(g.ptrs, m.v, sizeof(g.ptrs)) == 0 &&
-                g.algo == params->algo && g.radius == params->ploc_radius && g.max_iter == params->max_iterations;
+                g.algo == params->algo && g.radius == params->ploc_radius && g.max_iter == params->max_iterations &&
+                g.sort_variant == ws.sort_variant && g.shape == ((uint32_t)ws.ploc_nn_bps << 16 | (uint32_t)ws.ploc_mg_bps);
     if (!same) {
       if (g.exec) cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -484,6 +523,8 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
       g.algo = params->algo;
       g.radius = params->ploc_radius;
       g.max_iter = params->max_iterations;
+      g.sort_variant = ws.sort_variant;
+      g.shape = (uint32_t)ws.ploc_nn_bps << 16 | (uint32_t)ws.ploc_mg_bps;
     }
     cudaEventRecord(ctx->evs.ev[0], st);
     if ((e = epoch_tick(ws, st)) != cudaSuccess) return from_cuda(e);  // the graph bumps the epoch
@@ -547,6 +588,7 @@ extern "C" bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char*
   std::vector<float> ms(nv, 0.0f);
   cudaError_t e = autotune_sort(ctx->ws, n, st, ms.data());
   if (e != cudaSuccess) return from_cuda(e);
+  ctx->base.sort_variant = ctx->ws.sort_variant;
   if (json_out && json_cap) {
     std::string js = "{\"n\": " + std::to_string(n) + ", \"sort\": {\"chosen\": " +
                      std::to_string(ctx->ws.sort_variant) + ", \"variants\": [";
@@ -574,6 +616,228 @@ extern "C" bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant) {
 extern "C" bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant) {
   if (!ctx || variant < 0 || variant >= sort_variant_count()) return BVH_ERR_INVALID_ARG;
   ctx->ws.sort_variant = variant;
+  ctx->base.sort_variant = variant;
+  return BVH_OK;
+}
+
+// ---- autotuning of whole builds ------------------------------------------------------------
+static std::string entry_json(const TuneEntry& t) {
+  char buf[200];
+  snprintf(buf, sizeof(buf),
+           "{\"algo\": %d, \"bucket\": %d, \"sort_variant\": %d, \"ploc_tail_pairs\": %u, \"ploc_nn_bps\": %d, "
+           "\"ploc_mg_bps\": %d}",
+           t.algo, t.bucket, t.sort_variant, t.tail_pairs, t.nn_bps, t.mg_bps);
+  return buf;
+}
+
+static bool valid_entry(const TuneEntry& t) {
+  return t.sort_variant >= 0 && t.sort_variant < sort_variant_count() && t.nn_bps >= 1 && t.nn_bps <= 16 &&
+         t.mg_bps >= 1 && t.mg_bps <= 32 && t.tail_pairs <= 10000000u && t.bucket >= 0 && t.bucket < 32;
+}
+
+static bvh_status write_json(const std::string& js, char* out, size_t cap) {
+  if (!out || !cap) return BVH_OK;
+  if (js.size() + 1 > cap) return BVH_ERR_INVALID_ARG;
+  memcpy(out, js.c_str(), js.size() + 1);
+  return BVH_OK;
+}
+
+// Builds the mesh `reps` times after one warm-up build: the mean device time, the tree's hash
+// and (sah != NULL) its SAH.
+static bvh_status timed_builds(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* p, cudaStream_t st, int reps,
+                               float* ms, unsigned long long* hash, double* sah) {
+  bvh_tree tr;
+  bvh_status s = build_impl(ctx, mesh, p, st, &tr);
+  if (s == BVH_OK) s = bvh_sync(ctx);
+  if (s != BVH_OK) return s;
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return BVH_ERR_DEVICE;
+  if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return BVH_ERR_DEVICE; }
+  cudaEventRecord(a, st);
+  for (int k = 0; k < reps && s == BVH_OK; ++k) s = build_impl(ctx, mesh, p, st, &tr);
+  cudaEventRecord(b, st);
+  if (s == BVH_OK) s = bvh_sync(ctx);
+  if (s == BVH_OK) s = from_cuda(cudaEventSynchronize(b));
+  float t = 0;
+  if (s == BVH_OK) s = from_cuda(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (s != BVH_OK) return s;
+  *ms = t / (float)reps;
+  if ((s = from_cuda(tree_hash(reinterpret_cast<const Node*>(tr.nodes), tr.n_nodes, ctx->hash_buf, st))) != BVH_OK)
+    return s;
+  if ((s = from_cuda(cudaMemcpyAsync(ctx->h_status + 24, ctx->hash_buf, 8, cudaMemcpyDeviceToHost, st))) != BVH_OK ||
+      (s = from_cuda(cudaStreamSynchronize(st))) != BVH_OK)
+    return s;
+  memcpy(hash, ctx->h_status + 24, 8);  // (words 4-19 take PLOC's control words)
+  if (sah) {
+    bvh_eval_stats es;
+    if ((s = bvh_evaluate(ctx, tr.nodes, tr.n_nodes, reinterpret_cast<void*>(st), &es)) != BVH_OK) return s;
+    *sah = es.sah;
+  }
+  return BVH_OK;
+}
+
+extern "C" bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params,
+                                         void* stream, char* json_out, size_t json_cap) {
+  if (!ctx || !mesh_ok(mesh) || !valid_params(params) || mesh->n < 1024) return BVH_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (!ctx->hash_buf && cudaMalloc(&ctx->hash_buf, 8) != cudaSuccess) return BVH_ERR_OUT_OF_MEMORY;
+  const uint32_t n = mesh->n;
+  const int32_t algo = params->algo;
+  // start from the shapes the build would use now
+  ctx->tuning_locked = false;
+  apply_tuning(ctx, algo, n);
+  TuneEntry best;
+  best.sort_variant = ctx->ws.sort_variant;
+  best.tail_pairs = ctx->ws.ploc_tail_pairs;
+  best.nn_bps = ctx->ws.ploc_nn_bps;
+  best.mg_bps = ctx->ws.ploc_mg_bps;
+  best.algo = algo;
+  best.bucket = size_bucket(n);
+  ctx->tuning_locked = true;
+  const int reps = 3;
+  std::string trials;
+  float best_ms = 0;
+  unsigned long long ref_hash = 0;
+  auto trial = [&](const TuneEntry& t, bool first) -> bvh_status {
+    set_shapes(ctx->ws, t);
+    float ms = 0;
+    unsigned long long h = 0;
+    bvh_status s = timed_builds(ctx, mesh, params, st, reps, &ms, &h, nullptr);
+    if (s != BVH_OK) return s;
+    if (first) ref_hash = h;
+    const bool same = h == ref_hash;
+    char buf[240];
+    snprintf(buf, sizeof(buf),
+             "%s{\"sort_variant\": %d, \"ploc_tail_pairs\": %u, \"ploc_nn_bps\": %d, \"ploc_mg_bps\": %d, "
+             "\"ms\": %.4f, \"same_tree\": %s}",
+             trials.empty() ? "" : ", ", t.sort_variant, t.tail_pairs, t.nn_bps, t.mg_bps, ms, same ? "true" : "false");
+    trials += buf;
+    if (!same) return BVH_ERR_DEVICE;  // a launch shape changed the tree: never expected
+    if (first || ms < best_ms) {
+      best = t;
+      best_ms = ms;
+    }
+    return BVH_OK;
+  };
+  bvh_status s = trial(best, true);
+  for (int v = 0; s == BVH_OK && v < sort_variant_count(); ++v) {
+    TuneEntry t = best;
+    t.sort_variant = v;
+    if (v != best.sort_variant) s = trial(t, false);
+  }
+  if (algo == BVH_ALGO_PLOC) {
+    for (uint32_t pairs : {0u, 50000u, 100000u, 200000u}) {
+      TuneEntry t = best;
+      t.tail_pairs = pairs;
+      if (s == BVH_OK && pairs != best.tail_pairs) s = trial(t, false);
+    }
+    for (int k : {2, 3, 4}) {
+      TuneEntry t = best;
+      t.nn_bps = k;
+      if (s == BVH_OK && k != best.nn_bps) s = trial(t, false);
+    }
+    for (int k : {4, 8, 16}) {
+      TuneEntry t = best;
+      t.mg_bps = k;
+      if (s == BVH_OK && k != best.mg_bps) s = trial(t, false);
+    }
+  }
+  // choices that change the tree are reported with their cost and SAH, not chosen
+  std::string quality;
+  if (s == BVH_OK) {
+    set_shapes(ctx->ws, best);
+    std::vector<bvh_params> alts;
+    const char* what = "";
+    if (algo == BVH_ALGO_PLOC) {
+      what = "ploc_radius";
+      for (int r : {10, 25, 50, 100}) { bvh_params q = *params; q.ploc_radius = r; alts.push_back(q); }
+    } else if (algo == BVH_ALGO_LBVH_PLUS) {
+      what = "treelet_rounds";
+      for (int r : {1, 2, 3}) { bvh_params q = *params; q.treelet_rounds = r; alts.push_back(q); }
+    } else {
+      what = "morton_bits";
+      for (int b : {30, 60, 63}) { bvh_params q = *params; q.morton_bits = b; alts.push_back(q); }
+    }
+    for (const bvh_params& q : alts) {
+      float ms = 0;
+      unsigned long long h = 0;
+      double sah = 0;
+      if ((s = timed_builds(ctx, mesh, &q, st, reps, &ms, &h, &sah)) != BVH_OK) break;
+      const int val = algo == BVH_ALGO_PLOC ? q.ploc_radius : algo == BVH_ALGO_LBVH_PLUS ? q.treelet_rounds : q.morton_bits;
+      char buf[160];
+      snprintf(buf, sizeof(buf), "%s{\"%s\": %d, \"ms\": %.4f, \"sah\": %.17g}", quality.empty() ? "" : ", ", what,
+               val, ms, sah);
+      quality += buf;
+    }
+  }
+  ctx->tuning_locked = false;
+  if (s != BVH_OK) return s;
+  bool replaced = false;
+  for (TuneEntry& t : ctx->table)
+    if (t.algo == best.algo && t.bucket == best.bucket) {
+      t = best;
+      replaced = true;
+    }
+  if (!replaced) ctx->table.push_back(best);
+  apply_tuning(ctx, algo, n);
+  return write_json("{\"n\": " + std::to_string(n) + ", \"chosen\": " + entry_json(best) + ", \"best_ms\": " +
+                        std::to_string(best_ms) + ", \"trials\": [" + trials + "], \"tree_changing\": [" + quality +
+                        "]}",
+                    json_out, json_cap);
+}
+
+extern "C" bvh_status bvh_tuning_export(const bvh_ctx* ctx, char* json_out, size_t json_cap) {
+  if (!ctx || !json_out || !json_cap) return BVH_ERR_INVALID_ARG;
+  std::string js = "{\"base\": " + entry_json(ctx->base) + ", \"entries\": [";
+  for (size_t k = 0; k < ctx->table.size(); ++k) js += (k ? ", " : "") + entry_json(ctx->table[k]);
+  return write_json(js + "]}", json_out, json_cap);
+}
+
+// Reads the integer after "key": in [p, end); false when absent.
+static bool json_int(const char* p, const char* end, const char* key, long long* v) {
+  const std::string k = std::string("\"") + key + "\"";
+  const char* f = std::search(p, end, k.begin(), k.end());
+  if (f == end) return false;
+  f += k.size();
+  while (f < end && (*f == ' ' || *f == ':' || *f == '\t' || *f == '\n')) ++f;
+  char* stop = nullptr;
+  *v = strtoll(f, &stop, 10);
+  return stop != f;
+}
+
+extern "C" bvh_status bvh_tuning_import(bvh_ctx* ctx, const char* json) {
+  if (!ctx || !json) return BVH_ERR_INVALID_ARG;
+  // the objects of the "entries" array (flat objects, no nested arrays); anything else in the
+  // document (a "base" entry, reports) is ignored
+  const char* ent = strstr(json, "\"entries\"");
+  const char* lb = ent ? strchr(ent, '[') : nullptr;
+  const char* rb = lb ? strchr(lb, ']') : nullptr;
+  if (!rb) return BVH_ERR_INVALID_ARG;
+  std::vector<TuneEntry> table;
+  for (const char* o = std::find(lb, rb, '{'); o < rb; o = std::find(o + 1, rb, '{')) {
+    const char* c = std::find(o, rb, '}');
+    if (c == rb) return BVH_ERR_INVALID_ARG;
+    TuneEntry t;
+    long long v;
+    if (!json_int(o, c, "algo", &v)) return BVH_ERR_INVALID_ARG;
+    t.algo = (int32_t)v;
+    if (!json_int(o, c, "bucket", &v)) return BVH_ERR_INVALID_ARG;
+    t.bucket = (int32_t)v;
+    if (json_int(o, c, "sort_variant", &v)) t.sort_variant = (int32_t)v;
+    if (json_int(o, c, "ploc_tail_pairs", &v)) {
+      if (v < 0 || v > 10000000ll) return BVH_ERR_INVALID_ARG;
+      t.tail_pairs = (uint32_t)v;
+    }
+    if (json_int(o, c, "ploc_nn_bps", &v)) t.nn_bps = (int32_t)v;
+    if (json_int(o, c, "ploc_mg_bps", &v)) t.mg_bps = (int32_t)v;
+    if (!valid_entry(t)) return BVH_ERR_INVALID_ARG;
+    table.push_back(t);
+    o = c;
+  }
+  ctx->table = table;
   return BVH_OK;
 }
 

@@ -6,6 +6,9 @@ increasing numeric order (every proper subset comes first); cost[s] = min over s
 cost[p] + cost[s ^ p], plus the area of s; single leaves cost 0.  The splits of s are the
 nonempty subsets p of s without its lowest member, in increasing order, and the first minimum
 is kept (a strict < from INF, so a subset whose splits all cost >= INF keeps INF and no split).
+Subsets with four or more splits run two first-minimum chains over the two halves of their
+splits, interleaved, and keep the second half's minimum only if it is strictly smaller: the same
+result with half the dependency depth.
 
 Run from this directory:  python gen_treelet_dp.py > treelet_dp_unrolled.cuh
 """
@@ -33,9 +36,26 @@ def emit(n, w):
             continue
         delta = s & (s - 1)
         last = s == full  # only its best split is needed
-        w(("" if last else f"  float c{s};\n") + "  {\n    float b = kTlInf, v;\n    uint32_t bp = 0xffu;\n")
-        for p in subsets_of(delta):
-            w(f"    v = __fadd_rn(c{p}, c{s ^ p});\n    if (v < b) {{ b = v; bp = {p}u; }}\n")
+        splits = subsets_of(delta)
+        w(("" if last else f"  float c{s};\n") + "  {\n")
+        if len(splits) < 4:
+            w("    float b = kTlInf, v;\n    uint32_t bp = 0xffu;\n")
+            for p in splits:
+                w(f"    v = __fadd_rn(c{p}, c{s ^ p});\n    if (v < b) {{ b = v; bp = {p}u; }}\n")
+        else:
+            # two independent first-minimum chains over the first and the second half of the
+            # splits, interleaved; the second wins only if strictly smaller, so the first
+            # minimum in split order is kept
+            h = (len(splits) + 1) // 2
+            a, z = splits[:h], splits[h:]
+            w("    float b = kTlInf, b2 = kTlInf, v, v2;\n    uint32_t bp = 0xffu, bp2 = 0xffu;\n")
+            for k in range(h):
+                p = a[k]
+                w(f"    v = __fadd_rn(c{p}, c{s ^ p});\n    if (v < b) {{ b = v; bp = {p}u; }}\n")
+                if k < len(z):
+                    q = z[k]
+                    w(f"    v2 = __fadd_rn(c{q}, c{s ^ q});\n    if (v2 < b2) {{ b2 = v2; bp2 = {q}u; }}\n")
+            w("    if (b2 < b) { b = b2; bp = bp2; }\n")
         if not last:
             w(f"    c{s} = __fadd_rn(b, A[{s} * 32]);\n")
         w(f"    P[{s} * 32] = (uint8_t)bp;\n  }}\n")

@@ -16,6 +16,10 @@ struct MeshPtrs {
 struct Workspace {
   uint32_t cap_n = 0;        // triangles the buffers can hold
   int sort_variant = 0;      // onesweep variant (bvh_autotune)
+  // PLOC launch shapes (bvh_autotune_build); none of them changes the tree
+  uint32_t ploc_tail_pairs = 100000;  // hand over to k_ploc_tail below this many pair areas (0: never)
+  int ploc_nn_bps = 3;                // neighbour-search blocks per SM
+  int ploc_mg_bps = 8;                // merge (count / scatter) blocks per SM
   void* keys[2] = {nullptr, nullptr};
   uint32_t* vals[2] = {nullptr, nullptr};
   Box* boxes = nullptr;      // per-triangle AABB in input order
@@ -41,6 +45,7 @@ struct Workspace {
   int ploc_key_r = 0;
   const void* ploc_key_nodes = nullptr;
   const void* ploc_key_scratch = nullptr;
+  uint32_t ploc_key_shape = 0;  // nn and merge blocks per SM the cached loop graph was made with
   cudaStream_t aux_stream = nullptr;  // a second stream for capturing loop bodies
   uint64_t epoch_builds = 0;           // builds that bumped this workspace's epoch (epoch_tick)
   // the batched PLOC loop graph and what it was made for
@@ -48,6 +53,7 @@ struct Workspace {
   uint32_t ploc_seg_key_n = 0, ploc_seg_key_count = 0;
   int ploc_seg_key_r = 0;
   const void* ploc_seg_key[4] = {};
+  uint32_t ploc_seg_key_shape = 0;
   // device-side mesh copy for host-pointer builds
   float* mesh_dev = nullptr;
   uint32_t mesh_cap = 0;
@@ -141,6 +147,11 @@ cudaError_t workspace_reserve(Workspace& ws, uint32_t n, cudaStream_t st);
 cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n);
 // PLOC kernel attributes for a radius (shared memory of the neighbour search); before any capture.
 cudaError_t ploc_prepare(int radius);
+// Live clusters at which k_ploc_tail takes over for a radius and a pair budget (0: never).
+uint32_t ploc_tail_threshold(int radius, uint32_t pairs);
+// Order-independent 64-bit hash of every node's min, max, left and right (with its index), on the
+// device; *out (device) receives it.  Equal trees hash equal.
+cudaError_t tree_hash(const Node* nodes, uint32_t n_nodes, unsigned long long* out, cudaStream_t st);
 void workspace_free(Workspace& ws);
 
 // Tree statistics on the device (BVHEvaluator, src/evaluator.cpp:38-113).

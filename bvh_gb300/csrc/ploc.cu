@@ -619,10 +619,10 @@ __global__ void k_ploc_step(PlocBufs B, cudaGraphConditionalHandle handle) {
 // same stop (one cluster), no-progress and cap rules, iteration count and live-cluster sum.
 constexpr int kTailThreads = 1024;
 constexpr uint32_t kTailMax = 2048;
-constexpr uint32_t kTailPairs = 100000;  // pair areas per iteration at the hand-over, at most
 
-uint32_t ploc_tail_threshold(int radius) {
-  const uint32_t t = kTailPairs / (2u * (uint32_t)std::max(radius, 1));
+uint32_t ploc_tail_threshold(int radius, uint32_t pairs) {
+  if (pairs == 0) return 0;
+  const uint32_t t = pairs / (2u * (uint32_t)std::max(radius, 1));
   return std::min<uint32_t>(kTailMax, std::max<uint32_t>(t, 64));
 }
 static size_t tail_smem() { return (size_t)kTailMax * (4 * 16 + 3 * 4) + 2 * 32 * 4; }
@@ -865,17 +865,29 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
 
 static size_t nn_smem(int radius) { return 32 * (kNnTile + 2 * (size_t)radius) + 4 * (size_t)kNnKc * kNnTile; }
 
-static uint32_t nn_grid_for(uint32_t n) { return std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152 * 3)); }
-static uint32_t mg_grid_for(uint32_t n) { return std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152 * 8)); }
+// Persistent grids sized for n, capped at `bps` blocks per SM (the workspace's launch shapes).
+struct PlocShape {
+  int nn_bps, mg_bps;
+  uint32_t key() const { return (uint32_t)nn_bps << 16 | (uint32_t)mg_bps; }
+};
+static PlocShape ploc_shape(const Workspace& ws) {
+  return PlocShape{std::max(1, std::min(ws.ploc_nn_bps, 16)), std::max(1, std::min(ws.ploc_mg_bps, 32))};
+}
+static uint32_t nn_grid_for(uint32_t n, const PlocShape& sh) {
+  return std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kNnTile), 152u * (uint32_t)sh.nn_bps));
+}
+static uint32_t mg_grid_for(uint32_t n, const PlocShape& sh) {
+  return std::max<uint32_t>(1, std::min<uint32_t>(div_up(n, kPlocTile), 152u * (uint32_t)sh.mg_bps));
+}
 
 // One clustering iteration: neighbours, tile counts + scan, (batched: per-mesh ranks), merge +
 // compaction, loop control.  Grids are persistent (sized for n); the kernels read the live
 // cluster count from the control words.
 template <bool SEG, bool GRAPH>
-static void enqueue_iteration(const PlocBufs& B, const PlocSeg& S, uint32_t n, int radius, cudaStream_t st,
-                              cudaGraphConditionalHandle handle) {
-  const uint32_t mg_grid = mg_grid_for(n);
-  k_ploc_nn<SEG><<<nn_grid_for(n), kPlocThreads, nn_smem(radius), st>>>(B, radius);
+static void enqueue_iteration(const PlocBufs& B, const PlocSeg& S, uint32_t n, int radius, const PlocShape& sh,
+                              cudaStream_t st, cudaGraphConditionalHandle handle) {
+  const uint32_t mg_grid = mg_grid_for(n, sh);
+  k_ploc_nn<SEG><<<nn_grid_for(n, sh), kPlocThreads, nn_smem(radius), st>>>(B, radius);
   k_ploc_count<<<mg_grid, kPlocThreads, 0, st>>>(B);
   if constexpr (SEG) k_ploc_seg<<<std::max<uint32_t>(1, std::min<uint32_t>(div_up(S.count, 256), 152 * 4)), 256, 0,
                                   st>>>(B, S, mg_grid);
@@ -885,7 +897,8 @@ static void enqueue_iteration(const PlocBufs& B, const PlocSeg& S, uint32_t n, i
 
 // The loop as a graph: WHILE(cond) { one iteration }.
 template <bool SEG>
-static cudaError_t make_loop_graph(const PlocBufs& B, const PlocSeg& S, uint32_t n, int radius, cudaGraphExec_t* out) {
+static cudaError_t make_loop_graph(const PlocBufs& B, const PlocSeg& S, uint32_t n, int radius, const PlocShape& sh,
+                                   cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
   if (e != cudaSuccess) return e;
@@ -905,7 +918,7 @@ static cudaError_t make_loop_graph(const PlocBufs& B, const PlocSeg& S, uint32_t
     if ((e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
         cudaSuccess)
       break;
-    enqueue_iteration<SEG, true>(B, S, n, radius, cs, handle);
+    enqueue_iteration<SEG, true>(B, S, n, radius, sh, cs, handle);
     cudaGraph_t captured = nullptr;
     cudaError_t e2 = cudaGetLastError();
     e = cudaStreamEndCapture(cs, &captured);
@@ -962,20 +975,22 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   if ((e = set_tail_smem()) != cudaSuccess) return e;
   // every iteration that makes progress removes at least one cluster, so n bounds the loop
   const uint32_t cap = max_iter > 0 ? (uint32_t)max_iter : n;
-  const uint32_t tail = ploc_tail_threshold(radius);
-  const bool loop = n > tail;  // else k_ploc_tail runs every iteration
+  const uint32_t tail = ploc_tail_threshold(radius, ws.ploc_tail_pairs);
+  const bool loop = n > 1 && n > tail;  // else k_ploc_tail runs every iteration
+  const PlocShape sh = ploc_shape(ws);
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
   if (loop && !host_loop) {
     const bool same = ws.ploc_exec && ws.ploc_key_n == n && ws.ploc_key_r == radius && ws.ploc_key_nodes == ws.nodes &&
-                      ws.ploc_key_scratch == ws.scratch;
+                      ws.ploc_key_scratch == ws.scratch && ws.ploc_key_shape == sh.key();
     if (!same) {
       if (ws.ploc_exec) cudaGraphExecDestroy(ws.ploc_exec);
       ws.ploc_exec = nullptr;
-      if ((e = make_loop_graph<false>(B, none, n, radius, &ws.ploc_exec)) != cudaSuccess) return e;
+      if ((e = make_loop_graph<false>(B, none, n, radius, sh, &ws.ploc_exec)) != cudaSuccess) return e;
       ws.ploc_key_n = n;
       ws.ploc_key_r = radius;
       ws.ploc_key_nodes = ws.nodes;
       ws.ploc_key_scratch = ws.scratch;
+      ws.ploc_key_shape = sh.key();
     }
   }
   if (evs && evs->use) cudaEventRecord(evs->ev[0], st);
@@ -986,7 +1001,7 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
   if (loop && host_loop) {
     for (uint32_t it = 0; it < cap; ++it) {
-      enqueue_iteration<false, false>(B, none, n, radius, st, cudaGraphConditionalHandle{});
+      enqueue_iteration<false, false>(B, none, n, radius, sh, st, cudaGraphConditionalHandle{});
       if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
           (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return e;
@@ -996,7 +1011,7 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
     if ((e = cudaGraphLaunch(ws.ploc_exec, st)) != cudaSuccess) return e;
   }
   if (n > 1) {
-    k_ploc_tail<<<1, kTailThreads, tail_smem(), st>>>(B, radius);
+    if (tail) k_ploc_tail<<<1, kTailThreads, tail_smem(), st>>>(B, radius);
     k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
   }
   if (evs && evs->use) cudaEventRecord(evs->ev[5], st);
@@ -1028,17 +1043,19 @@ cudaError_t batched_ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, con
   const uint32_t cap = max_iter > 0 ? max_iter : n;
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
   const bool loop = n > count;  // some mesh has two or more triangles
+  const PlocShape sh = ploc_shape(ws);
   cudaStreamCaptureStatus cst0 = cudaStreamCaptureStatusNone;
   if ((e = cudaStreamIsCapturing(st, &cst0)) != cudaSuccess) return e;
   if (loop && !host_loop && cst0 == cudaStreamCaptureStatusNone) {
     const bool same = ws.ploc_seg_exec && ws.ploc_seg_key_n == n && ws.ploc_seg_key_count == count &&
                       ws.ploc_seg_key_r == radius && ws.ploc_seg_key[0] == ws.nodes &&
                       ws.ploc_seg_key[1] == ws.scratch && ws.ploc_seg_key[2] == d_offsets &&
-                      ws.ploc_seg_key[3] == d_mbox;
+                      ws.ploc_seg_key[3] == d_mbox && ws.ploc_seg_key_shape == sh.key();
     if (!same) {
       if (ws.ploc_seg_exec) cudaGraphExecDestroy(ws.ploc_seg_exec);
       ws.ploc_seg_exec = nullptr;
-      if ((e = make_loop_graph<true>(B, S, n, radius, &ws.ploc_seg_exec)) != cudaSuccess) return e;
+      if ((e = make_loop_graph<true>(B, S, n, radius, sh, &ws.ploc_seg_exec)) != cudaSuccess) return e;
+      ws.ploc_seg_key_shape = sh.key();
       ws.ploc_seg_key_n = n;
       ws.ploc_seg_key_count = count;
       ws.ploc_seg_key_r = radius;
@@ -1055,7 +1072,7 @@ cudaError_t batched_ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, con
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
   if (loop && host_loop) {
     for (uint32_t it = 0; it < cap; ++it) {
-      enqueue_iteration<true, false>(B, S, n, radius, st, cudaGraphConditionalHandle{});
+      enqueue_iteration<true, false>(B, S, n, radius, sh, st, cudaGraphConditionalHandle{});
       if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
           (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return e;
@@ -1084,7 +1101,7 @@ cudaError_t batched_ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, con
       if ((e = cudaStreamBeginCaptureToGraph(aux, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                              cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return e;
-      enqueue_iteration<true, true>(B, S, n, radius, aux, h);
+      enqueue_iteration<true, true>(B, S, n, radius, sh, aux, h);
       cudaGraph_t body = nullptr;
       const cudaError_t e2 = cudaGetLastError();
       if ((e = cudaStreamEndCapture(aux, &body)) != cudaSuccess) return e;
@@ -1098,6 +1115,40 @@ cudaError_t batched_ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, con
   }
   if (loop) k_ploc_root_seg<<<grid, 256, 0, st>>>(ws.nodes, d_items, n_items, S, B.ctrl);
   if (evs && evs->use) cudaEventRecord(evs->ev[5], st);
+  return cudaGetLastError();
+}
+
+// Order-independent hash of a tree's node fields: each node's (index, min, max, left, right)
+// mixed to 64 bits (splitmix64 finaliser), XOR-combined per warp and then atomically.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256) k_tree_hash(const Node* __restrict__ nodes, uint32_t n_nodes,
+                                                   unsigned long long* __restrict__ out) {
+  unsigned long long h = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes; i += gridDim.x * blockDim.x) {
+    const float4* p = reinterpret_cast<const float4*>(nodes + i);
+    const float4 lo = __ldg(p), hi = __ldg(p + 1);
+    const int2 ch = __ldg(reinterpret_cast<const int2*>(p + 2));
+    unsigned long long z = mix64(i + 0x9e3779b97f4a7c15ull);
+    z = mix64(z ^ ((unsigned long long)__float_as_uint(lo.x) << 32 | __float_as_uint(lo.y)));
+    z = mix64(z ^ ((unsigned long long)__float_as_uint(lo.z) << 32 | __float_as_uint(hi.x)));
+    z = mix64(z ^ ((unsigned long long)__float_as_uint(hi.y) << 32 | __float_as_uint(hi.z)));
+    z = mix64(z ^ ((unsigned long long)(uint32_t)ch.x << 32 | (uint32_t)ch.y));
+    h ^= z;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) h ^= __shfl_xor_sync(0xffffffffu, h, o);
+  if ((threadIdx.x & 31) == 0 && h) atomicXor(out, h);
+}
+
+cudaError_t tree_hash(const Node* nodes, uint32_t n_nodes, unsigned long long* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 8, st);
+  if (e != cudaSuccess || n_nodes == 0) return e;
+  k_tree_hash<<<std::min<uint32_t>(div_up(n_nodes, 256), 152 * 8), 256, 0, st>>>(nodes, n_nodes, out);
   return cudaGetLastError();
 }
 

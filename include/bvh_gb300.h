@@ -207,9 +207,28 @@ bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_par
  * 30-bit codes whole, the high halves of longer codes), keeps the fastest in the context and
  * writes a JSON table of the timings to json_out (may be NULL).  Synchronous. */
 bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char* json_out, size_t json_cap);
-/* Read or set the sort variant a context uses (0 .. 4). */
+/* Read or set the sort variant a context uses (0 .. 4) where no tuning-table entry applies. */
 bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant);
 bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
+
+/* Autotuner for whole builds (no reference counterpart).  Builds `mesh` (device SoA, at least
+ * 1,024 triangles) with `params` under each launch shape -- radix-sort variant; for PLOC also the
+ * size at which the one-block tail kernel takes over and the neighbour-search and merge grids --
+ * by coordinate descent, 3 timed builds each, checking that every shape gives the identical
+ * tree (a device hash of all node fields; BVH_ERR_DEVICE if one did not).  The fastest is kept in
+ * the context's tuning table under (algorithm, floor(log2(n))) and used by later builds of that
+ * algorithm and size (batched builds have their own entries, algorithm + 256).  Choices that
+ * change the tree -- PLOC radius 10/25/50/100, LBVH+ treelet passes 1/2/3, LBVH Morton bits
+ * 30/60/63 -- are built and reported with their time and SAH, never chosen.  json_out (may be
+ * NULL) receives {"n", "chosen", "best_ms", "trials": [...], "tree_changing": [...]}.
+ * Synchronous. */
+bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
+                              char* json_out, size_t json_cap);
+/* The tuning table as JSON ({"base": {...}, "entries": [{"algo", "bucket", "sort_variant",
+ * "ploc_tail_pairs", "ploc_nn_bps", "ploc_mg_bps"}, ...]}), to persist it; and back (replaces the
+ * table; BVH_ERR_INVALID_ARG for malformed input or out-of-range shapes). */
+bvh_status bvh_tuning_export(const bvh_ctx* ctx, char* json_out, size_t json_cap);
+bvh_status bvh_tuning_import(bvh_ctx* ctx, const char* json);
 
 /* LBVH build that allocates nothing (no counterpart in the reference).  For callers that cannot
  * call cudaMalloc -- a host that forbids device allocations after start-up, a real-time loop
