@@ -394,6 +394,7 @@ def run_ours(args):
             t = ctx.last_timing()
             stages.append((t.bounds_ms, t.morton_ms, t.sort_ms, t.emit_ms, t.optimize_ms, t.total_ms))
             ploc_iters, ploc_csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
+            ploc_launches = int(t.kernel_launches)
             tree_height = int(t.tree_height)
         # a short timed region gets few clock samples: keep building (untimed, the same build)
         # until the sampled window around it spans at least 150 ms
@@ -570,7 +571,9 @@ def run_ours(args):
         "quality": quality,
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": args.steps * kernels_per_build(algo, bits, rounds, ploc_iters, tree_height),
+        # PLOC's loop runs on the device: the build reports its own launches
+        "gpu_launches": args.steps * (ploc_launches if algo == "ploc" and ploc_launches > 0
+                                      else kernels_per_build(algo, bits, rounds, ploc_iters, tree_height)),
         "clocks": clk.summary(),
         "autotune": tuning,
     }

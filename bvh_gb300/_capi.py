@@ -53,7 +53,8 @@ class Tree(ctypes.Structure):
 class Timing(ctypes.Structure):
     _fields_ = [("total_ms", c_float), ("bounds_ms", c_float), ("morton_ms", c_float), ("sort_ms", c_float),
                 ("emit_ms", c_float), ("optimize_ms", c_float), ("ploc_iterations", c_int32),
-                ("tree_height", c_int32), ("ploc_cluster_sum", c_uint64)]
+                ("tree_height", c_int32), ("ploc_cluster_sum", c_uint64), ("kernel_launches", c_int32),
+                ("reserved", c_int32)]
 
 
 class Hits(ctypes.Structure):

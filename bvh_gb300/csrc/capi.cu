@@ -29,6 +29,7 @@ struct TuneEntry {
   int32_t sort_variant = 0;
   uint32_t tail_pairs = 100000;
   int32_t nn_bps = 3, mg_bps = 8;
+  uint32_t grid_max = 0xffffffffu;  // PLOC: k_ploc_grid from this many live clusters (0: never)
 };
 
 struct bvh_ctx {
@@ -46,6 +47,7 @@ struct bvh_ctx {
   StageEvents evs;
   bvh_timing last{};
   int last_algo = -1;
+  uint32_t last_n = 0;     // triangles of the last single build (0 after a batched one)
   bool have_timing = false;
   uint32_t* h_status = nullptr;  // pinned copy of the device status word
   cudaStream_t last_stream = nullptr;
@@ -187,6 +189,7 @@ static void set_shapes(Workspace& ws, const TuneEntry& t) {
   ws.ploc_tail_pairs = t.tail_pairs;
   ws.ploc_nn_bps = t.nn_bps;
   ws.ploc_mg_bps = t.mg_bps;
+  ws.ploc_grid_max = t.grid_max;
 }
 
 // The table entry for this algorithm and size, else the base shapes.
@@ -204,6 +207,7 @@ static void apply_tuning(bvh_ctx* ctx, int32_t algo_key, uint32_t n) {
 static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, cudaStream_t st,
                              bvh_tree* out) {
   const uint32_t n = mesh->n;
+  ctx->last_n = n;
   apply_tuning(ctx, params->algo, n);
   ctx->have_timing = false;
   ctx->last = bvh_timing{};
@@ -230,7 +234,7 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   ScratchLayout L = scratch_layout(ctx->ws.cap_n);
   cudaMemcpyAsync(ctx->h_status, ctx->ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
   if (params->algo == BVH_ALGO_PLOC)  // iterations and live-cluster sum, read at bvh_sync
-    cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.ploc, 16 * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.ploc, 20 * 4, cudaMemcpyDeviceToHost, st);
   if (params->algo == BVH_ALGO_LBVH_PLUS && params->treelet_rounds > 0 && n > 1)  // tree height, read at bvh_sync
     cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.hist + kTlCtlWord, 2 * 4, cudaMemcpyDeviceToHost, st);
   cudaEventRecord(ctx->evs.ev[6], st);
@@ -250,7 +254,7 @@ extern "C" bvh_status bvh_build_device(bvh_ctx* ctx, const bvh_mesh_soa* mesh, c
 
 static bvh_status check_status_word(bvh_ctx* ctx) {
   uint32_t s = *ctx->h_status;
-  if (s & (kStatusSortTimeout | kStatusClimbTimeout)) return BVH_ERR_TIMEOUT;
+  if (s & (kStatusSortTimeout | kStatusClimbTimeout | kStatusGridTimeout)) return BVH_ERR_TIMEOUT;
   if (s & kStatusNoProgress) return BVH_ERR_NO_PROGRESS;
   if (s & kStatusBadInput) return BVH_ERR_DEVICE;  // a kernel skipped an index outside its buffer
   return BVH_OK;
@@ -277,6 +281,13 @@ extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
     const uint32_t* w = ctx->h_status + 4;
     ctx->last.ploc_iterations = (int32_t)w[kPlocIterWord];
     ctx->last.ploc_cluster_sum = (uint64_t)w[kPlocSumWord + 1] << 32 | w[kPlocSumWord];
+    // bounds, Morton, 4 sort passes, cluster init; 4 per iteration run as separate launches; the
+    // middle-iterations and tail kernels (each one launch, whatever it ran); the root fix
+    const int32_t one_launch_its = (int32_t)(w[16] + w[17]);
+    ctx->last.kernel_launches = ctx->last_n == 0   ? 0  // batched: the caller counts
+                                : ctx->last_n > 1 ? 7 + 4 * (ctx->last.ploc_iterations - one_launch_its) +
+                                                      (int32_t)w[18] + (int32_t)w[19] + 1
+                                                  : 7;
   } else if (ctx->last_algo == BVH_ALGO_LBVH_PLUS) {
     ctx->last.tree_height = (int32_t)ctx->h_status[5];
   }
@@ -471,6 +482,7 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   Workspace& ws = ctx->ws;
   ctx->have_timing = false;
   ctx->last = bvh_timing{};
+  ctx->last_n = 0;
   ctx->last_algo = params->algo;
   apply_tuning(ctx, params->algo + 256, n);
   const uint32_t n_items = count_items(batch->offsets, count);
@@ -536,7 +548,7 @@ extern "C" bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, co
   ScratchLayout L = scratch_layout(ws.cap_n);
   cudaMemcpyAsync(ctx->h_status, ws.scratch + L.status, 4, cudaMemcpyDeviceToHost, st);
   if (ploc)  // iterations and live-cluster sum, read at bvh_sync
-    cudaMemcpyAsync(ctx->h_status + 4, ws.scratch + L.ploc, 16 * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(ctx->h_status + 4, ws.scratch + L.ploc, 20 * 4, cudaMemcpyDeviceToHost, st);
   cudaEventRecord(ctx->evs.ev[6], st);
   ctx->last_stream = st;
   ctx->have_timing = true;
@@ -625,8 +637,8 @@ static std::string entry_json(const TuneEntry& t) {
   char buf[200];
   snprintf(buf, sizeof(buf),
            "{\"algo\": %d, \"bucket\": %d, \"sort_variant\": %d, \"ploc_tail_pairs\": %u, \"ploc_nn_bps\": %d, "
-           "\"ploc_mg_bps\": %d}",
-           t.algo, t.bucket, t.sort_variant, t.tail_pairs, t.nn_bps, t.mg_bps);
+           "\"ploc_mg_bps\": %d, \"ploc_grid_max\": %u}",
+           t.algo, t.bucket, t.sort_variant, t.tail_pairs, t.nn_bps, t.mg_bps, t.grid_max);
   return buf;
 }
 
@@ -694,6 +706,7 @@ extern "C" bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh,
   best.tail_pairs = ctx->ws.ploc_tail_pairs;
   best.nn_bps = ctx->ws.ploc_nn_bps;
   best.mg_bps = ctx->ws.ploc_mg_bps;
+  best.grid_max = ctx->ws.ploc_grid_max;
   best.algo = algo;
   best.bucket = size_bucket(n);
   ctx->tuning_locked = true;
@@ -709,11 +722,13 @@ extern "C" bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh,
     if (s != BVH_OK) return s;
     if (first) ref_hash = h;
     const bool same = h == ref_hash;
-    char buf[240];
+    char buf[320];
     snprintf(buf, sizeof(buf),
              "%s{\"sort_variant\": %d, \"ploc_tail_pairs\": %u, \"ploc_nn_bps\": %d, \"ploc_mg_bps\": %d, "
+             "\"ploc_grid_max\": %u, "
              "\"ms\": %.4f, \"same_tree\": %s}",
-             trials.empty() ? "" : ", ", t.sort_variant, t.tail_pairs, t.nn_bps, t.mg_bps, ms, same ? "true" : "false");
+             trials.empty() ? "" : ", ", t.sort_variant, t.tail_pairs, t.nn_bps, t.mg_bps, t.grid_max, ms,
+             same ? "true" : "false");
     trials += buf;
     if (!same) return BVH_ERR_DEVICE;  // a launch shape changed the tree: never expected
     if (first || ms < best_ms) {
@@ -743,6 +758,11 @@ extern "C" bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh,
       TuneEntry t = best;
       t.mg_bps = k;
       if (s == BVH_OK && k != best.mg_bps) s = trial(t, false);
+    }
+    for (uint32_t g : {0u, 65536u, 150000u, 0xffffffffu}) {
+      TuneEntry t = best;
+      t.grid_max = g;
+      if (s == BVH_OK && g != best.grid_max) s = trial(t, false);
     }
   }
   // choices that change the tree are reported with their cost and SAH, not chosen
@@ -833,6 +853,10 @@ extern "C" bvh_status bvh_tuning_import(bvh_ctx* ctx, const char* json) {
     }
     if (json_int(o, c, "ploc_nn_bps", &v)) t.nn_bps = (int32_t)v;
     if (json_int(o, c, "ploc_mg_bps", &v)) t.mg_bps = (int32_t)v;
+    if (json_int(o, c, "ploc_grid_max", &v)) {
+      if (v < 0 || v > 0xffffffffll) return BVH_ERR_INVALID_ARG;
+      t.grid_max = (uint32_t)v;
+    }
     if (!valid_entry(t)) return BVH_ERR_INVALID_ARG;
     table.push_back(t);
     o = c;

@@ -35,6 +35,7 @@ enum : uint32_t {
   kStatusClimbTimeout = 1u << 1,    // reserved: bounded waits in bottom-up passes
   kStatusNoProgress = 1u << 2,      // PLOC iteration merged nothing
   kStatusBadInput = 1u << 3,        // index outside its buffer was seen and skipped
+  kStatusGridTimeout = 1u << 4,     // a grid-wide barrier of a cooperative kernel gave up
 };
 
 // Spin limit for every device-side wait: ~1e7 polls of an L2 line (well over 100 ms),

@@ -35,7 +35,7 @@ ScratchLayout scratch_layout(uint32_t n) {
   L.epoch = o; o += 1;
   o = (o + 3) & ~size_t(3);
   L.scene = o; o += 8;
-  L.ploc = o; o += 16;
+  L.ploc = o; o += 20;
   L.partials = o; o += (size_t)kBoundsBlocks * 8;
   o = (o + 3) & ~size_t(3);
   L.zero_begin = o;

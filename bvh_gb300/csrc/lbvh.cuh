@@ -18,6 +18,8 @@ struct Workspace {
   int sort_variant = 0;      // onesweep variant (bvh_autotune)
   // PLOC launch shapes (bvh_autotune_build); none of them changes the tree
   uint32_t ploc_tail_pairs = 100000;  // hand over to k_ploc_tail below this many pair areas (0: never)
+  uint32_t ploc_grid_max = 0xffffffffu;  // k_ploc_grid takes over at this many live clusters
+                                         // (capped at what its grid holds; 0: never)
   int ploc_nn_bps = 3;                // neighbour-search blocks per SM
   int ploc_mg_bps = 8;                // merge (count / scatter) blocks per SM
   void* keys[2] = {nullptr, nullptr};
@@ -86,7 +88,7 @@ struct ScratchLayout {
   size_t hist;       // passes * 256
   size_t desc;       // passes * tiles * 256
   size_t partials;   // bounds partials, kBoundsBlocks * 8
-  size_t ploc;       // PLOC control words (16)
+  size_t ploc;       // PLOC control words (20)
   size_t zero_begin; // first word zeroed at the start of each build
   size_t zero_end;
   size_t total;

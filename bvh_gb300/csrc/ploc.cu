@@ -29,6 +29,12 @@ constexpr int kPlocTile = kPlocThreads * kPlocIpt;
 //   [11] meshes (1 for a single build): the loop ends at one cluster per mesh
 //   [12] hand-over size: the loop stops at this many live clusters and k_ploc_tail finishes
 //        (0: no hand-over)
+//   [13] single builds: the node that took node 0 (sorted triangle 0's leaf) as its left child,
+//        for the root fix (cluster 0 stays at position 0 until it merges, always as the left)
+//   [14] single builds: the loop also stops at this many live clusters and k_ploc_grid goes on
+//        (0: no hand-over)  [15] k_ploc_grid's barrier counter
+//   [16] iterations run by k_ploc_grid  [17] iterations run by k_ploc_tail
+//   [18] k_ploc_grid was launched  [19] k_ploc_tail was launched (launch accounting)
 struct PlocBufs {
   Box* cbox[2];
   int32_t* cid[2];
@@ -52,7 +58,7 @@ struct PlocSeg {
 };
 
 __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __restrict__ tri_boxes, PlocBufs B, uint32_t n,
-                            uint32_t cap, uint32_t tail) {
+                            uint32_t cap, uint32_t tail, uint32_t grid_at) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     B.ctrl[0] = n;
@@ -65,6 +71,10 @@ __global__ void k_ploc_init(const uint32_t* __restrict__ sidx, const Box* __rest
     B.ctrl[9] = 0;
     B.ctrl[11] = 1;
     B.ctrl[12] = tail;
+    B.ctrl[13] = 0xffffffffu;
+    B.ctrl[14] = grid_at;
+#pragma unroll
+    for (int k = 15; k < 20; ++k) B.ctrl[k] = 0;
   }
   if (i >= n) return;
   uint32_t prim = __ldg(sidx + i);
@@ -282,7 +292,7 @@ __device__ __forceinline__ void ploc_step(PlocBufs B, cudaGraphConditionalHandle
   if (go && (nc >= c || it >= cap)) {  // no mutual pair anywhere, or the cap: stop and report
     atomicOr(B.status, kStatusNoProgress);
     go = false;
-  } else if (go && nc <= B.ctrl[12]) {  // few enough for k_ploc_tail, which finishes the loop
+  } else if (go && (nc <= B.ctrl[12] || nc <= B.ctrl[14])) {  // k_ploc_grid / k_ploc_tail go on
     go = false;
   }
   if constexpr (GRAPH) cudaGraphSetConditional(handle, go ? 1u : 0u);
@@ -475,6 +485,7 @@ __device__ __forceinline__ void scatter_tiles(const PlocBufs& B, uint32_t c, uin
           } else {
             nid = (int32_t)(next + mpos + __popc(mb[r] & lt));
             np = reinterpret_cast<float4*>(nodes + nid);
+            if (id[g] == 0) B.ctrl[13] = (uint32_t)nid;  // node 0's parent, for the root fix
           }
           if (np) {
             np[0] = make_float4(a.x, a.y, a.z, 0.f);
@@ -581,6 +592,8 @@ __global__ void __launch_bounds__(256) k_ploc_init_seg(const uint32_t* __restric
     B.ctrl[9] = 0;
     B.ctrl[11] = S.count;
     B.ctrl[12] = 0;
+#pragma unroll
+    for (int k = 14; k < 20; ++k) B.ctrl[k] = 0;
   }
   for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
     const SegItem w = items[it];
@@ -636,6 +649,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_ploc_tail(PlocBufs B, int r
   int32_t* s_nbr = s_id[1] + kTailMax;
   uint32_t* s_w = reinterpret_cast<uint32_t*>(s_nbr + kTailMax);  // 2 x 32 warp sums
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) B.ctrl[19] = 1;
   uint32_t c = __ldcg(B.ctrl + 0);
   // nothing left, or the loop stopped without handing over (too many clusters, an error)
   if (c <= 1 || c > kTailMax || (__ldcg(B.status) & kStatusNoProgress)) return;
@@ -649,6 +663,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_ploc_tail(PlocBufs B, int r
     s_id[0][x] = __ldcg(idin + x);
   }
   uint32_t next = __ldcg(B.ctrl + 1), it = __ldcg(B.ctrl + 6);
+  const uint32_t it0 = it;
   const uint32_t cap = __ldcg(B.ctrl + 7);
   unsigned long long sum = (unsigned long long)__ldcg(B.ctrl + 9) << 32 | __ldcg(B.ctrl + 8);
   int cur = 0;
@@ -734,6 +749,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_ploc_tail(PlocBufs B, int r
         np[0] = a;
         np[1] = b;
         reinterpret_cast<int4*>(np + 2)[0] = make_int4(nid, s_id[cur][j], 0, 0);
+        if (nid == 0) B.ctrl[13] = (uint32_t)id_new;  // node 0's parent, for the root fix
         nid = id_new;
         ++mpos;
       }
@@ -762,14 +778,231 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_ploc_tail(PlocBufs B, int r
     B.ctrl[6] = it;
     B.ctrl[8] = (uint32_t)sum;
     B.ctrl[9] = (uint32_t)(sum >> 32);
+    B.ctrl[17] = it - it0;
+    if (no_progress) atomicOr(B.status, kStatusNoProgress);
+  }
+}
+
+// The middle iterations in one cooperative kernel.  Between the iterations over many clusters
+// (one launch per phase over persistent grids) and k_ploc_tail (one block), an iteration costs
+// mostly the latency of its four launches.  k_ploc_grid runs those iterations in one cooperative
+// launch (every block resident): block b owns the contiguous chunk [b*ch, (b+1)*ch) of at most
+// kGridPerBlock clusters and stages its window (the chunk and r clusters either side) in shared
+// memory; grid barriers separate the neighbour search, the flag count and the merge + compaction.
+// Same rules and results as the kernels above and k_ploc_tail (neighbour = smallest union area in
+// [x-r, x+r], smallest j on ties, +inf and NaN never winning; mutual pairs merge into the smaller
+// index; new ids in ascending cluster order; survivors compacted in order; the same stop rules,
+// iteration count and live-cluster sum).  It runs while the live clusters number more than the
+// tail hand-over (ctrl[12]) and at most kGridPerBlock per block.
+constexpr int kGridThreads = 1024;
+constexpr uint32_t kGridPerBlock = 2048;  // 2 clusters per thread
+constexpr int kGridMaxR = 128;
+constexpr uint32_t kGridWin = kGridPerBlock + 2 * kGridMaxR;
+constexpr uint32_t kGridMaxBlocks = 1024;
+static size_t grid_smem() { return (size_t)kGridWin * (2 * 16 + 4) + 64 * 8; }
+
+// Grid-wide barrier of a cooperative launch: arrivals count up in *bar, and the k-th barrier of
+// the kernel waits until k * gridDim.x blocks have arrived.  Bounded: past kSpinLimit polls the
+// block records kStatusGridTimeout and returns false (every other block then gives up at its
+// next wait).  The counter is zeroed before the launch (k_ploc_init).
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, uint32_t* status, uint32_t* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    uint32_t ok = 1, spins = 0;
+    while (ld_acquire(bar) < target) {
+      if (++spins > kSpinLimit) {
+        atomicOr(status, kStatusGridTimeout);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// Exclusive block scan of one 64-bit value per thread (kGridThreads); *total gets the sum.
+__device__ __forceinline__ unsigned long long grid_block_scan(unsigned long long v, unsigned long long* s_w,
+                                                              unsigned long long* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long t = s_w[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    s_w[32 + lane] = t;  // inclusive warp totals
+  }
+  __syncthreads();
+  const unsigned long long before = (wid ? s_w[32 + wid - 1] : 0ull) + x - v;
+  *total = s_w[32 + 31];
+  __syncthreads();  // s_w is reused by the next scan
+  return before;
+}
+
+__global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r) {
+  extern __shared__ float4 gsm[];
+  float4* s_lo = gsm;
+  float4* s_hi = gsm + kGridWin;
+  int32_t* s_id = reinterpret_cast<int32_t*>(gsm + 2 * kGridWin);
+  unsigned long long* s_w = reinterpret_cast<unsigned long long*>(s_id + kGridWin);
+  __shared__ uint32_t s_ok;
+  const uint32_t G = gridDim.x, b = blockIdx.x;
+  const int tid = threadIdx.x;
+  if (b == 0 && tid == 0) B.ctrl[18] = 1;  // (no block reads it)
+  // every block reads the same words (nothing writes them before the first barrier)
+  uint32_t c = __ldcg(B.ctrl + 0);
+  const uint32_t tail = __ldcg(B.ctrl + 12), cap = __ldcg(B.ctrl + 7);
+  if (c <= 1 || c <= tail || c > G * kGridPerBlock || r > kGridMaxR || r < 1 ||
+      (__ldcg(B.status) & kStatusNoProgress))
+    return;
+  uint32_t next = __ldcg(B.ctrl + 1), par = __ldcg(B.ctrl + 3) & 1u, it = __ldcg(B.ctrl + 6);
+  const uint32_t it0 = it;
+  unsigned long long sum = (unsigned long long)__ldcg(B.ctrl + 9) << 32 | __ldcg(B.ctrl + 8);
+  uint32_t* bar = B.ctrl + 15;
+  unsigned long long* totals = reinterpret_cast<unsigned long long*>(B.flags);  // one per block
+  uint32_t nbar = 0;
+  bool no_progress = false, ok = true;
+  const float kInf = __int_as_float(0x7f800000);
+  while (true) {
+    const Box* cin = par ? B.cbox[1] : B.cbox[0];
+    const int32_t* idin = par ? B.cid[1] : B.cid[0];
+    Box* cout = par ? B.cbox[0] : B.cbox[1];
+    int32_t* idout = par ? B.cid[0] : B.cid[1];
+    const uint32_t ch = div_up(c, G);
+    const uint32_t x0 = min(c, b * ch), x1 = min(c, x0 + ch);
+    const uint32_t w0 = x0 > (uint32_t)r ? x0 - (uint32_t)r : 0u, w1 = min(c, x1 + (uint32_t)r);
+    for (uint32_t x = w0 + tid; x < w1; x += kGridThreads) {
+      const float4* bp = reinterpret_cast<const float4*>(cin + x);
+      s_lo[x - w0] = __ldcg(bp);
+      s_hi[x - w0] = __ldcg(bp + 1);
+      s_id[x - w0] = __ldcg(idin + x);
+    }
+    __syncthreads();
+    // neighbours of the chunk: ascending j with a strict < keeps the smallest j of equal areas
+    for (uint32_t x = x0 + tid; x < x1; x += kGridThreads) {
+      const float4 xa = s_lo[x - w0], xb = s_hi[x - w0];
+      const uint32_t j0 = x > (uint32_t)r ? x - (uint32_t)r : 0u, j1 = min(c - 1, x + (uint32_t)r);
+      float best = kInf;
+      int32_t bj = -1;
+      for (uint32_t j = j0; j <= j1; ++j) {
+        if (j == x) continue;
+        const float d = pair_area(xa, xb, s_lo[j - w0], s_hi[j - w0]);
+        if (d < best) {
+          best = d;
+          bj = (int32_t)j;
+        }
+      }
+      __stcg(B.nbr + x, bj);
+    }
+    if (!(ok = grid_sync(bar, ++nbar * G, B.status, &s_ok))) break;
+    // merge / survivor flags of this thread's clusters x0 + 2 tid + q (ascending)
+    bool m2[2] = {false, false}, v2[2] = {false, false};
+    int32_t nj[2] = {-1, -1};
+    uint32_t mk = 0, vk = 0;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t x = x0 + 2u * (uint32_t)tid + (uint32_t)q;
+      if (x < x1) {
+        const int32_t j = __ldcg(B.nbr + x);
+        const int32_t back = (j >= 0 && (uint32_t)j < c) ? __ldcg(B.nbr + j) : -1;
+        const bool mutual = j >= 0 && back == (int32_t)x;
+        m2[q] = mutual && (int32_t)x < j;
+        v2[q] = !(mutual && j < (int32_t)x);
+        nj[q] = j;
+      }
+      mk += m2[q];
+      vk += v2[q];
+    }
+    unsigned long long btot;
+    const unsigned long long before = grid_block_scan((unsigned long long)mk << 32 | vk, s_w, &btot);
+    if (tid == 0) __stcg(totals + b, btot);
+    if (!(ok = grid_sync(bar, ++nbar * G, B.status, &s_ok))) break;
+    // this block's offset and the totals over all blocks
+    unsigned long long mine = 0;
+    for (uint32_t k = (uint32_t)tid; k < G; k += kGridThreads) mine += k < b ? __ldcg(totals + k) : 0ull;
+    unsigned long long all = 0;
+    for (uint32_t k = (uint32_t)tid; k < G; k += kGridThreads) all += __ldcg(totals + k);
+    unsigned long long offs_b, grand_b;  // the block sums of `mine` and `all`
+    grid_block_scan(mine, s_w, &offs_b);
+    grid_block_scan(all, s_w, &grand_b);
+    uint32_t mpos = (uint32_t)(offs_b >> 32) + (uint32_t)(before >> 32);
+    uint32_t vpos = (uint32_t)offs_b + (uint32_t)before;
+    const uint32_t M = (uint32_t)(grand_b >> 32), V = (uint32_t)grand_b;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t xi = x0 + 2u * (uint32_t)tid + (uint32_t)q;
+      if (xi >= x1) continue;
+      float4 a = s_lo[xi - w0], bb = s_hi[xi - w0];
+      int32_t nid = s_id[xi - w0];
+      if (m2[q]) {
+        const uint32_t j = (uint32_t)nj[q];  // within [xi - r, xi + r], so inside the staged window
+        const float4 ja = s_lo[j - w0], jb = s_hi[j - w0];
+        a = make_float4(fminf(a.x, ja.x), fminf(a.y, ja.y), fminf(a.z, ja.z), 0.f);
+        bb = make_float4(fmaxf(bb.x, jb.x), fmaxf(bb.y, jb.y), fmaxf(bb.z, jb.z), 0.f);
+        const int32_t id_new = (int32_t)(next + mpos);
+        float4* np = reinterpret_cast<float4*>(B.nodes + id_new);
+        np[0] = a;
+        np[1] = bb;
+        reinterpret_cast<int4*>(np + 2)[0] = make_int4(nid, s_id[j - w0], 0, 0);
+        if (nid == 0) B.ctrl[13] = (uint32_t)id_new;  // node 0's parent, for the root fix
+        nid = id_new;
+        ++mpos;
+      }
+      if (v2[q]) {
+        float4* op = reinterpret_cast<float4*>(cout + vpos);
+        op[0] = a;
+        op[1] = bb;
+        idout[vpos] = nid;
+        ++vpos;
+      }
+    }
+    sum += c;
+    ++it;
+    next += M;
+    const uint32_t prev = c;
+    c = V;
+    par ^= 1u;
+    if (c <= 1) break;
+    if (c >= prev || it >= cap) {  // no mutual pair anywhere, or the cap
+      no_progress = true;
+      break;
+    }
+    if (c <= tail) break;
+    if (!(ok = grid_sync(bar, ++nbar * G, B.status, &s_ok))) break;  // the next window reads the compacted buffer
+  }
+  if (ok && b == 0 && tid == 0) {
+    B.ctrl[0] = c;
+    B.ctrl[1] = next;
+    B.ctrl[3] = par;
+    B.ctrl[6] = it;
+    B.ctrl[8] = (uint32_t)sum;
+    B.ctrl[9] = (uint32_t)(sum >> 32);
+    B.ctrl[16] = it - it0;
     if (no_progress) atomicOr(B.status, kStatusNoProgress);
   }
 }
 
 // Move the root (last node) to index 0 and swap every reference to 0 and the root
-// (ploc_builder.cu:563-582); skipped when the loop did not converge.  Thread 0 owns 0 and R.
+// (ploc_builder.cu:563-582); skipped when the loop did not converge.  The root has no parent and
+// node 0 (a leaf) has one, recorded by the merge that made it (ctrl[13]), so three nodes change:
+// 0, R and that parent.  Without a recorded parent every node is checked (one block).
 __global__ void k_ploc_root(Node* __restrict__ nodes, uint32_t total, const uint32_t* __restrict__ ctrl) {
-  if (__ldcg(ctrl + 0) != 1) return;
+  if (__ldcg(ctrl + 0) != 1 || total < 2) return;
   const uint32_t R = total - 1;
   auto fix = [&](int32_t c) -> int32_t {
     if (c < 0) return c;
@@ -777,7 +1010,16 @@ __global__ void k_ploc_root(Node* __restrict__ nodes, uint32_t total, const uint
     if (c == (int32_t)R) return 0;
     return c;
   };
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+  const uint32_t p = __ldcg(ctrl + 13);
+  const bool known = p > 0 && p < total;
+  for (uint32_t k = threadIdx.x; k < total; k += blockDim.x) {
+    if (known && k != 0) {  // only node 0's parent refers to 0 or R (R itself moves with k == 0)
+      if (k == 1 && p != R) {
+        int2 ch = *reinterpret_cast<int2*>(&nodes[p].left);
+        *reinterpret_cast<int2*>(&nodes[p].left) = make_int2(fix(ch.x), fix(ch.y));
+      }
+      break;
+    }
     if (k == 0) {
       Node a = nodes[0], b = nodes[R];
       if (b.left >= 0) { b.left = fix(b.left); b.right = fix(b.right); }
@@ -957,10 +1199,27 @@ static cudaError_t set_tail_smem() {
   return cudaFuncSetAttribute(k_ploc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem());
 }
 
+// Blocks of a k_ploc_grid launch on the current device: SMs x resident blocks per SM, or 0 where
+// cooperative launches are not available.  Sets the kernel's shared-memory limit (so it is called
+// before any capture, from ploc_prepare, and again by builds).
+static uint32_t ploc_grid_blocks() {
+  int dev = 0, coop = 0, sms = 0, occ = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaFuncSetAttribute(k_ploc_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)grid_smem()) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_ploc_grid, kGridThreads, grid_smem()) != cudaSuccess)
+    return 0;
+  return (uint32_t)std::min<long long>((long long)sms * occ, kGridMaxBlocks);
+}
+
 cudaError_t ploc_prepare(int radius) {
   cudaError_t e = set_nn_smem<false>(radius);
   if (e == cudaSuccess) e = set_nn_smem<true>(radius);
-  return e == cudaSuccess ? set_tail_smem() : e;
+  if (e == cudaSuccess) e = set_tail_smem();
+  if (e == cudaSuccess) ploc_grid_blocks();
+  return e;
 }
 
 cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius, int max_iter, cudaStream_t st,
@@ -976,7 +1235,14 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   // every iteration that makes progress removes at least one cluster, so n bounds the loop
   const uint32_t cap = max_iter > 0 ? (uint32_t)max_iter : n;
   const uint32_t tail = ploc_tail_threshold(radius, ws.ploc_tail_pairs);
-  const bool loop = n > 1 && n > tail;  // else k_ploc_tail runs every iteration
+  // k_ploc_grid: from grid_at live clusters down to the tail hand-over (its per-block totals
+  // live in the ballot words, which hold them from 65,536 triangles on)
+  const uint32_t grid_blocks = ploc_grid_blocks();
+  uint32_t grid_at = 0;
+  if (grid_blocks && radius <= kGridMaxR && n >= 65536)
+    grid_at = std::min<uint32_t>(ws.ploc_grid_max, grid_blocks * kGridPerBlock);
+  if (grid_at <= tail) grid_at = 0;
+  const bool loop = n > 1 && n > std::max(tail, grid_at);  // else the one-launch kernels do every iteration
   const PlocShape sh = ploc_shape(ws);
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
   if (loop && !host_loop) {
@@ -997,7 +1263,7 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
   uint32_t* sidx = nullptr;
   if ((e = prefix_sort30(ws, m, n, st, evs, &sidx)) != cudaSuccess) return e;
   *out_indices = sidx;
-  k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap, tail);
+  k_ploc_init<<<div_up(n, 256), 256, 0, st>>>(sidx, ws.boxes, B, n, cap, tail, grid_at);
   if (evs && evs->use) cudaEventRecord(evs->ev[4], st);
   if (loop && host_loop) {
     for (uint32_t it = 0; it < cap; ++it) {
@@ -1011,8 +1277,21 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
     if ((e = cudaGraphLaunch(ws.ploc_exec, st)) != cudaSuccess) return e;
   }
   if (n > 1) {
+    if (grid_at) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grid_blocks);
+      cfg.blockDim = dim3(kGridThreads);
+      cfg.dynamicSmemBytes = grid_smem();
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      if ((e = cudaLaunchKernelEx(&cfg, k_ploc_grid, B, radius)) != cudaSuccess) return e;
+    }
     if (tail) k_ploc_tail<<<1, kTailThreads, tail_smem(), st>>>(B, radius);
-    k_ploc_root<<<std::min<uint32_t>(div_up(2 * n - 1, 256), 152 * 8), 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
+    k_ploc_root<<<1, 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);
   }
   if (evs && evs->use) cudaEventRecord(evs->ev[5], st);
   return cudaGetLastError();

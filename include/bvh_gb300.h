@@ -100,6 +100,10 @@ typedef struct bvh_timing {
   int32_t ploc_iterations;
   int32_t tree_height;       /* LBVH+: tree height in the last treelet pass (one kernel pair per level) */
   uint64_t ploc_cluster_sum; /* sum of live clusters over PLOC iterations */
+  int32_t kernel_launches;   /* PLOC: this library's kernels the build launched (its loop runs on the
+                                device: 4 per iteration launched one kernel per phase, 1 each for the
+                                middle-iterations and tail kernels); 0 for the other algorithms */
+  int32_t reserved;
 } bvh_timing;
 
 /* Per-ray traversal result (HitInfo, src/render_engine.cu:279-287, minus the normal). */
@@ -213,7 +217,8 @@ bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
 
 /* Autotuner for whole builds (no reference counterpart).  Builds `mesh` (device SoA, at least
  * 1,024 triangles) with `params` under each launch shape -- radix-sort variant; for PLOC also the
- * size at which the one-block tail kernel takes over and the neighbour-search and merge grids --
+ * sizes at which the cooperative middle-iterations kernel and the one-block tail kernel take
+ * over, and the neighbour-search and merge grids --
  * by coordinate descent, 3 timed builds each, checking that every shape gives the identical
  * tree (a device hash of all node fields; BVH_ERR_DEVICE if one did not).  The fastest is kept in
  * the context's tuning table under (algorithm, floor(log2(n))) and used by later builds of that
@@ -225,7 +230,7 @@ bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
 bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, void* stream,
                               char* json_out, size_t json_cap);
 /* The tuning table as JSON ({"base": {...}, "entries": [{"algo", "bucket", "sort_variant",
- * "ploc_tail_pairs", "ploc_nn_bps", "ploc_mg_bps"}, ...]}), to persist it; and back (replaces the
+ * "ploc_tail_pairs", "ploc_nn_bps", "ploc_mg_bps", "ploc_grid_max"}, ...]}), to persist it; and back (replaces the
  * table; BVH_ERR_INVALID_ARG for malformed input or out-of-range shapes). */
 bvh_status bvh_tuning_export(const bvh_ctx* ctx, char* json_out, size_t json_cap);
 bvh_status bvh_tuning_import(bvh_ctx* ctx, const char* json);

@@ -33,6 +33,7 @@ def test_autotune_keeps_the_tree_and_reports_quality(gpu, oracle_lib, mesh_dev, 
     assert rep["trials"] and all(t["same_tree"] for t in rep["trials"])
     if algo == C.ALGO_PLOC:  # the PLOC shapes were all tried
         assert {t["ploc_tail_pairs"] for t in rep["trials"]} >= {0, 50000, 100000, 200000}
+        assert {t["ploc_grid_max"] for t in rep["trials"]} >= {0, 65536, 150000, 2**32 - 1}
     assert [q[knob] for q in rep["tree_changing"]] == values
     assert all(q["sah"] > 0 and q["ms"] > 0 for q in rep["tree_changing"])
     chosen = rep["chosen"]
@@ -55,8 +56,12 @@ def test_odd_shapes_from_an_imported_table_give_the_same_tree(gpu, oracle_lib, m
     ctx = Context(0)
     params = ctx.params(C.ALGO_PLOC, ploc_radius=25)
     ref_nodes, ref_idx, _, _ = build(ctx, gpu, m, params)
-    for shape in ({"sort_variant": 3, "ploc_tail_pairs": 0, "ploc_nn_bps": 2, "ploc_mg_bps": 16},
-                  {"sort_variant": 4, "ploc_tail_pairs": 200000, "ploc_nn_bps": 4, "ploc_mg_bps": 4}):
+    for shape in ({"sort_variant": 3, "ploc_tail_pairs": 0, "ploc_nn_bps": 2, "ploc_mg_bps": 16,
+                   "ploc_grid_max": 0},
+                  {"sort_variant": 4, "ploc_tail_pairs": 200000, "ploc_nn_bps": 4, "ploc_mg_bps": 4,
+                   "ploc_grid_max": 100000},
+                  {"sort_variant": 1, "ploc_tail_pairs": 0, "ploc_nn_bps": 3, "ploc_mg_bps": 8,
+                   "ploc_grid_max": 2**32 - 1}):
         entry = dict(algo=C.ALGO_PLOC, bucket=bucket, **shape)
         ctx.tuning_import(json.dumps({"entries": [entry]}))
         assert json.loads(ctx.tuning_export())["entries"] == [entry]
