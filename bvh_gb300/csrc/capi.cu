@@ -266,10 +266,11 @@ extern "C" bvh_status bvh_selftest_bounded_wait(int device, uint32_t polls) {
       polls > kSpinLimit)
     return BVH_ERR_INVALID_ARG;
   cudaSetDevice(device);
-  uint32_t status = 0;
+  uint32_t status = 0, grid_status = 0;
   cudaError_t e = wait_selftest(polls, &status);
   if (e != cudaSuccess) return from_cuda(e);
-  return (status & kStatusSortTimeout) ? BVH_ERR_TIMEOUT : BVH_ERR_DEVICE;
+  if ((e = grid_wait_selftest(polls, &grid_status)) != cudaSuccess) return from_cuda(e);
+  return (status & kStatusSortTimeout) && (grid_status & kStatusGridTimeout) ? BVH_ERR_TIMEOUT : BVH_ERR_DEVICE;
 }
 
 extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {

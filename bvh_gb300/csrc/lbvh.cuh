@@ -135,6 +135,9 @@ cudaError_t prefix_sort30(Workspace& ws, const MeshPtrs& m, uint32_t n, cudaStre
 // Runs the sort's bounded look-back wait against a predecessor that never publishes, giving up
 // after `limit` polls; *status_out = the status word it left (kStatusSortTimeout expected).
 cudaError_t wait_selftest(uint32_t limit, uint32_t* status_out);
+// Runs the cooperative PLOC kernel's grid barrier against a block that never arrives, giving up
+// after `limit` polls per block; *status_out = the status word it left (kStatusGridTimeout).
+cudaError_t grid_wait_selftest(uint32_t limit, uint32_t* status_out);
 
 // Kernel attributes (dynamic shared memory limits), set once per device before any capture.
 cudaError_t prepare_kernels();

@@ -805,14 +805,15 @@ static size_t grid_smem() { return (size_t)kGridWin * (2 * 16 + 4) + 64 * 8; }
 // the kernel waits until k * gridDim.x blocks have arrived.  Bounded: past kSpinLimit polls the
 // block records kStatusGridTimeout and returns false (every other block then gives up at its
 // next wait).  The counter is zeroed before the launch (k_ploc_init).
-__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, uint32_t* status, uint32_t* s_ok) {
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, uint32_t* status, uint32_t* s_ok,
+                                          uint32_t limit = kSpinLimit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     atomicAdd(bar, 1u);
     uint32_t ok = 1, spins = 0;
     while (ld_acquire(bar) < target) {
-      if (++spins > kSpinLimit) {
+      if (++spins > limit) {
         atomicOr(status, kStatusGridTimeout);
         ok = 0;
         break;
@@ -995,6 +996,44 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
     B.ctrl[16] = it - it0;
     if (no_progress) atomicOr(B.status, kStatusNoProgress);
   }
+}
+
+// Self-test of the grid barrier's bound: a cooperative launch whose blocks wait for one arrival
+// more than there are blocks (a block that never comes), giving up after `limit` polls each.
+// Words: [0] arrival counter, [1] status.
+__device__ uint32_t g_grid_selftest[2];
+
+__global__ void k_grid_selftest(uint32_t limit) {
+  __shared__ uint32_t s_ok;
+  grid_sync(g_grid_selftest, gridDim.x + 1, g_grid_selftest + 1, &s_ok, limit);
+}
+
+cudaError_t grid_wait_selftest(uint32_t limit, uint32_t* status_out) {
+  int dev = 0, coop = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (e != cudaSuccess) return e;
+  if (!coop) return cudaErrorNotSupported;
+  cudaStream_t st = nullptr;
+  if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  const uint32_t zero[2] = {0u, 0u};
+  e = cudaMemcpyToSymbolAsync(g_grid_selftest, zero, sizeof(zero), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(4);
+    cfg.blockDim = dim3(64);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_grid_selftest, limit);
+  }
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(status_out, g_grid_selftest, 4, 4, cudaMemcpyDeviceToHost, st);
+  const cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return e != cudaSuccess ? e : e2;
 }
 
 // Move the root (last node) to index 0 and swap every reference to 0 and the root

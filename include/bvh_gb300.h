@@ -183,11 +183,12 @@ bvh_status bvh_build_host(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_para
 bvh_status bvh_tree_download(bvh_ctx* ctx, const bvh_tree* tree, void* stream, bvh_node* host_nodes,
                              uint32_t* host_indices);
 
-/* Self-test of the device-side bounded wait (no reference counterpart): the radix sort's
- * look-back wait is run on `device` against a predecessor that never publishes, giving up after
- * `polls` polls (1 .. 16,777,216).  Returns BVH_ERR_TIMEOUT -- the expected outcome: the wait
+/* Self-test of the device-side bounded waits (no reference counterpart): the radix sort's
+ * look-back wait is run on `device` against a predecessor that never publishes, and the grid
+ * barrier of the cooperative PLOC kernel against a block that never arrives, each giving up after
+ * `polls` polls (1 .. 16,777,216).  Returns BVH_ERR_TIMEOUT -- the expected outcome: both waits
  * ended and reported it, and the device is still usable -- or BVH_ERR_DEVICE / another error if
- * it did not.  Synchronous; allocates nothing. */
+ * either did not.  Synchronous; allocates nothing. */
 bvh_status bvh_selftest_bounded_wait(int device, uint32_t polls);
 
 /* Timing of the last build; waits for it to finish.  Also reports device-side errors. */
