@@ -126,14 +126,39 @@ def stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0, clust
     return 144.0 * rounds
 
 
+def impl_stage_bytes_per_tri(stage: str, algo: str, bits: int, rounds: int = 0,
+                             cluster_sum_per_tri: float = 0.0) -> float:
+    """Bytes per triangle this implementation moves in a stage (its own buffers, not the problem's
+    B(K) split): bounds 36 read; Morton 36 read + 4 key + (60/63-bit: 4 low bits) + 32 box
+    written; sort: 4 passes over 32-bit (key, index) pairs, 12 B in the first (no index read) and
+    16 B in each other, + for 60/63-bit codes the run fix-up's 8 B read, 1 B delta write and about
+    4 B of low-bit gathers and index moves; emission: 4 index + 32 box gathered + 48 leaf + 48
+    internal node + 1 delta (30-bit: 4 key read, the delta bytes stay in shared memory).  Stages
+    this accounting does not split (the treelet pass, the PLOC loop and its cluster init) report
+    their algorithmic bytes."""
+    split = bits != 30 and algo != "ploc"
+    if stage == "scene_bounds":
+        return 36.0
+    if stage == "morton_boxes_hist":
+        return 36.0 + 4 + (4 if split else 0) + 32.0
+    if stage == "onesweep_sort":
+        return 12.0 + 3 * 16.0 + (13.0 if split else 0.0)
+    if stage == "emit_refit" and algo != "ploc":
+        return 4.0 + 32 + 48 + 48 + (1.0 if split else 4.0)
+    return stage_bytes_per_tri(stage, algo, bits, rounds, cluster_sum_per_tri)
+
+
 def kernels_per_build(algo: str, bits: int, rounds: int = 0, ploc_iterations: int = 0, tree_height: int = 0) -> int:
     """Launches of this library's kernels in one build: bounds, Morton, 4 onesweep passes, the run
     fix-up of 60/63-bit codes (short runs, listed long runs; it writes the delta bytes too),
     emission (which computes the delta bytes of 30-bit codes) + frontier climb;
     per treelet pass five (heights, counts, offsets, grouping by height, the fallback check) plus
     growth, DP and loop control per tree level; PLOC adds cluster init, 4 per clustering iteration
-    (neighbours, tile counts + scan, merge + compaction, loop control) and the root fix (its
-    30-bit prefix stops after the sort)."""
+    launched one kernel per phase (neighbours, tile counts + scan, merge + compaction, loop
+    control) and the root fix
+    (its 30-bit prefix stops after the sort).  A PLOC build reports its exact count itself (some
+    iterations run inside its middle-iterations and tail kernels); this is the count when every
+    iteration is launched per phase."""
     if algo == "ploc":
         return 2 + 4 + 1 + 4 * ploc_iterations + 1
     n = 2 + 4 + (2 if bits != 30 else 0) + 2
@@ -394,7 +419,7 @@ def run_ours(args):
             t = ctx.last_timing()
             stages.append((t.bounds_ms, t.morton_ms, t.sort_ms, t.emit_ms, t.optimize_ms, t.total_ms))
             ploc_iters, ploc_csum = int(t.ploc_iterations), int(t.ploc_cluster_sum)
-            ploc_launches = int(t.kernel_launches)
+            build_launches = int(t.kernel_launches)
             tree_height = int(t.tree_height)
         # a short timed region gets few clock samples: keep building (untimed, the same build)
         # until the sampled window around it spans at least 150 ms
@@ -437,6 +462,18 @@ def run_ours(args):
                              "frac": round(136.0 * n / (med[5] / 1e3) / 1e9 / peak, 4)}}
     if algo == "ploc":
         roofline["ploc"] = {"iterations": ploc_iters, "cluster_sum": ploc_csum}
+    # every stage against the measured peak, in the problem's bytes and in the bytes this
+    # implementation moves
+    roofline["stages"] = {}
+    for k, ms in shares.items():
+        if ms <= 0.005:
+            continue
+        alg = stage_bytes_per_tri(k, algo, bits, rounds, csum)
+        imp = impl_stage_bytes_per_tri(k, algo, bits, rounds, csum)
+        roofline["stages"][k] = {"ms": round(ms, 4), "algorithmic_bytes_per_tri": round(alg, 2),
+                                 "frac_algorithmic": round(alg * n / (ms / 1e3) / 1e9 / peak, 4),
+                                 "implementation_bytes_per_tri": round(imp, 2),
+                                 "frac_implementation": round(imp * n / (ms / 1e3) / 1e9 / peak, 4)}
     stage_ms = {k: round(v, 4) for k, v in shares.items()}
 
     # --- tree quality: evaluator statistics on the GPU, 1920x1080 pinhole primary rays -----
@@ -571,8 +608,8 @@ def run_ours(args):
         "quality": quality,
         "roofline": roofline,
         "e2e": e2e,
-        # PLOC's loop runs on the device: the build reports its own launches
-        "gpu_launches": args.steps * (ploc_launches if algo == "ploc" and ploc_launches > 0
+        # PLOC's and LBVH+'s loops run on the device: those builds report their own launches
+        "gpu_launches": args.steps * (build_launches if algo in ("ploc", "lbvh_plus") and build_launches > 0
                                       else kernels_per_build(algo, bits, rounds, ploc_iters, tree_height)),
         "clocks": clk.summary(),
         "autotune": tuning,

@@ -48,6 +48,8 @@ struct bvh_ctx {
   bvh_timing last{};
   int last_algo = -1;
   uint32_t last_n = 0;     // triangles of the last single build (0 after a batched one)
+  int32_t last_bits = 30, last_rounds = 0;  // Morton bits and treelet passes of the last build
+  bool last_host_loops = false;
   bool have_timing = false;
   uint32_t* h_status = nullptr;  // pinned copy of the device status word
   cudaStream_t last_stream = nullptr;
@@ -208,6 +210,9 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
                              bvh_tree* out) {
   const uint32_t n = mesh->n;
   ctx->last_n = n;
+  ctx->last_bits = params->morton_bits;
+  ctx->last_rounds = params->treelet_rounds;
+  ctx->last_host_loops = params->reserved[1] == BVH_HOST_DRIVEN_LOOPS;
   apply_tuning(ctx, params->algo, n);
   ctx->have_timing = false;
   ctx->last = bvh_timing{};
@@ -236,7 +241,7 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   if (params->algo == BVH_ALGO_PLOC)  // iterations and live-cluster sum, read at bvh_sync
     cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.ploc, 20 * 4, cudaMemcpyDeviceToHost, st);
   if (params->algo == BVH_ALGO_LBVH_PLUS && params->treelet_rounds > 0 && n > 1)  // tree height, read at bvh_sync
-    cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.hist + kTlCtlWord, 2 * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(ctx->h_status + 4, ctx->ws.scratch + L.hist + kTlCtlWord, 3 * 4, cudaMemcpyDeviceToHost, st);
   cudaEventRecord(ctx->evs.ev[6], st);
   out->nodes = reinterpret_cast<const bvh_node*>(ctx->ws.nodes);
   out->indices = idx;
@@ -291,6 +296,17 @@ extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
                                                   : 7;
   } else if (ctx->last_algo == BVH_ALGO_LBVH_PLUS) {
     ctx->last.tree_height = (int32_t)ctx->h_status[5];
+    // LBVH kernels, then per treelet pass: heights, counts, offsets, grouping, the fallback
+    // check; heights 1 (growth, step) and 2 (growth, DP, step); then growth + DP + step per height
+    // of the loop (the graph runs at least one), and k_tl_narrow for the rest (the last pass's
+    // heights stand for every pass)
+    const uint32_t* c = ctx->h_status + 4;  // [0] too high, [1] largest height, [2] first height left
+    int32_t loop_h;
+    if (ctx->last_host_loops) loop_h = c[0] ? 0 : std::max(0, (int32_t)c[1] - 2);
+    else loop_h = c[0] ? 1 : std::max(1, (ctx->ws.tl_narrow ? (int32_t)c[2] : (int32_t)c[1] + 1) - 3);
+    const int32_t lbvh = 2 + 4 + (ctx->last_bits != 30 ? 2 : 0) + 2;
+    ctx->last.kernel_launches =
+        ctx->last_n > 1 ? lbvh + ctx->last_rounds * (5 + 5 + 3 * loop_h + (ctx->ws.tl_narrow ? 1 : 0)) : lbvh;
   }
   return check_status_word(ctx);
 }
@@ -760,7 +776,7 @@ extern "C" bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh,
       t.mg_bps = k;
       if (s == BVH_OK && k != best.mg_bps) s = trial(t, false);
     }
-    for (uint32_t g : {0u, 65536u, 150000u, 0xffffffffu}) {
+    for (uint32_t g : {0u, 65536u, 150000u, 300000u, 0xffffffffu}) {
       TuneEntry t = best;
       t.grid_max = g;
       if (s == BVH_OK && g != best.grid_max) s = trial(t, false);

@@ -198,6 +198,32 @@ __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Grid-wide barrier of a cooperative launch: arrivals count up in *bar, and the k-th barrier of
+// the kernel waits until k * gridDim.x blocks have arrived.  Bounded: past kSpinLimit polls the
+// block records kStatusGridTimeout and returns false (every other block then gives up at its
+// next wait).  The counter is zeroed before the launch.
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, uint32_t* status, uint32_t* s_ok,
+                                          uint32_t limit = kSpinLimit) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    uint32_t ok = 1, spins = 0;
+    while (ld_acquire(bar) < target) {
+      if (++spins > limit) {
+        atomicOr(status, kStatusGridTimeout);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
 __host__ __device__ inline uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 }  // namespace bvhgb

@@ -795,37 +795,12 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_ploc_tail(PlocBufs B, int r
 // iteration count and live-cluster sum).  It runs while the live clusters number more than the
 // tail hand-over (ctrl[12]) and at most kGridPerBlock per block.
 constexpr int kGridThreads = 1024;
-constexpr uint32_t kGridPerBlock = 2048;  // 2 clusters per thread
+constexpr uint32_t kGridPerBlock = 2048;
+constexpr int kGridPer = (int)kGridPerBlock / kGridThreads;  // consecutive clusters per thread
 constexpr int kGridMaxR = 128;
 constexpr uint32_t kGridWin = kGridPerBlock + 2 * kGridMaxR;
 constexpr uint32_t kGridMaxBlocks = 1024;
 static size_t grid_smem() { return (size_t)kGridWin * (2 * 16 + 4) + 64 * 8; }
-
-// Grid-wide barrier of a cooperative launch: arrivals count up in *bar, and the k-th barrier of
-// the kernel waits until k * gridDim.x blocks have arrived.  Bounded: past kSpinLimit polls the
-// block records kStatusGridTimeout and returns false (every other block then gives up at its
-// next wait).  The counter is zeroed before the launch (k_ploc_init).
-__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, uint32_t* status, uint32_t* s_ok,
-                                          uint32_t limit = kSpinLimit) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(bar, 1u);
-    uint32_t ok = 1, spins = 0;
-    while (ld_acquire(bar) < target) {
-      if (++spins > limit) {
-        atomicOr(status, kStatusGridTimeout);
-        ok = 0;
-        break;
-      }
-      __nanosleep(32);
-    }
-    __threadfence();
-    *s_ok = ok;
-  }
-  __syncthreads();
-  return *s_ok != 0;
-}
 
 // Exclusive block scan of one 64-bit value per thread (kGridThreads); *total gets the sum.
 __device__ __forceinline__ unsigned long long grid_block_scan(unsigned long long v, unsigned long long* s_w,
@@ -911,13 +886,15 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
       __stcg(B.nbr + x, bj);
     }
     if (!(ok = grid_sync(bar, ++nbar * G, B.status, &s_ok))) break;
-    // merge / survivor flags of this thread's clusters x0 + 2 tid + q (ascending)
-    bool m2[2] = {false, false}, v2[2] = {false, false};
-    int32_t nj[2] = {-1, -1};
+    // merge / survivor flags of this thread's clusters x0 + kGridPer tid + q (ascending)
+    bool m2[kGridPer], v2[kGridPer];
+    int32_t nj[kGridPer];
     uint32_t mk = 0, vk = 0;
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const uint32_t x = x0 + 2u * (uint32_t)tid + (uint32_t)q;
+    for (int q = 0; q < kGridPer; ++q) {
+      const uint32_t x = x0 + (uint32_t)kGridPer * (uint32_t)tid + (uint32_t)q;
+      m2[q] = v2[q] = false;
+      nj[q] = -1;
       if (x < x1) {
         const int32_t j = __ldcg(B.nbr + x);
         const int32_t back = (j >= 0 && (uint32_t)j < c) ? __ldcg(B.nbr + j) : -1;
@@ -945,8 +922,8 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
     uint32_t vpos = (uint32_t)offs_b + (uint32_t)before;
     const uint32_t M = (uint32_t)(grand_b >> 32), V = (uint32_t)grand_b;
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const uint32_t xi = x0 + 2u * (uint32_t)tid + (uint32_t)q;
+    for (int q = 0; q < kGridPer; ++q) {
+      const uint32_t xi = x0 + (uint32_t)kGridPer * (uint32_t)tid + (uint32_t)q;
       if (xi >= x1) continue;
       float4 a = s_lo[xi - w0], bb = s_hi[xi - w0];
       int32_t nid = s_id[xi - w0];

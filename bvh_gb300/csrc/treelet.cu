@@ -337,7 +337,8 @@ __device__ __forceinline__ void reg_grow(const Node* nodes, int32_t root, const 
 }
 
 // Areas of the subsets s < 2^nv with two or more leaves into this lane's column A (stride 32):
-// the box of s is (its leaves among 3..6) U (its leaves among 0..2).
+// the box of s is (its leaves among 3..6) U (its leaves among 0..2).  NVMAX: nv's bound.
+template <int NVMAX = kTlMax>
 __device__ __forceinline__ void reg_areas(const RegTreelet& T, int nv, float* A) {
   const uint32_t full = (1u << nv) - 1u;
   Box lo8[8];
@@ -353,7 +354,7 @@ __device__ __forceinline__ void reg_areas(const RegTreelet& T, int nv, float* A)
     Box bh = box_empty();
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      if ((hi >> j) & 1u) bh = box_union(bh, T.b[3 + j]);
+      if (3 + j < NVMAX && ((hi >> j) & 1u)) bh = box_union(bh, T.b[3 + j]);
 #pragma unroll
     for (int lo = 0; lo < 8; ++lo) {
       const uint32_t s = hi * 8u + (uint32_t)lo;
@@ -364,8 +365,9 @@ __device__ __forceinline__ void reg_areas(const RegTreelet& T, int nv, float* A)
 
 // Subset DP (:119-165) by one lane for up to nv leaves, straight-line code with the costs in
 // registers (treelet_dp_unrolled.cuh); best splits into this lane's column P.
+template <int NVMAX = kTlMax>
 __device__ __forceinline__ void reg_dp(int nv, const float* A, uint8_t* P) {
-  if (nv <= 4) dp_unrolled_4(A, P);
+  if (NVMAX <= 4 || nv <= 4) dp_unrolled_4(A, P);
   else if (nv == 5) dp_unrolled_5(A, P);
   else if (nv == 6) dp_unrolled_6(A, P);
   else dp_unrolled_7(A, P);
@@ -561,9 +563,16 @@ __global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ 
     __stcg(p + 1, box.hi);
     GrowTreelet T;
     reg_grow(nodes, x, box, ch, T);
+    const uint32_t q = k - b;
+    if (T.n == 2) {
+      // Two leaves (the root's children; both are BVH leaves): the DP's only split puts the
+      // second leaf left, so the rebuild swaps the children (box and parent links stay).
+      __stcg(reinterpret_cast<int2*>(&nodes[x].left), make_int2(T.id[1], T.id[0]));
+      desc[q] = 0u;  // nothing left for k_tl_dp
+      continue;
+    }
     int avail[kTlMax];
     const int na = T.n >= 2 ? reg_avail(nodes, x, T, avail) : 0;
-    const uint32_t q = k - b;
     desc[q] = (uint32_t)T.n | ((uint32_t)na << 8);
 #pragma unroll
     for (int i = 0; i < kTlMax; ++i) desc[(size_t)(1 + i) * stride + q] = (uint32_t)T.id[i];
@@ -572,11 +581,15 @@ __global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ 
   }
 }
 
+// NVMAX < kTlMax: a DP for treelets of at most NVMAX leaves (heights where no more fit: height 2
+// holds at most 4), compiled for fewer registers, so more warps share an SM.
+template <int NVMAX>
 __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, const uint32_t* __restrict__ off,
                                                       const uint32_t* __restrict__ ctl,
                                                       const uint32_t* __restrict__ desc, uint32_t stride) {
-  __shared__ float s_cost[(1 << kTlMax) * 32];
-  __shared__ uint8_t s_part[(1 << kTlMax) * 32];
+  // per-lane columns of 2^NVMAX costs and partitions (the narrow path below uses 768 words)
+  __shared__ float s_cost[std::max((1 << NVMAX) * 32, 1024)];
+  __shared__ uint8_t s_part[(1 << NVMAX) * 32];
   if (__ldcg(ctl) != 0u) return;
   const uint32_t h = __ldcg(ctl + 2);
   const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
@@ -631,13 +644,13 @@ __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, 
     const int na = (int)(w0 >> 8);
 #pragma unroll
     for (int i = 0; i < kTlMax; ++i) {
-      T.id[i] = i < T.n ? (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q) : 0;
-      T.b[i] = i < T.n ? ldcg_box(nodes, T.id[i]) : box_empty();
+      T.id[i] = i < NVMAX && i < T.n ? (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q) : 0;
+      T.b[i] = i < NVMAX && i < T.n ? ldcg_box(nodes, T.id[i]) : box_empty();
     }
     const int nv = (int)__reduce_max_sync(0xffffffffu, (uint32_t)T.n);
     if (nv < 2) continue;
-    reg_areas(T, nv, C);
-    reg_dp(nv, C, P);
+    reg_areas<NVMAX>(T, nv, C);
+    reg_dp<NVMAX>(nv, C, P);
     if (T.n >= 2) {
       int avail[kTlMax];
 #pragma unroll
@@ -647,14 +660,90 @@ __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, 
   }
 }
 
+// The narrow heights in one cooperative launch.  Once a height has few nodes, its two launches
+// (growth, DP) cost mostly their latency; k_tl_narrow runs the remaining heights, from the current
+// one (ctl[2]) to the largest (ctl[1]), with a grid barrier between heights (nodes of one height
+// have disjoint subtrees, a height needs all lower ones done).  Per node, one warp: lane 0 refits
+// the node and grows its treelet (as k_tl_grow), the warp runs the cooperative DP and lane 0
+// rebuilds (as k_tl_dp's narrow path).  Same work and result as the per-height kernels.
+constexpr int kNarrowThreads = 256;
+
+struct NarrowWarp {
+  LaneTreelet S;
+  float cost[1 << kTlMax];
+  float area[1 << kTlMax];
+  int32_t avail[kTlMax];
+  int32_t na;
+};
+
+__global__ void __launch_bounds__(kNarrowThreads) k_tl_narrow(Node* __restrict__ nodes, const uint32_t* __restrict__ list,
+                                                              const uint32_t* __restrict__ off, uint32_t* __restrict__ ctl,
+                                                              uint32_t* __restrict__ status) {
+  __shared__ NarrowWarp s_warp[kNarrowThreads / 32];
+  __shared__ uint32_t s_ok;
+  // every block reads the same words (nothing writes them in this kernel)
+  if (__ldcg(ctl) != 0u) return;  // too high: the fallback pass does the work
+  const uint32_t h0 = __ldcg(ctl + 2), h1 = __ldcg(ctl + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  NarrowWarp& W = s_warp[w];
+  const uint32_t gw = blockIdx.x * (kNarrowThreads / 32) + (uint32_t)w, nw = gridDim.x * (kNarrowThreads / 32);
+  uint32_t nbar = 0;
+  for (uint32_t h = h0; h <= h1; ++h) {
+    const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
+    for (uint32_t k = b + gw; k < e; k += nw) {
+      if (lane == 0) {
+        const int32_t x = (int32_t)__ldcg(list + k);
+        const int2 ch = ldcg_children(nodes, x);
+        const Box box = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
+        float4* p = reinterpret_cast<float4*>(nodes + x);
+        __stcg(p, box.lo);
+        __stcg(p + 1, box.hi);
+        GrowTreelet T;
+        reg_grow(nodes, x, box, ch, T);
+        W.S.n = T.n;
+#pragma unroll
+        for (int i = 0; i < kTlMax; ++i) W.S.act[i] = T.id[i];
+        W.na = T.n >= 2 ? reg_avail(nodes, x, T, W.avail) : 0;
+      }
+      __syncwarp();
+      const int n = W.S.n;
+      if (n >= 2) {  // uniform over the warp
+        if (lane < kTlMax) {
+          const Box bx = lane < n ? ldcg_box(nodes, W.S.act[lane]) : box_empty();
+          W.S.box[0][lane] = bx.lo.x; W.S.box[1][lane] = bx.lo.y; W.S.box[2][lane] = bx.lo.z;
+          W.S.box[3][lane] = bx.hi.x; W.S.box[4][lane] = bx.hi.y; W.S.box[5][lane] = bx.hi.z;
+        }
+        __syncwarp();
+        treelet_dp(W.S, W.cost, W.area);
+        if (lane == 0) {
+          RegTreelet T;
+          T.n = n;
+#pragma unroll
+          for (int i = 0; i < kTlMax; ++i) {
+            T.id[i] = W.S.act[i];
+            T.b[i] = leaf_box(W.S, i);
+          }
+          reg_build<1>(nodes, T, W.S.part, W.avail, W.na);
+        }
+      }
+      __syncwarp();
+    }
+    if (h < h1 && !grid_sync(ctl + 4, ++nbar * gridDim.x, status, &s_ok)) return;
+  }
+}
+
 // End of a height: the next one, and whether the loop goes on (the graph's WHILE condition;
-// the host-driven loop only advances the height).
+// the host-driven loop only advances the height).  The loop also stops at the first height of
+// at most `narrow` nodes (0: never), from which k_tl_narrow goes on.
 template <bool GRAPH>
-__global__ void k_tl_step(uint32_t* __restrict__ ctl, cudaGraphConditionalHandle handle) {
+__global__ void k_tl_step(uint32_t* __restrict__ ctl, const uint32_t* __restrict__ off, uint32_t narrow,
+                          cudaGraphConditionalHandle handle) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const uint32_t h = ctl[2] + 1;
   ctl[2] = h;
-  if constexpr (GRAPH) cudaGraphSetConditional(handle, (ctl[0] == 0u && h <= ctl[1]) ? 1u : 0u);
+  bool go = ctl[0] == 0u && h <= ctl[1];
+  if (go && narrow && off[h + 1] - off[h] <= narrow) go = false;
+  if constexpr (GRAPH) cudaGraphSetConditional(handle, go ? 1u : 0u);
 }
 
 // The climb-ordered pass as a fallback for trees higher than kTlMaxHeight: persistent warps
@@ -710,12 +799,14 @@ __global__ void __launch_bounds__(64) k_treelet_fallback(Node* __restrict__ node
   }
 }
 
-static int g_dp_grid[64] = {};  // resident blocks of k_tl_dp per device
+static int g_dp_grid[64] = {};      // resident blocks of k_tl_dp per device
+static int g_dp4_grid[64] = {};     // resident blocks of k_tl_dp<4> per device
+static int g_narrow_grid[64] = {};  // resident blocks of k_tl_narrow per device (-1: no cooperative launch)
 
 // The loop over heights as a graph: WHILE(cond) { grow; dp; step }.
 static cudaError_t make_height_graph(Node* nodes, const uint32_t* list, const uint32_t* off, uint32_t* ctl,
                                      uint32_t* desc, uint32_t stride, uint32_t grow_grid, uint32_t dp_grid,
-                                     cudaGraphExec_t* out) {
+                                     uint32_t narrow, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaGraphCreate(&g, 0);
   if (e != cudaSuccess) return e;
@@ -736,8 +827,8 @@ static cudaError_t make_height_graph(Node* nodes, const uint32_t* list, const ui
         cudaSuccess)
       break;
     k_tl_grow<<<grow_grid, kGrowThreads, 0, cs>>>(nodes, list, off, ctl, desc, stride);
-    k_tl_dp<<<dp_grid, kLvThreads, 0, cs>>>(nodes, off, ctl, desc, stride);
-    k_tl_step<true><<<1, 32, 0, cs>>>(ctl, handle);
+    k_tl_dp<kTlMax><<<dp_grid, kLvThreads, 0, cs>>>(nodes, off, ctl, desc, stride);
+    k_tl_step<true><<<1, 32, 0, cs>>>(ctl, off, narrow, handle);
     cudaGraph_t captured = nullptr;
     const cudaError_t e2 = cudaGetLastError();
     e = cudaStreamEndCapture(cs, &captured);
@@ -761,9 +852,22 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
   if (!g_dp_grid[dev]) {
     int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_dp, kLvThreads, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_dp<kTlMax>, kLvThreads, 0)) != cudaSuccess)
+      return e;
     g_dp_grid[dev] = std::max(1, per_sm * sms);
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_dp<4>, kLvThreads, 0)) != cudaSuccess) return e;
+    g_dp4_grid[dev] = std::max(1, per_sm * sms);
   }
+  if (!g_narrow_grid[dev]) {
+    int coop = 0, per_sm = 0;
+    if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_narrow, kNarrowThreads, 0)) != cudaSuccess)
+      return e;
+    g_narrow_grid[dev] = coop && per_sm > 0 ? per_sm * sms : -1;
+  }
+  // heights of at most `narrow` nodes (two per warp of the cooperative grid) run in k_tl_narrow
+  const uint32_t narrow =
+      !host_loop && g_narrow_grid[dev] > 0 ? 2u * (uint32_t)g_narrow_grid[dev] * (kNarrowThreads / 32) : 0u;
   // scratch: heights in the delta bytes (emission is done with them), the id list in the idle
   // value buffer, descriptors in the triangle boxes (32 B per triangle; a height has at most
   // n/2 nodes), counters / offsets / control words in the sort histogram words
@@ -776,7 +880,7 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   uint32_t* cursor = off + 264;              // 256
   uint32_t* ctl = cursor + 256;              // [0] too high, [1] largest height, [2] current height
   static_assert(kTlCtlWord == 256 + 264 + 256, "control words of the treelet pass");
-  static_assert(kTlCtlWord + 3 <= (size_t)kMaxPasses * 256, "treelet words fit the histogram area");
+  static_assert(kTlCtlWord + 8 <= (size_t)kMaxPasses * 256, "treelet words fit the histogram area");
   const uint32_t* epoch = ws.scratch + L.epoch;
   const uint32_t grow_grid = std::max<uint32_t>(1, std::min<uint32_t>(div_up(stride, kGrowThreads), sms * 16));
   if (host_loop && !ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
@@ -785,7 +889,7 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
   if (!same) {
     if (ws.tl_exec) cudaGraphExecDestroy(ws.tl_exec);
     ws.tl_exec = nullptr;
-    if ((e = make_height_graph(ws.nodes, list, off, ctl, desc, stride, grow_grid, (uint32_t)g_dp_grid[dev],
+    if ((e = make_height_graph(ws.nodes, list, off, ctl, desc, stride, grow_grid, (uint32_t)g_dp_grid[dev], narrow,
                                &ws.tl_exec)) != cudaSuccess)
       return e;
     ws.tl_key_n = n;
@@ -794,26 +898,48 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
     ws.tl_key_desc = desc;
     ws.tl_key_ctl = ctl;
   }
+  ws.tl_narrow = narrow != 0;
   for (int r = 0; r < rounds && r + 1 < 0x20; ++r) {
     if ((e = cudaMemsetAsync(cnt, 0, 256 * 4, st)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(ctl, 0, 4 * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ctl, 0, 8 * 4, st)) != cudaSuccess) return e;  // [4]: k_tl_narrow's barrier
     k_tl_heights<<<div_up(n, 256), 256, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, hgt, ctl);
     k_tl_count<<<std::max<uint32_t>(1, std::min<uint32_t>(div_up(n - 1, 256), sms * 8)), 256, 0, st>>>(hgt, n - 1, cnt);
     k_tl_offsets<<<1, 256, 0, st>>>(cnt, n - 1, off, cursor, ctl);
     k_tl_scatter<<<div_up(n - 1, 256), 256, 0, st>>>(hgt, n - 1, cursor, list);
+    // heights 1 and 2 first: every height-1 treelet has two leaves and is finished by the growth
+    // kernel; height 2 holds at most 4 leaves and takes the smaller DP
+    k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
+    k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
+    k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
+    k_tl_dp<4><<<g_dp4_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+    k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
     if (host_loop) {
       // read the largest height (and the too-high flag) once, then one grow + dp per height
       if ((e = cudaMemcpyAsync(ws.ploc_host, ctl, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
           (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return e;
       const uint32_t maxh = ws.ploc_host[0] ? 0u : ws.ploc_host[1];
-      for (uint32_t h = 1; h <= maxh; ++h) {
+      for (uint32_t h = 3; h <= maxh; ++h) {
         k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
-        k_tl_dp<<<g_dp_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
-        k_tl_step<false><<<1, 32, 0, st>>>(ctl, cudaGraphConditionalHandle{});
+        k_tl_dp<kTlMax><<<g_dp_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+        k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
       }
-    } else if ((e = cudaGraphLaunch(ws.tl_exec, st)) != cudaSuccess) {
-      return e;
+    } else {
+      if ((e = cudaGraphLaunch(ws.tl_exec, st)) != cudaSuccess) return e;
+      if (narrow) {  // the remaining heights, from where the graph's loop stopped
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((uint32_t)g_narrow_grid[dev]);
+        cfg.blockDim = dim3(kNarrowThreads);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        if ((e = cudaLaunchKernelEx(&cfg, k_tl_narrow, ws.nodes, (const uint32_t*)list, (const uint32_t*)off, ctl,
+                                    ws.scratch + L.status)) != cudaSuccess)
+          return e;
+      }
     }
     k_treelet_fallback<<<sms * 8, 64, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, ctl);
   }

@@ -100,9 +100,11 @@ typedef struct bvh_timing {
   int32_t ploc_iterations;
   int32_t tree_height;       /* LBVH+: tree height in the last treelet pass (one kernel pair per level) */
   uint64_t ploc_cluster_sum; /* sum of live clusters over PLOC iterations */
-  int32_t kernel_launches;   /* PLOC: this library's kernels the build launched (its loop runs on the
-                                device: 4 per iteration launched one kernel per phase, 1 each for the
-                                middle-iterations and tail kernels); 0 for the other algorithms */
+  int32_t kernel_launches;   /* PLOC and LBVH+: this library's kernels the build launched (their loops
+                                run on the device: PLOC 4 per iteration launched one kernel per
+                                phase and 1 each for the middle-iterations and tail kernels; LBVH+ 3
+                                per tree height launched per phase and 1 for the narrow heights);
+                                0 for LBVH */
   int32_t reserved;
 } bvh_timing;
 

@@ -39,3 +39,17 @@ def test_treelet_passes_per_workload():
     assert bench.treelet_rounds("c1_lbvhplus") == 1
     assert bench.treelet_rounds("c1_lbvh63") == 0
     assert bench.treelet_rounds("c1_ploc25") == 0
+
+
+def test_implementation_bytes_per_stage():
+    """The bytes this implementation moves per stage (beside the problem's B(K) split): the sort
+    moves 4 passes of 32-bit pairs, not the 8 passes of 64-bit keys that B(63) counts."""
+    assert bench.impl_stage_bytes_per_tri("onesweep_sort", "lbvh", 30) == 60
+    assert bench.impl_stage_bytes_per_tri("onesweep_sort", "lbvh", 63) == 73
+    assert bench.stage_bytes_per_tri("onesweep_sort", "lbvh", 63) > bench.impl_stage_bytes_per_tri("onesweep_sort", "lbvh", 63)
+    total63 = sum(bench.impl_stage_bytes_per_tri(s, "lbvh", 63)
+                  for s in ("scene_bounds", "morton_boxes_hist", "onesweep_sort", "emit_refit"))
+    assert total63 == 36 + 76 + 73 + 133
+    # stages the accounting does not split fall back to the algorithmic figure
+    assert bench.impl_stage_bytes_per_tri("treelet_or_ploc_loop", "ploc", 30, 0, 9.84) == \
+        bench.stage_bytes_per_tri("treelet_or_ploc_loop", "ploc", 30, 0, 9.84)
