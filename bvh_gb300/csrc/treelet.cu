@@ -561,9 +561,14 @@ __global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ 
     float4* p = reinterpret_cast<float4*>(nodes + x);
     __stcg(p, box.lo);
     __stcg(p + 1, box.hi);
+    const uint32_t q = k - b;
+    if (h == 1) {  // both children are BVH leaves: the two-leaf treelet below, without growing it
+      __stcg(reinterpret_cast<int2*>(&nodes[x].left), make_int2(ch.y, ch.x));
+      desc[q] = 0u;
+      continue;
+    }
     GrowTreelet T;
     reg_grow(nodes, x, box, ch, T);
-    const uint32_t q = k - b;
     if (T.n == 2) {
       // Two leaves (the root's children; both are BVH leaves): the DP's only split puts the
       // second leaf left, so the rebuild swaps the children (box and parent links stay).
