@@ -798,9 +798,12 @@ constexpr int kGridThreads = 1024;
 constexpr uint32_t kGridPerBlock = 2048;
 constexpr int kGridPer = (int)kGridPerBlock / kGridThreads;  // consecutive clusters per thread
 constexpr int kGridMaxR = 128;
-constexpr uint32_t kGridWin = kGridPerBlock + 2 * kGridMaxR;
+// the window: the chunk and 2r clusters either side (the neighbours of the chunk and of r
+// clusters either side of it, so the flag count needs no other block's neighbours)
+constexpr uint32_t kGridWin = kGridPerBlock + 4 * kGridMaxR;
+constexpr uint32_t kGridNbr = kGridPerBlock + 2 * kGridMaxR;
 constexpr uint32_t kGridMaxBlocks = 1024;
-static size_t grid_smem() { return (size_t)kGridWin * (2 * 16 + 4) + 64 * 8; }
+static size_t grid_smem() { return (size_t)kGridWin * (2 * 16 + 4) + (size_t)kGridNbr * 4 + 64 * 8; }
 
 // Exclusive block scan of one 64-bit value per thread (kGridThreads); *total gets the sum.
 __device__ __forceinline__ unsigned long long grid_block_scan(unsigned long long v, unsigned long long* s_w,
@@ -835,7 +838,8 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
   float4* s_lo = gsm;
   float4* s_hi = gsm + kGridWin;
   int32_t* s_id = reinterpret_cast<int32_t*>(gsm + 2 * kGridWin);
-  unsigned long long* s_w = reinterpret_cast<unsigned long long*>(s_id + kGridWin);
+  int32_t* s_nbr = s_id + kGridWin;  // neighbours of [h0, h1)
+  unsigned long long* s_w = reinterpret_cast<unsigned long long*>(s_nbr + kGridNbr);
   __shared__ uint32_t s_ok;
   const uint32_t G = gridDim.x, b = blockIdx.x;
   const int tid = threadIdx.x;
@@ -861,7 +865,8 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
     int32_t* idout = par ? B.cid[0] : B.cid[1];
     const uint32_t ch = div_up(c, G);
     const uint32_t x0 = min(c, b * ch), x1 = min(c, x0 + ch);
-    const uint32_t w0 = x0 > (uint32_t)r ? x0 - (uint32_t)r : 0u, w1 = min(c, x1 + (uint32_t)r);
+    const uint32_t h0 = x0 > (uint32_t)r ? x0 - (uint32_t)r : 0u, h1 = min(c, x1 + (uint32_t)r);
+    const uint32_t w0 = h0 > (uint32_t)r ? h0 - (uint32_t)r : 0u, w1 = min(c, h1 + (uint32_t)r);
     for (uint32_t x = w0 + tid; x < w1; x += kGridThreads) {
       const float4* bp = reinterpret_cast<const float4*>(cin + x);
       s_lo[x - w0] = __ldcg(bp);
@@ -869,8 +874,9 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
       s_id[x - w0] = __ldcg(idin + x);
     }
     __syncthreads();
-    // neighbours of the chunk: ascending j with a strict < keeps the smallest j of equal areas
-    for (uint32_t x = x0 + tid; x < x1; x += kGridThreads) {
+    // neighbours of the chunk and r clusters either side: ascending j with a strict < keeps the
+    // smallest j of equal areas
+    for (uint32_t x = h0 + tid; x < h1; x += kGridThreads) {
       const float4 xa = s_lo[x - w0], xb = s_hi[x - w0];
       const uint32_t j0 = x > (uint32_t)r ? x - (uint32_t)r : 0u, j1 = min(c - 1, x + (uint32_t)r);
       float best = kInf;
@@ -883,10 +889,11 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
           bj = (int32_t)j;
         }
       }
-      __stcg(B.nbr + x, bj);
+      s_nbr[x - h0] = bj;
     }
-    if (!(ok = grid_sync(bar, ++nbar * G, B.status, &s_ok))) break;
-    // merge / survivor flags of this thread's clusters x0 + kGridPer tid + q (ascending)
+    __syncthreads();
+    // merge / survivor flags of this thread's clusters x0 + kGridPer tid + q (ascending); a
+    // neighbour j lies within r of x, so both j and its neighbour are in s_nbr
     bool m2[kGridPer], v2[kGridPer];
     int32_t nj[kGridPer];
     uint32_t mk = 0, vk = 0;
@@ -896,8 +903,8 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_ploc_grid(PlocBufs B, int r
       m2[q] = v2[q] = false;
       nj[q] = -1;
       if (x < x1) {
-        const int32_t j = __ldcg(B.nbr + x);
-        const int32_t back = (j >= 0 && (uint32_t)j < c) ? __ldcg(B.nbr + j) : -1;
+        const int32_t j = s_nbr[x - h0];
+        const int32_t back = j >= 0 ? s_nbr[(uint32_t)j - h0] : -1;
         const bool mutual = j >= 0 && back == (int32_t)x;
         m2[q] = mutual && (int32_t)x < j;
         v2[q] = !(mutual && j < (int32_t)x);
