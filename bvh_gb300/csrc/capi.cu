@@ -297,16 +297,16 @@ extern "C" bvh_status bvh_sync(bvh_ctx* ctx) {
   } else if (ctx->last_algo == BVH_ALGO_LBVH_PLUS) {
     ctx->last.tree_height = (int32_t)ctx->h_status[5];
     // LBVH kernels, then per treelet pass: heights, counts, offsets, grouping, the fallback
-    // check; heights 1 (growth, step) and 2 (growth, DP, step); then growth + DP + step per height
-    // of the loop (the graph runs at least one), and k_tl_narrow for the rest (the last pass's
-    // heights stand for every pass)
+    // check; heights 1 (growth, step), 2 (growth, DP, step) and 3 (growth, four DPs by size
+    // class, step); then growth + DP + step per height of the loop (the graph runs at least
+    // one), and k_tl_narrow for the rest (the last pass's heights stand for every pass)
     const uint32_t* c = ctx->h_status + 4;  // [0] too high, [1] largest height, [2] first height left
     int32_t loop_h;
-    if (ctx->last_host_loops) loop_h = c[0] ? 0 : std::max(0, (int32_t)c[1] - 2);
-    else loop_h = c[0] ? 1 : std::max(1, (ctx->ws.tl_narrow ? (int32_t)c[2] : (int32_t)c[1] + 1) - 3);
+    if (ctx->last_host_loops) loop_h = c[0] ? 0 : std::max(0, (int32_t)c[1] - 3);
+    else loop_h = c[0] ? 1 : std::max(1, (ctx->ws.tl_narrow ? (int32_t)c[2] : (int32_t)c[1] + 1) - 4);
     const int32_t lbvh = 2 + 4 + (ctx->last_bits != 30 ? 2 : 0) + 2;
     ctx->last.kernel_launches =
-        ctx->last_n > 1 ? lbvh + ctx->last_rounds * (5 + 5 + 3 * loop_h + (ctx->ws.tl_narrow ? 1 : 0)) : lbvh;
+        ctx->last_n > 1 ? lbvh + ctx->last_rounds * (5 + 11 + 3 * loop_h + (ctx->ws.tl_narrow ? 1 : 0)) : lbvh;
   }
   return check_status_word(ctx);
 }

@@ -368,8 +368,8 @@ __device__ __forceinline__ void reg_areas(const RegTreelet& T, int nv, float* A)
 template <int NVMAX = kTlMax>
 __device__ __forceinline__ void reg_dp(int nv, const float* A, uint8_t* P) {
   if (NVMAX <= 4 || nv <= 4) dp_unrolled_4(A, P);
-  else if (nv == 5) dp_unrolled_5(A, P);
-  else if (nv == 6) dp_unrolled_6(A, P);
+  else if (NVMAX <= 5 || nv == 5) dp_unrolled_5(A, P);
+  else if (NVMAX <= 6 || nv == 6) dp_unrolled_6(A, P);
   else dp_unrolled_7(A, P);
 }
 
@@ -586,6 +586,34 @@ __global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ 
   }
 }
 
+// One lane's treelet q of the current height (act: a real one): leaf ids and boxes from its
+// descriptor and the nodes, subset areas and the DP in this lane's shared-memory columns C and
+// P (stride 32), then the rebuild.  The warp runs the DP variant of its largest treelet, at most
+// NVMAX leaves.  Called by all 32 lanes together.
+template <int NVMAX>
+__device__ __forceinline__ void lane_dp(Node* nodes, const uint32_t* desc, uint32_t stride, uint32_t q, bool act,
+                                        float* C, uint8_t* P) {
+  const uint32_t w0 = act ? __ldcg(desc + q) : 0u;
+  RegTreelet T;
+  T.n = (int)(w0 & 255u);
+  const int na = (int)(w0 >> 8);
+#pragma unroll
+  for (int i = 0; i < kTlMax; ++i) {
+    T.id[i] = i < NVMAX && i < T.n ? (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q) : 0;
+    T.b[i] = i < NVMAX && i < T.n ? ldcg_box(nodes, T.id[i]) : box_empty();
+  }
+  const int nv = (int)__reduce_max_sync(0xffffffffu, (uint32_t)T.n);
+  if (nv < 2) return;
+  reg_areas<NVMAX>(T, nv, C);
+  reg_dp<NVMAX>(nv, C, P);
+  if (T.n >= 2) {
+    int avail[kTlMax];
+#pragma unroll
+    for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
+    reg_build<32>(nodes, T, P, avail, na);
+  }
+}
+
 // NVMAX < kTlMax: a DP for treelets of at most NVMAX leaves (heights where no more fit: height 2
 // holds at most 4), compiled for fewer registers, so more warps share an SM.
 template <int NVMAX>
@@ -641,27 +669,47 @@ __global__ void __launch_bounds__(kLvThreads) k_tl_dp(Node* __restrict__ nodes, 
   // warp-uniform loop: the warp runs the DP variant of its largest treelet
   for (uint32_t kb = b + blockIdx.x * kLvThreads; kb < e; kb += gridDim.x * kLvThreads) {
     const uint32_t k = kb + lane;
-    const bool act = k < e;
-    const uint32_t q = k - b;
-    const uint32_t w0 = act ? __ldcg(desc + q) : 0u;
-    RegTreelet T;
-    T.n = (int)(w0 & 255u);
-    const int na = (int)(w0 >> 8);
-#pragma unroll
-    for (int i = 0; i < kTlMax; ++i) {
-      T.id[i] = i < NVMAX && i < T.n ? (int32_t)__ldcg(desc + (size_t)(1 + i) * stride + q) : 0;
-      T.b[i] = i < NVMAX && i < T.n ? ldcg_box(nodes, T.id[i]) : box_empty();
+    lane_dp<NVMAX>(nodes, desc, stride, k - b, k < e, C, P);
+  }
+}
+
+// A height where treelet sizes are mixed (height 3: most treelets have 4 or 5 leaves, few 7):
+// one kernel per size class, NV = 4 (3 or 4 leaves), 5, 6, 7, each running only the
+// height's treelets of its class, so a warp runs the DP its own treelets need.  Each warp scans
+// R rounds of 32 nodes, packs those of its class into a shared list (ballots) and runs them 32
+// at a time; R shrinks with the height's node count so that every block gets a chunk.
+template <int NV>
+__global__ void __launch_bounds__(kLvThreads) k_tl_dpc(Node* __restrict__ nodes, const uint32_t* __restrict__ off,
+                                                       const uint32_t* __restrict__ ctl,
+                                                       const uint32_t* __restrict__ desc, uint32_t stride) {
+  constexpr int R = 8;
+  __shared__ float s_cost[(1 << NV) * 32];
+  __shared__ uint8_t s_part[(1 << NV) * 32];
+  __shared__ uint32_t s_list[32 * R];
+  if (__ldcg(ctl) != 0u) return;
+  const uint32_t h = __ldcg(ctl + 2);
+  const uint32_t b = __ldcg(off + h), e = __ldcg(off + h + 1);
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  float* C = s_cost + lane;
+  uint8_t* P = s_part + lane;
+  const uint32_t rounds = max(1u, min((uint32_t)R, div_up(e - b, 32u * gridDim.x)));
+  for (uint32_t chunk = b + blockIdx.x * (32u * rounds); chunk < e; chunk += gridDim.x * (32u * rounds)) {
+    uint32_t cnt = 0;
+    for (uint32_t r = 0; r < rounds; ++r) {
+      const uint32_t k = chunk + r * 32u + (uint32_t)lane;
+      const int n = k < e ? (int)(__ldcg(desc + (k - b)) & 255u) : 0;
+      const bool match = n >= 2 && (n <= 4 ? 4 : n) == NV;
+      const uint32_t bal = __ballot_sync(0xffffffffu, match);
+      if (match) s_list[cnt + __popc(bal & lt)] = k - b;
+      cnt += (uint32_t)__popc(bal);
     }
-    const int nv = (int)__reduce_max_sync(0xffffffffu, (uint32_t)T.n);
-    if (nv < 2) continue;
-    reg_areas<NVMAX>(T, nv, C);
-    reg_dp<NVMAX>(nv, C, P);
-    if (T.n >= 2) {
-      int avail[kTlMax];
-#pragma unroll
-      for (int i = 0; i < kTlMax - 1; ++i) avail[i] = (int)__ldcg(desc + (size_t)(8 + i) * stride + q);
-      reg_build<32>(nodes, T, P, avail, na);
+    __syncwarp();
+    for (uint32_t i = 0; i < cnt; i += 32) {
+      const bool act = i + (uint32_t)lane < cnt;
+      lane_dp<NV>(nodes, desc, stride, act ? s_list[i + lane] : 0u, act, C, P);
     }
+    __syncwarp();  // the list is refilled by the next chunk
   }
 }
 
@@ -806,6 +854,7 @@ __global__ void __launch_bounds__(64) k_treelet_fallback(Node* __restrict__ node
 
 static int g_dp_grid[64] = {};      // resident blocks of k_tl_dp per device
 static int g_dp4_grid[64] = {};     // resident blocks of k_tl_dp<4> per device
+static int g_dpc_grid[64][4] = {};  // resident blocks of k_tl_dpc<4..7> per device
 static int g_narrow_grid[64] = {};  // resident blocks of k_tl_narrow per device (-1: no cooperative launch)
 
 // The loop over heights as a graph: WHILE(cond) { grow; dp; step }.
@@ -862,6 +911,12 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
     g_dp_grid[dev] = std::max(1, per_sm * sms);
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tl_dp<4>, kLvThreads, 0)) != cudaSuccess) return e;
     g_dp4_grid[dev] = std::max(1, per_sm * sms);
+    const void* dpc[4] = {reinterpret_cast<const void*>(k_tl_dpc<4>), reinterpret_cast<const void*>(k_tl_dpc<5>),
+                          reinterpret_cast<const void*>(k_tl_dpc<6>), reinterpret_cast<const void*>(k_tl_dpc<7>)};
+    for (int c = 0; c < 4; ++c) {
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dpc[c], kLvThreads, 0)) != cudaSuccess) return e;
+      g_dpc_grid[dev][c] = std::max(1, per_sm * sms);
+    }
   }
   if (!g_narrow_grid[dev]) {
     int coop = 0, per_sm = 0;
@@ -911,12 +966,19 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
     k_tl_count<<<std::max<uint32_t>(1, std::min<uint32_t>(div_up(n - 1, 256), sms * 8)), 256, 0, st>>>(hgt, n - 1, cnt);
     k_tl_offsets<<<1, 256, 0, st>>>(cnt, n - 1, off, cursor, ctl);
     k_tl_scatter<<<div_up(n - 1, 256), 256, 0, st>>>(hgt, n - 1, cursor, list);
-    // heights 1 and 2 first: every height-1 treelet has two leaves and is finished by the growth
-    // kernel; height 2 holds at most 4 leaves and takes the smaller DP
+    // heights 1 to 3 first: every height-1 treelet has two leaves and is finished by the growth
+    // kernel; height 2 holds at most 4 leaves and takes the smaller DP; height 3 mixes treelet
+    // sizes (mostly 4 and 5 leaves, few 7) and runs one DP per size class
     k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
     k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
     k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
     k_tl_dp<4><<<g_dp4_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+    k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
+    k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
+    k_tl_dpc<4><<<g_dpc_grid[dev][0], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+    k_tl_dpc<5><<<g_dpc_grid[dev][1], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+    k_tl_dpc<6><<<g_dpc_grid[dev][2], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+    k_tl_dpc<7><<<g_dpc_grid[dev][3], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
     k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
     if (host_loop) {
       // read the largest height (and the too-high flag) once, then one grow + dp per height
@@ -924,7 +986,7 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
           (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return e;
       const uint32_t maxh = ws.ploc_host[0] ? 0u : ws.ploc_host[1];
-      for (uint32_t h = 3; h <= maxh; ++h) {
+      for (uint32_t h = 4; h <= maxh; ++h) {
         k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
         k_tl_dp<kTlMax><<<g_dp_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
         k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
