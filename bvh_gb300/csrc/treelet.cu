@@ -336,6 +336,44 @@ __device__ __forceinline__ void reg_grow(const Node* nodes, int32_t root, const 
   T.n = cnt;
 }
 
+// reg_grow after its first step, the root's expansion, whose loads the caller has made: leaves
+// (left, right) with their boxes and children, then the same steps from there.
+__device__ __forceinline__ void reg_grow_expanded(const Node* nodes, int32_t root, int2 rootch, const Box& lb,
+                                                  const Box& rb, int2 lc, int2 rc, GrowTreelet& T) {
+  reg_set(T, 0, rootch.x, lb, lc);
+  reg_set(T, 1, rootch.y, rb, rc);
+  T.en[0] = root;
+  T.el[0] = rootch.x;
+  T.er[0] = rootch.y;
+  int cnt = 2;
+#pragma unroll
+  for (int step = 1; step < kTlMax - 1; ++step) {
+    int best = -1;
+    float max_area = -1.0f;
+    int32_t bl = 0, br = 0, bn = 0;
+#pragma unroll
+    for (int i = 0; i < kTlMax; ++i) {
+      if (i < cnt && !((uint32_t)T.cl[i] & kLeafBit) && T.area[i] > max_area) {
+        max_area = T.area[i];
+        best = i;
+        bl = T.cl[i];
+        br = T.cr[i];
+        bn = T.id[i];
+      }
+    }
+    if (best < 0) break;
+    T.en[step] = bn;
+    T.el[step] = bl;
+    T.er[step] = br;
+    const Box lb2 = ldcg_box(nodes, bl), rb2 = ldcg_box(nodes, br);
+    const int2 lc2 = ldcg_children(nodes, bl), rc2 = ldcg_children(nodes, br);
+    reg_set(T, best, bl, lb2, lc2);
+    reg_set(T, cnt, br, rb2, rc2);
+    ++cnt;
+  }
+  T.n = cnt;
+}
+
 // Areas of the subsets s < 2^nv with two or more leaves into this lane's column A (stride 32):
 // the box of s is (its leaves among 3..6) U (its leaves among 0..2).  NVMAX: nv's bound.
 template <int NVMAX = kTlMax>
@@ -557,18 +595,25 @@ __global__ void __launch_bounds__(kGrowThreads, 8) k_tl_grow(Node* __restrict__ 
   for (uint32_t k = b + blockIdx.x * blockDim.x + threadIdx.x; k < e; k += gridDim.x * blockDim.x) {
     const int32_t x = (int32_t)__ldcg(list + k);
     const int2 ch = ldcg_children(nodes, x);
-    const Box box = box_union(ldcg_box(nodes, ch.x), ldcg_box(nodes, ch.y));
+    // the children's boxes (the refit) and their own children (the root's expansion) together
+    const Box lb = ldcg_box(nodes, ch.x), rb = ldcg_box(nodes, ch.y);
+    const int2 lc = h == 1 ? make_int2(0, 0) : ldcg_children(nodes, ch.x);
+    const int2 rc = h == 1 ? make_int2(0, 0) : ldcg_children(nodes, ch.y);
+    const Box box = box_union(lb, rb);
     float4* p = reinterpret_cast<float4*>(nodes + x);
     __stcg(p, box.lo);
     __stcg(p + 1, box.hi);
     const uint32_t q = k - b;
+    // growth expands the root first, unless its area is not above -1 (NaN): then n = 1
+    const bool expand = box_area(box) > -1.0f;
     if (h == 1) {  // both children are BVH leaves: the two-leaf treelet below, without growing it
-      __stcg(reinterpret_cast<int2*>(&nodes[x].left), make_int2(ch.y, ch.x));
+      if (expand) __stcg(reinterpret_cast<int2*>(&nodes[x].left), make_int2(ch.y, ch.x));
       desc[q] = 0u;
       continue;
     }
     GrowTreelet T;
-    reg_grow(nodes, x, box, ch, T);
+    if (expand) reg_grow_expanded(nodes, x, ch, lb, rb, lc, rc, T);
+    else reg_grow(nodes, x, box, ch, T);
     if (T.n == 2) {
       // Two leaves (the root's children; both are BVH leaves): the DP's only split puts the
       // second leaf left, so the rebuild swaps the children (box and parent links stay).

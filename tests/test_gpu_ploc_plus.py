@@ -109,3 +109,22 @@ def test_lbvh_plus_bit_exact_vs_reference_kernels(ctx, gpu, name):
     nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH_PLUS, morton_bits=60, treelet_rounds=1))
     assert np.array_equal(idx, ri)
     assert O.node_fields_equal(nodes, rn)
+
+
+@pytest.mark.parametrize("rounds", [1, 3])
+def test_lbvh_plus_with_nan_triangles_equals_oracle(ctx, gpu, oracle_lib, rounds):
+    """Treelets whose root box has a NaN area are not grown (growth expands only areas above -1),
+    so those subtrees keep their shape; the rest are restructured as usual.  One triangle in 50
+    carries a NaN coordinate, so NaN boxes appear at every height, height 1 included."""
+    O = oracle_lib
+    m = meshgen.clustered(60_000, seed=91)
+    arrs = [np.array(a, copy=True) for a in m.arrays()]
+    rng = np.random.default_rng(5)
+    bad = rng.choice(m.size(), m.size() // 50, replace=False)
+    for k, idx in enumerate(np.array_split(bad, 9)):
+        arrs[k][idx] = np.nan
+    mesh = type(m)(*arrs)
+    nodes, idx, _, _ = build(ctx, gpu, mesh, ctx.params(C.ALGO_LBVH_PLUS, morton_bits=60, treelet_rounds=rounds))
+    onodes, oidx = O.lbvh_plus(mesh.arrays(), 60, rounds)
+    assert np.array_equal(idx, oidx)
+    assert O.node_fields_equal(nodes, onodes)
