@@ -72,6 +72,7 @@ class Batch(ctypes.Structure):
 
 BATCH_USE_GRAPH = 1
 HOST_DRIVEN_LOOPS = 1  # bvh_params.reserved[1]: PLOC / LBVH+ loops driven from the host
+NO_COOPERATIVE = 1  # bvh_params.reserved[2]: no cooperative kernels (their host-driven fallbacks)
 SERVE_BATCHED = 1  # bvh_serve_config.reserved[0]: batched ticks
 
 

@@ -87,10 +87,12 @@ class Context:
 
     def params(self, algo: int, morton_bits: Optional[int] = None, treelet_rounds: Optional[int] = None,
                ploc_radius: Optional[int] = None, max_iterations: Optional[int] = None,
-               host_loops: bool = False) -> C.Params:
+               host_loops: bool = False, no_cooperative: bool = False) -> C.Params:
         p = self.lib.bvh_default_params(algo)
         if host_loops:
             p.reserved[1] = C.HOST_DRIVEN_LOOPS
+        if no_cooperative:
+            p.reserved[2] = C.NO_COOPERATIVE
         if morton_bits is not None:
             p.morton_bits = morton_bits
         if treelet_rounds is not None:

@@ -213,6 +213,7 @@ static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_p
   ctx->last_bits = params->morton_bits;
   ctx->last_rounds = params->treelet_rounds;
   ctx->last_host_loops = params->reserved[1] == BVH_HOST_DRIVEN_LOOPS;
+  ctx->ws.no_cooperative = params->reserved[2] == BVH_NO_COOPERATIVE;
   apply_tuning(ctx, params->algo, n);
   ctx->have_timing = false;
   ctx->last = bvh_timing{};

@@ -44,6 +44,7 @@ struct Workspace {
   const void* tl_key_desc = nullptr;
   const void* tl_key_ctl = nullptr;
   bool tl_narrow = false;               // the last treelet pass launched k_tl_narrow
+  bool no_cooperative = false;          // run no cooperative kernel (their host-driven fallbacks)
   uint32_t ploc_key_n = 0;
   int ploc_key_r = 0;
   const void* ploc_key_nodes = nullptr;

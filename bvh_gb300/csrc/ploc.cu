@@ -1311,7 +1311,28 @@ cudaError_t ploc_build(Workspace& ws, const MeshPtrs& m, uint32_t n, int radius,
       attr[0].val.cooperative = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      if ((e = cudaLaunchKernelEx(&cfg, k_ploc_grid, B, radius)) != cudaSuccess) return e;
+      e = ws.no_cooperative ? cudaErrorNotSupported : cudaLaunchKernelEx(&cfg, k_ploc_grid, B, radius);
+      if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        // no co-resident grid (a client limited to part of the GPU, or asked for): the same
+        // iterations as one launch per kernel each, driven from the host, down to the tail
+        // hand-over; the loop above stopped at grid_at live clusters or for good
+        (void)cudaGetLastError();
+        if (!ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(B.ctrl + 14, 0, 4, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(ws.ploc_host, B.ctrl, 8 * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+          return e;
+        bool go = ws.ploc_host[0] > std::max<uint32_t>(tail, 1u) && ws.ploc_host[6] < ws.ploc_host[7];
+        while (go) {
+          enqueue_iteration<false, false>(B, none, n, radius, sh, st, cudaGraphConditionalHandle{});
+          if ((e = cudaMemcpyAsync(ws.ploc_host, B.ctrl + 10, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+              (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return e;
+          go = *ws.ploc_host != 0;
+        }
+      } else if (e != cudaSuccess) {
+        return e;
+      }
     }
     if (tail) k_ploc_tail<<<1, kTailThreads, tail_smem(), st>>>(B, radius);
     k_ploc_root<<<1, 256, 0, st>>>(ws.nodes, 2 * n - 1, B.ctrl);

@@ -1048,9 +1048,27 @@ cudaError_t treelet_rounds_run(Workspace& ws, uint32_t n, int rounds, cudaStream
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        if ((e = cudaLaunchKernelEx(&cfg, k_tl_narrow, ws.nodes, (const uint32_t*)list, (const uint32_t*)off, ctl,
-                                    ws.scratch + L.status)) != cudaSuccess)
+        e = ws.no_cooperative ? cudaErrorNotSupported
+                              : cudaLaunchKernelEx(&cfg, k_tl_narrow, ws.nodes, (const uint32_t*)list,
+                                                   (const uint32_t*)off, ctl, ws.scratch + L.status);
+        if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+          // no co-resident grid (a client limited to part of the GPU, or asked for): the
+          // remaining heights as one grow + dp launch each, driven from the host
+          (void)cudaGetLastError();
+          ws.tl_narrow = false;
+          if (!ws.ploc_host && (e = cudaMallocHost(&ws.ploc_host, 64)) != cudaSuccess) return e;
+          if ((e = cudaMemcpyAsync(ws.ploc_host, ctl, 12, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+              (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return e;
+          if (!ws.ploc_host[0])
+            for (uint32_t h = ws.ploc_host[2]; h <= ws.ploc_host[1]; ++h) {
+              k_tl_grow<<<grow_grid, kGrowThreads, 0, st>>>(ws.nodes, list, off, ctl, desc, stride);
+              k_tl_dp<kTlMax><<<g_dp_grid[dev], kLvThreads, 0, st>>>(ws.nodes, off, ctl, desc, stride);
+              k_tl_step<false><<<1, 32, 0, st>>>(ctl, off, 0u, cudaGraphConditionalHandle{});
+            }
+        } else if (e != cudaSuccess) {
           return e;
+        }
       }
     }
     k_treelet_fallback<<<sms * 8, 64, 0, st>>>(ws.nodes, ws.slots, epoch, (uint32_t)r, n, ctl);

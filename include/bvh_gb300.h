@@ -152,6 +152,13 @@ typedef struct bvh_batch {
  * conditional graph nodes (profilers) and drivers without them. */
 #define BVH_HOST_DRIVEN_LOOPS 1
 
+/* bvh_params.reserved[2]: 1 = launch no cooperative kernel.  PLOC's middle iterations and LBVH+'s
+ * last, narrow tree heights normally run as one cooperative launch each, with grid barriers; here
+ * they run one launch per kernel and iteration (or height), driven from the host, which is also
+ * what a build does by itself when the device refuses the cooperative launch (a client limited
+ * to part of the GPU).  Same tree; slower. */
+#define BVH_NO_COOPERATIVE 1
+
 typedef struct bvh_ctx bvh_ctx;
 
 const char* bvh_status_string(bvh_status s);
