@@ -245,6 +245,138 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
   }
 }
 
+// The large iterations take a second form of the same search, which moves a third of the
+// shared-memory bytes: thread t owns kNcP consecutive clusters x0 .. x0 + 3, so each window box
+// it loads serves all four (r + 3 loads for 4r pairs instead of 4r), and the backward candidates
+// a thread produces for one later cluster are reduced to one (area, index) entry before they go
+// through the shared-memory table.  Both searches pick the smallest (area, index) pair in each
+// direction, so they give the same neighbours.  The first H = ceil(r / kNcP) threads of a tile hold
+// the r clusters before it: they only feed backward candidates.  Window boxes are stored with one
+// pad slot per 8, so that lanes reading every fourth box hit distinct banks.
+constexpr int kNcP = 4;      // consecutive clusters per thread
+constexpr int kNcQ = 4;      // thread distances per table round
+constexpr int kNcMaxR = 64;  // larger radii keep the strided form
+__host__ __device__ constexpr int nc_pad(int w) { return w + (w >> 3); }
+__host__ __device__ constexpr int nc_span(int r) { return kPlocThreads * kNcP + r + kNcP; }  // + reads past the last pair
+static size_t nc_smem(int r) {
+  const int h = (r + kNcP - 1) / kNcP;
+  return 2 * 16 * (size_t)nc_pad(nc_span(r)) + 8 * (size_t)kNcQ * kNcP * (kPlocThreads + h);
+}
+
+template <bool SEG, bool CHECK>
+__device__ __forceinline__ void nc_pairs(int r, int c, int x0, int o, const float4 (&a)[kNcP], const float4 (&b)[kNcP],
+                                         float4 jl, float4 jh, float (&fd)[kNcP], int (&fj)[kNcP], float& pa,
+                                         int& ps) {
+#pragma unroll
+  for (int m = 0; m < kNcP; ++m) {
+    if (m < o && o - m <= r) {
+      float d = pair_d<SEG>(a[m], b[m], jl, jh);
+      if (CHECK && !(x0 + m >= 0 && x0 + o < c)) d = __int_as_float(0x7f800000);
+      if (d < fd[m]) {  // increasing o: the first of equal areas stays
+        fd[m] = d;
+        fj[m] = x0 + o;
+      }
+      if (d < pa) {  // increasing m: the smaller index stays
+        pa = d;
+        ps = x0 + m;
+      }
+    }
+  }
+}
+
+template <bool SEG, bool CHECK>
+__device__ __forceinline__ void nc_tile(const PlocBufs& B, int r, int c, int lo, int h, const float4* s_lo,
+                                        const float4* s_hi, float2* sT) {
+  constexpr int P = kNcP, Q = kNcQ;
+  const int t = threadIdx.x, tw = kPlocThreads + h;
+  const int x0 = lo + P * t;
+  const float kInf = __int_as_float(0x7f800000);
+  float4 a[P], b[P];
+  float fd[P], ed[P];
+  int fj[P], ej[P];
+#pragma unroll
+  for (int m = 0; m < P; ++m) {
+    a[m] = s_lo[nc_pad(P * t + m)];
+    b[m] = s_hi[nc_pad(P * t + m)];
+    fd[m] = ed[m] = kInf;
+    fj[m] = ej[m] = -1;
+  }
+  // pairs among the thread's own clusters
+#pragma unroll
+  for (int o = 1; o < P; ++o) {
+    float pa = kInf;
+    int ps = -1;
+    nc_pairs<SEG, CHECK>(r, c, x0, o, a, b, a[o], b[o], fd, fj, pa, ps);
+    if (pa < ed[o] || (pa == ed[o] && ps < ej[o])) {
+      ed[o] = pa;
+      ej[o] = ps;
+    }
+  }
+  // pairs with the clusters of the threads q = 1 .. h further on, Q distances per table round
+  for (int q0 = 1; q0 <= h; q0 += Q) {
+    const int qn = min(Q, h - q0 + 1);
+    for (int s = 0; s < qn; ++s) {
+      const int q = q0 + s;
+#pragma unroll
+      for (int mp = 0; mp < P; ++mp) {
+        const int o = P * q + mp;
+        const int w = nc_pad(P * t + o);
+        float pa = kInf;
+        int ps = -1;
+        nc_pairs<SEG, CHECK>(r, c, x0, o, a, b, s_lo[w], s_hi[w], fd, fj, pa, ps);
+        sT[(s * P + mp) * tw + t + q] = make_float2(pa, __int_as_float(ps));
+      }
+    }
+    __syncthreads();
+    for (int s = 0; s < qn; ++s) {
+#pragma unroll
+      for (int mp = 0; mp < P; ++mp) {
+        const float2 e = sT[(s * P + mp) * tw + t];
+        const int es = __float_as_int(e.y);
+        if (e.x < ed[mp] || (e.x == ed[mp] && es < ej[mp])) {  // the smaller index wins ties
+          ed[mp] = e.x;
+          ej[mp] = es;
+        }
+      }
+    }
+    __syncthreads();  // the table is refilled by the next round
+  }
+  if (t >= h) {
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+      const int x = x0 + m;
+      if (x < c) B.nbr[x] = (ej[m] >= 0 && ed[m] <= fd[m]) ? ej[m] : fj[m];  // earlier index wins ties
+    }
+  }
+}
+
+template <bool SEG>
+__device__ __forceinline__ void nn_tiles_consec(const PlocBufs& B, int r, uint32_t c, const Box* __restrict__ cbox,
+                                                float4* sw) {
+  const int h = (r + kNcP - 1) / kNcP;            // halo threads = the largest thread distance of a pair
+  const int out = (kPlocThreads - h) * kNcP;      // clusters a tile decides
+  const int span = kPlocThreads * kNcP + r;       // boxes staged: the halo, the tile, r past it
+  float4* s_lo = sw;
+  float4* s_hi = sw + nc_pad(nc_span(r));
+  float2* sT = reinterpret_cast<float2*>(s_hi + nc_pad(nc_span(r)));  // [kNcQ][kNcP][threads + h]
+  const int t = threadIdx.x;
+  for (uint32_t tb = blockIdx.x * (uint32_t)out; tb < c; tb += gridDim.x * (uint32_t)out) {
+    const int lo = (int)tb - kNcP * h;  // window position 0; may be negative
+    __syncthreads();                    // previous tile's window no longer read
+    for (int k = t; k < span; k += kPlocThreads) {
+      const int j = lo + k;
+      if (j >= 0 && j < (int)c) {
+        const float4* bp = reinterpret_cast<const float4*>(cbox + j);
+        s_lo[nc_pad(k)] = __ldcg(bp);
+        s_hi[nc_pad(k)] = __ldcg(bp + 1);
+      }
+    }
+    __syncthreads();
+    if (lo >= 0 && lo + span <= (int)c) nc_tile<SEG, false>(B, r, (int)c, lo, h, s_lo, s_hi, sT);
+    else nc_tile<SEG, true>(B, r, (int)c, lo, h, s_lo, s_hi, sT);
+  }
+}
+
 template <bool SEG>
 __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   extern __shared__ float4 sw[];
@@ -254,7 +386,8 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(PlocBufs B, int r) {
   // one tile's latency: smaller tiles (2 or 1 clusters per thread) then spread it over more
   // blocks.  The result does not depend on the tiling.
   const uint32_t g = gridDim.x * (uint32_t)kPlocThreads;
-  if (c > 2u * g) nn_tiles<kNnPer, SEG>(B, r, c, cbox, sw);
+  if (c > 2u * g && r <= kNcMaxR) nn_tiles_consec<SEG>(B, r, c, cbox, sw);
+  else if (c > 2u * g) nn_tiles<kNnPer, SEG>(B, r, c, cbox, sw);
   else if (c > g) nn_tiles<2, SEG>(B, r, c, cbox, sw);
   else nn_tiles<1, SEG>(B, r, c, cbox, sw);
 }
@@ -1128,7 +1261,10 @@ cudaError_t workspace_reserve_ploc(Workspace& ws, uint32_t n) {
   return cudaSuccess;
 }
 
-static size_t nn_smem(int radius) { return 32 * (kNnTile + 2 * (size_t)radius) + 4 * (size_t)kNnKc * kNnTile; }
+static size_t nn_smem(int radius) {
+  const size_t strided = 32 * (kNnTile + 2 * (size_t)radius) + 4 * (size_t)kNnKc * kNnTile;
+  return radius <= kNcMaxR ? std::max(strided, nc_smem(radius)) : strided;
+}
 
 // Persistent grids sized for n, capped at `bps` blocks per SM (the workspace's launch shapes).
 struct PlocShape {
