@@ -251,16 +251,18 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
 // a thread produces for one later cluster are reduced to one (area, index) entry before they go
 // through the shared-memory table.  Both searches pick the smallest (area, index) pair in each
 // direction, so they give the same neighbours.  The first H = ceil(r / kNcP) threads of a tile hold
-// the r clusters before it: they only feed backward candidates.  Window boxes are stored with one
-// pad slot per 8, so that lanes reading every fourth box hit distinct banks.
+// the r clusters before it: they only feed backward candidates.  Window box w is stored at
+// w ^ ((w >> 3) & 3), which puts the 16-byte boxes that 8 lanes read -- every fourth box, or 8
+// consecutive ones -- in distinct bank groups.
 constexpr int kNcP = 4;      // consecutive clusters per thread
 constexpr int kNcQ = 4;      // thread distances per table round
 constexpr int kNcMaxR = 64;  // larger radii keep the strided form
-__host__ __device__ constexpr int nc_pad(int w) { return w + (w >> 3); }
-__host__ __device__ constexpr int nc_span(int r) { return kPlocThreads * kNcP + r + kNcP; }  // + reads past the last pair
+__host__ __device__ constexpr int nc_swz(int w) { return w ^ ((w >> 3) & 3); }
+// boxes staged: the halo, the tile, r past it, + kNcP read past the last pair; rounded to 8
+__host__ __device__ constexpr int nc_span(int r) { return (kPlocThreads * kNcP + r + kNcP + 7) & ~7; }
 static size_t nc_smem(int r) {
   const int h = (r + kNcP - 1) / kNcP;
-  return 2 * 16 * (size_t)nc_pad(nc_span(r)) + 8 * (size_t)kNcQ * kNcP * (kPlocThreads + h);
+  return 2 * 16 * (size_t)nc_span(r) + 8 * (size_t)kNcQ * kNcP * (kPlocThreads + h);
 }
 
 template <bool SEG, bool CHECK>
@@ -296,8 +298,8 @@ __device__ __forceinline__ void nc_tile(const PlocBufs& B, int r, int c, int lo,
   int fj[P], ej[P];
 #pragma unroll
   for (int m = 0; m < P; ++m) {
-    a[m] = s_lo[nc_pad(P * t + m)];
-    b[m] = s_hi[nc_pad(P * t + m)];
+    a[m] = s_lo[nc_swz(P * t + m)];
+    b[m] = s_hi[nc_swz(P * t + m)];
     fd[m] = ed[m] = kInf;
     fj[m] = ej[m] = -1;
   }
@@ -320,7 +322,7 @@ __device__ __forceinline__ void nc_tile(const PlocBufs& B, int r, int c, int lo,
 #pragma unroll
       for (int mp = 0; mp < P; ++mp) {
         const int o = P * q + mp;
-        const int w = nc_pad(P * t + o);
+        const int w = nc_swz(P * t + o);
         float pa = kInf;
         int ps = -1;
         nc_pairs<SEG, CHECK>(r, c, x0, o, a, b, s_lo[w], s_hi[w], fd, fj, pa, ps);
@@ -357,8 +359,8 @@ __device__ __forceinline__ void nn_tiles_consec(const PlocBufs& B, int r, uint32
   const int out = (kPlocThreads - h) * kNcP;      // clusters a tile decides
   const int span = kPlocThreads * kNcP + r;       // boxes staged: the halo, the tile, r past it
   float4* s_lo = sw;
-  float4* s_hi = sw + nc_pad(nc_span(r));
-  float2* sT = reinterpret_cast<float2*>(s_hi + nc_pad(nc_span(r)));  // [kNcQ][kNcP][threads + h]
+  float4* s_hi = sw + nc_span(r);
+  float2* sT = reinterpret_cast<float2*>(s_hi + nc_span(r));  // [kNcQ][kNcP][threads + h]
   const int t = threadIdx.x;
   for (uint32_t tb = blockIdx.x * (uint32_t)out; tb < c; tb += gridDim.x * (uint32_t)out) {
     const int lo = (int)tb - kNcP * h;  // window position 0; may be negative
@@ -367,8 +369,8 @@ __device__ __forceinline__ void nn_tiles_consec(const PlocBufs& B, int r, uint32
       const int j = lo + k;
       if (j >= 0 && j < (int)c) {
         const float4* bp = reinterpret_cast<const float4*>(cbox + j);
-        s_lo[nc_pad(k)] = __ldcg(bp);
-        s_hi[nc_pad(k)] = __ldcg(bp + 1);
+        s_lo[nc_swz(k)] = __ldcg(bp);
+        s_hi[nc_swz(k)] = __ldcg(bp + 1);
       }
     }
     __syncthreads();
