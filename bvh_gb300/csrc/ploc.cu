@@ -256,7 +256,7 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
 // consecutive ones -- in distinct bank groups.
 constexpr int kNcP = 4;      // consecutive clusters per thread
 constexpr int kNcQ = 4;      // thread distances per table round
-constexpr int kNcMaxR = 64;  // larger radii keep the strided form
+constexpr int kNcMaxR = 128;  // larger radii keep the strided form (a halo of 32 threads at 128)
 __host__ __device__ constexpr int nc_swz(int w) { return w ^ ((w >> 3) & 3); }
 // boxes staged: the halo, the tile, r past it, + kNcP read past the last pair; rounded to 8
 __host__ __device__ constexpr int nc_span(int r) { return (kPlocThreads * kNcP + r + kNcP + 7) & ~7; }
