@@ -146,9 +146,9 @@ __device__ __forceinline__ uint32_t warp_match_bits(uint32_t d) {
   uint32_t m = 0xffffffffu;
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
-    const bool bit = (d >> b) & 1u;
-    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-    m &= bit ? bal : ~bal;
+    const uint32_t s = 0u - ((d >> b) & 1u);  // all ones where this lane's bit is set
+    const uint32_t bal = __ballot_sync(0xffffffffu, s != 0u);
+    m &= ~(bal ^ s);  // the lanes whose bit equals this lane's
   }
   return m;
 }

@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(256) k_morton(MeshPtrs m, uint32_t n, int vec4
 // k_onesweep: one stable LSD pass over an 8-bit digit with decoupled look-back
 // ---------------------------------------------------------------------------------------
 constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr int kMatchWords = 260;  // a warp's peer-mask words: 256 digits, items past n, padding
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 
@@ -288,22 +289,33 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan_u64(unsigned 
 }
 
 // Stable warp-local ranking of the warp's 32 x IPT items (item k of lane l is the warp's item
-// 32k + l, so (k, lane) order is input order).  NB = 8 for a full tile; NB = 9 gives the items
-// past n the digit 256, which is matched but never counted.  The leader of each group of equal
-// digits reserves the group's slots with one shared atomic; the atomics of one warp execute in
-// issue order, so earlier items of a digit always get the lower ranks.
-template <int NB, typename K, int IPT>
+// 32k + l, so (k, lane) order is input order).  The lanes holding one digit find each other
+// through the warp's peer-mask word for that digit: each ORs its lane bit in, and after the
+// warp's shared-memory writes are visible each reads the mask (one atomic and one load per
+// item, where a ballot per digit bit costs 8 votes and their masking).  Items past n (PARTIAL
+// tiles) use a word of their own and are never counted.  The leader of each group (its highest
+// lane) clears the word and reserves the group's slots with one shared atomic; the atomics of
+// one warp execute in issue order, so earlier items of a digit always get the lower ranks.
+template <bool PARTIAL, typename K, int IPT>
 __device__ __forceinline__ void warp_rank(const K (&key)[IPT], uint32_t (&rnk)[IPT], int shift, uint32_t wbase,
-                                          uint32_t n, uint32_t* wh, uint32_t lane) {
+                                          uint32_t n, uint32_t* wh, uint32_t* wm, uint32_t lane) {
   const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
-    uint32_t d = (uint32_t)(key[k] >> shift) & 255u;
-    if (NB > 8 && wbase + (uint32_t)k * 32u + lane >= n) d = 256u;
-    const uint32_t peers = warp_match_bits<NB>(d);
+    const uint32_t d = (uint32_t)(key[k] >> shift) & 255u;
+    const bool valid = !PARTIAL || wbase + (uint32_t)k * 32u + lane < n;
+    const uint32_t slot = valid ? d : 256u;
+    atomicOr(wm + slot, 1u << lane);
+    __syncwarp();
+    const uint32_t peers = wm[slot];
     const uint32_t leader = 31u - __clz(peers);
+    __syncwarp();  // every lane has read its mask before the leaders clear them
     uint32_t old = 0;
-    if (lane == leader && d < 256u) old = atomicAdd(wh + d, (uint32_t)__popc(peers));
+    if (lane == leader) {
+      wm[slot] = 0u;
+      if (valid) old = atomicAdd(wh + d, (uint32_t)__popc(peers));
+    }
+    __syncwarp();  // the words are clear before the next item marks them
     rnk[k] = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt);
   }
 }
@@ -322,11 +334,13 @@ __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict_
   uint32_t* s_gdelta = s_whist + NW * BINS;   // BINS: output position of tile item i is s_gdelta[digit] + i
   unsigned long long* s_scan = reinterpret_cast<unsigned long long*>(s_gdelta + 2 * BINS);  // 32
   uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_scan + 32);
+  uint32_t* s_match = s_tile + 4;             // NW x kMatchWords: peer masks per digit (+ items past n)
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int shift = 8 * pass;  // digit `pass` of the key
   if (tid == 0) *s_tile = atomicAdd(scratch + L.counters + pass, 1u);
   for (int b = tid; b < NW * BINS; b += THREADS) s_whist[b] = 0;
+  for (int b = tid; b < NW * kMatchWords; b += THREADS) s_match[b] = 0;
   __syncthreads();
   const uint32_t tile = *s_tile;
   const uint32_t base = tile * (uint32_t)TILE;
@@ -343,8 +357,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_onesweep(const K* __restrict_
     val[k] = ok ? (vin ? __ldcs(vin + idx) : idx) : 0u;
   }
   uint32_t* wh = s_whist + w * BINS;
-  if (base + (uint32_t)TILE <= n) warp_rank<8>(key, rnk, shift, wbase, n, wh, (uint32_t)lane);
-  else warp_rank<9>(key, rnk, shift, wbase, n, wh, (uint32_t)lane);
+  uint32_t* wm = s_match + w * kMatchWords;
+  if (base + (uint32_t)TILE <= n) warp_rank<false>(key, rnk, shift, wbase, n, wh, wm, (uint32_t)lane);
+  else warp_rank<true>(key, rnk, shift, wbase, n, wh, wm, (uint32_t)lane);
   __syncthreads();
   // per bin: the tile count, its exclusive scan over bins, and each warp's offset in tile order
   const int b = tid;
@@ -416,7 +431,8 @@ template <typename K, int IPT, int W, int MINB>
 constexpr SortVariant make_variant() {
   return SortVariant{reinterpret_cast<const void*>(&k_onesweep<K, kSortThreads, IPT, W, MINB>), IPT, W, MINB,
                      (size_t)kSortThreads * IPT * sizeof(K) + (size_t)kSortThreads * IPT * 4 +
-                         (size_t)(kSortThreads / 32) * 256 * 4 + 2 * 256 * 4 + 32 * 8 + 16};
+                         (size_t)(kSortThreads / 32) * 256 * 4 + 2 * 256 * 4 + 32 * 8 + 16 +
+                         (size_t)(kSortThreads / 32) * kMatchWords * 4};
 }
 
 static const SortVariant kVariants[] = {
