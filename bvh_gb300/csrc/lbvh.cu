@@ -436,7 +436,7 @@ constexpr SortVariant make_variant() {
 }
 
 static const SortVariant kVariants[] = {
-    make_variant<uint32_t, 16, 32, 2>(), make_variant<uint32_t, 16, 16, 3>(), make_variant<uint32_t, 12, 32, 3>(),
+    make_variant<uint32_t, 16, 32, 2>(), make_variant<uint32_t, 16, 16, 3>(), make_variant<uint32_t, 24, 16, 2>(),
     make_variant<uint32_t, 8, 32, 4>(),  make_variant<uint32_t, 24, 32, 2>(),
 };
 constexpr int kNumVariants = 5;
