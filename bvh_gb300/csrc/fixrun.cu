@@ -13,8 +13,8 @@
 // k_fixrun_split_short: one thread per 4 consecutive positions, with the next thread's 4 (from
 // the adjacent lane) as an 8-position window.  A thread owns the runs that START in its 4
 // positions (a run's first position differs from its predecessor).  A run that ends inside the
-// window is ranked in registers (rank = count of smaller (L, position) pairs; pairs take one
-// compare) and only its values move; a longer one is appended to a list, which
+// window is ordered in registers by (L, position) -- a pair by one compare, a longer run by an
+// 8-input sorting network -- and only its values move; a longer one is appended to a list, which
 // k_fixrun_split_long ranks by counting in shared memory (up to 1024 items) or sorts with a
 // block-wide stable LSD over L through idle buffers.  Other threads read positions of a run only
 // for H, which a permutation within the run does not change.
@@ -114,19 +114,24 @@ __device__ void block_sort_run(unsigned long long* keys, uint32_t* vals, unsigne
   }
 }
 
-// Stable rank of window item i among the window items [j, j + m) by (L, window position).
-__device__ __forceinline__ uint32_t window_rank(const unsigned long long (&w)[8], int j, int m, int i,
-                                                unsigned long long lmask) {
-  const unsigned long long li = w[i] & lmask;
-  uint32_t r = 0;
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    if (q >= j && q < j + m) {
-      const unsigned long long lq = w[q] & lmask;
-      r += (lq < li) || (lq == li && q < i);
-    }
-  }
-  return r;
+// Ascending sort of 8 (key, value) pairs in registers: Batcher's odd-even merge network,
+// 19 compare-exchanges.
+__device__ __forceinline__ void cx(unsigned long long& ka, uint32_t& va, unsigned long long& kb, uint32_t& vb) {
+  const bool sw = ka > kb;
+  const unsigned long long k0 = sw ? kb : ka, k1 = sw ? ka : kb;
+  const uint32_t v0 = sw ? vb : va, v1 = sw ? va : vb;
+  ka = k0;
+  kb = k1;
+  va = v0;
+  vb = v1;
+}
+__device__ __forceinline__ void sort8(unsigned long long (&k)[8], uint32_t (&v)[8]) {
+  cx(k[0], v[0], k[1], v[1]); cx(k[2], v[2], k[3], v[3]); cx(k[4], v[4], k[5], v[5]); cx(k[6], v[6], k[7], v[7]);
+  cx(k[0], v[0], k[2], v[2]); cx(k[1], v[1], k[3], v[3]); cx(k[4], v[4], k[6], v[6]); cx(k[5], v[5], k[7], v[7]);
+  cx(k[1], v[1], k[2], v[2]); cx(k[5], v[5], k[6], v[6]);
+  cx(k[0], v[0], k[4], v[4]); cx(k[1], v[1], k[5], v[5]); cx(k[2], v[2], k[6], v[6]); cx(k[3], v[3], k[7], v[7]);
+  cx(k[2], v[2], k[4], v[4]); cx(k[3], v[3], k[5], v[5]);
+  cx(k[1], v[1], k[2], v[2]); cx(k[3], v[3], k[4], v[4]); cx(k[5], v[5], k[6], v[6]);
 }
 
 // delta(k, k+1) + 1 of codes held split (the value of the delta pass on whole 64-bit codes:
@@ -245,31 +250,22 @@ __global__ void __launch_bounds__(256, 4) k_fixrun_split_short(const uint32_t* _
       if (DELTA) D[s] = delta_lo(la, lb, v[j], v[j + 1]);
       continue;
     }
-    unsigned long long w[8];  // L in the window slots of the run (positions order the ties)
+    // a run of 3 or more inside the window: an 8-input sorting network over (L, slot) puts its
+    // items in order (slots outside the run sort last); position j + r takes the r-th item
+    unsigned long long sk[8];
+    uint32_t sv[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) w[i] = (i >= j && i < j + m) ? (unsigned long long)lw[i] : 0ull;
-    uint32_t rk[8];
+    for (int i = 0; i < 8; ++i) {
+      sk[i] = (i >= j && i < j + m) ? ((unsigned long long)lw[i] << 3) | (unsigned)i : ~0ull;
+      sv[i] = v[i];
+    }
+    sort8(sk, sv);
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-      rk[i] = (i >= j && i < j + m) ? window_rank(w, j, m, i, ~0ull) + (uint32_t)j : (uint32_t)i;
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      if (i >= j && i < j + m && rk[i] != (uint32_t)i) vals[p0 + rk[i]] = v[i];
-    if (DELTA) {
-      // inner positions: item i lands at p0 + rk[i]; its successor is the item ranked next
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        if (i >= j && i < j + m && rk[i] + 1 < (uint32_t)(j + m)) {
-          uint32_t ls = 0, vs = 0;
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            if (q >= j && q < j + m && rk[q] == rk[i] + 1) {
-              ls = (uint32_t)w[q];
-              vs = v[q];
-            }
-          }
-          D[p0 + rk[i]] = delta_lo((uint32_t)w[i], ls, v[i], vs);
-        }
+    for (int r = 0; r < 8; ++r) {
+      if (r < m) {
+        if ((int)(sk[r] & 7ull) != j + r) vals[p0 + j + r] = sv[r];
+        if (DELTA && r + 1 < m)
+          D[p0 + j + r] = delta_lo((uint32_t)(sk[r] >> 3), (uint32_t)(sk[r + 1] >> 3), sv[r], sv[r + 1]);
       }
     }
   }
