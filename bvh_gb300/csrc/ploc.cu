@@ -245,8 +245,8 @@ __device__ __forceinline__ void nn_tiles(const PlocBufs& B, int r, uint32_t c, c
   }
 }
 
-// The large iterations take a second form of the same search, which moves a third of the
-// shared-memory bytes: thread t owns kNcP consecutive clusters x0 .. x0 + 3, so each window box
+// The large iterations take a second form of the same search (ploc_builder.cu:173-209), which
+// moves about half the shared-memory bytes: thread t owns kNcP consecutive clusters x0 .. x0 + 3, so each window box
 // it loads serves all four (r + 3 loads for 4r pairs instead of 4r), and the backward candidates
 // a thread produces for one later cluster are reduced to one (area, index) entry before they go
 // through the shared-memory table.  Both searches pick the smallest (area, index) pair in each
