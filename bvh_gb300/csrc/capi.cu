@@ -32,10 +32,18 @@ struct TuneEntry {
   uint32_t grid_max = 0xffffffffu;  // PLOC: k_ploc_grid from this many live clusters (0: never)
 };
 
+// Base shapes of a new context: the sort variant by mesh size (-1) until bvh_tuning_set or
+// bvh_autotune picks one.
+static TuneEntry by_size() {
+  TuneEntry t;
+  t.sort_variant = -1;
+  return t;
+}
+
 struct bvh_ctx {
   int device = 0;
   Workspace ws;
-  TuneEntry base;                 // shapes where no table entry matches (bvh_tuning_set sets its sort variant)
+  TuneEntry base = by_size();     // shapes where no table entry matches (bvh_tuning_set sets its sort variant)
   std::vector<TuneEntry> table;   // bvh_autotune_build / bvh_tuning_import
   bool tuning_locked = false;     // bvh_autotune_build sets the shapes itself
   unsigned long long* hash_buf = nullptr;  // device word for tree_hash
@@ -204,6 +212,7 @@ static void apply_tuning(bvh_ctx* ctx, int32_t algo_key, uint32_t n) {
       return;
     }
   set_shapes(ctx->ws, ctx->base);
+  if (ctx->base.sort_variant < 0) ctx->ws.sort_variant = default_sort_variant(n);
 }
 
 static bvh_status build_impl(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_params* params, cudaStream_t st,

@@ -445,6 +445,10 @@ static const SortVariant& variant(int v) { return kVariants[v < 0 || v >= kNumVa
 
 int sort_variant_count() { return kNumVariants; }
 int sort_variant_tile(int v) { return kSortThreads * variant(v).ipt; }
+// The variant a build uses where nothing chose one, by key count (clustered meshes, GB300): small
+// tiles fill the GPU below ~600k keys (8 keys per thread), 16 keys per thread win around 1M, and
+// 24 keys with the 16-wide window from ~2M (10M LBVH-63 sort 0.334 vs 0.371 ms with 16 keys).
+int default_sort_variant(uint32_t n) { return n < 600000u ? 3 : n < 2000000u ? 0 : 2; }
 void sort_variant_describe(int v, int* ipt, int* window, int* minb) {
   const SortVariant& sv = variant(v);
   *ipt = sv.ipt;

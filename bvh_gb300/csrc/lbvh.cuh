@@ -106,6 +106,7 @@ ScratchLayout scratch_layout(uint32_t n);
 int sort_tile();  // smallest tile over all variants (sizes the look-back scratch)
 int sort_variant_count();
 int sort_variant_tile(int v);
+int default_sort_variant(uint32_t n);  // by key count, where no tuning chose a variant
 void sort_variant_describe(int v, int* ipt, int* window, int* minb);
 // Times every onesweep variant on `n` pseudo-random 32-bit keys and keeps the fastest in ws.
 cudaError_t autotune_sort(Workspace& ws, uint32_t n, cudaStream_t st, float* ms_out /* per variant */);

@@ -104,6 +104,7 @@ extern "C" bvh_status bvh_build_lbvh_static(const bvh_mesh_soa* mesh, int32_t mo
     ws.epoch_builds = g_epoch_builds[device];
     g_epoch_builds[device] = ws.epoch_builds + 1;
   }
+  ws.sort_variant = default_sort_variant(n);
   cudaError_t e = lbvh_build(ws, m, n, morton_bits, 0, reinterpret_cast<cudaStream_t>(stream), nullptr, &out_idx);
   if (e != cudaSuccess) return BVH_ERR_DEVICE;
   return out_idx == indices ? BVH_OK : BVH_ERR_DEVICE;

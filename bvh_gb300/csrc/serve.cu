@@ -229,6 +229,7 @@ static cudaError_t launch_one(bvh_server* sv, Slot& s) {
     (k < 3 ? rp.o[k] : rp.d[k - 3]) = d;
   }
   uint32_t* idx = nullptr;
+  s.ws.sort_variant = default_sort_variant(n);
   if ((e = lbvh_build(s.ws, m, n, sv->cfg.morton_bits, 0, s.stream, nullptr, &idx)) != cudaSuccess) return e;
   float* ht = reinterpret_cast<float*>(s.hits);
   int32_t* hi = reinterpret_cast<int32_t*>(s.hits);

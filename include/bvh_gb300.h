@@ -221,7 +221,9 @@ bvh_status bvh_build_batched(bvh_ctx* ctx, const bvh_batch* batch, const bvh_par
  * 30-bit codes whole, the high halves of longer codes), keeps the fastest in the context and
  * writes a JSON table of the timings to json_out (may be NULL).  Synchronous. */
 bvh_status bvh_autotune(bvh_ctx* ctx, uint32_t n, void* stream, char* json_out, size_t json_cap);
-/* Read or set the sort variant a context uses (0 .. 4) where no tuning-table entry applies. */
+/* Read the sort variant of the context's last build, or set the one it uses (0 .. 4) where no
+ * tuning-table entry applies.  Until set (here or by bvh_autotune) a build picks it by mesh size:
+ * 8 keys per thread below 600k triangles, 16 up to 2M, 24 (16-wide look-back window) above. */
 bvh_status bvh_tuning_get(const bvh_ctx* ctx, int32_t* variant);
 bvh_status bvh_tuning_set(bvh_ctx* ctx, int32_t variant);
 

@@ -178,3 +178,23 @@ def test_autotune_table(ctx, gpu, oracle_lib):
     nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=63))
     onodes, oidx, _ = oracle_lib.lbvh(m.arrays(), 63)
     assert np.array_equal(idx, oidx) and oracle_lib.node_fields_equal(nodes, onodes)
+
+
+def test_untuned_context_picks_sort_variant_by_size(gpu, oracle_lib):
+    """Without bvh_tuning_set or an autotune, a build sorts with the variant its size calls for
+    (8 keys per thread below 600k triangles, 24 keys from 2M) and still equals the oracle."""
+    O = oracle_lib
+    ctx = Context(0)
+    try:
+        for n, want in ((100_000, 3), (2_500_000, 2)):
+            m = meshgen.clustered(n, seed=40 + n % 7)
+            nodes, idx, _, _ = build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=63))
+            assert ctx.tuning() == want
+            onodes, oidx, _ = O.lbvh(m.arrays(), 63)
+            assert np.array_equal(idx, oidx) and O.node_fields_equal(nodes, onodes)
+        ctx.set_tuning(0)  # an explicit choice holds for every size
+        m = meshgen.clustered(100_000, seed=43)
+        build(ctx, gpu, m, ctx.params(C.ALGO_LBVH, morton_bits=30))
+        assert ctx.tuning() == 0
+    finally:
+        ctx.close()
