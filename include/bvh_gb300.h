@@ -243,7 +243,9 @@ bvh_status bvh_autotune_build(bvh_ctx* ctx, const bvh_mesh_soa* mesh, const bvh_
                               char* json_out, size_t json_cap);
 /* The tuning table as JSON ({"base": {...}, "entries": [{"algo", "bucket", "sort_variant",
  * "ploc_tail_pairs", "ploc_nn_bps", "ploc_mg_bps", "ploc_grid_max"}, ...]}), to persist it; and back (replaces the
- * table; BVH_ERR_INVALID_ARG for malformed input or out-of-range shapes). */
+ * table; BVH_ERR_INVALID_ARG for malformed input or out-of-range shapes).  The base entry is
+ * informational (import reads only "entries"); its sort_variant is -1 while builds pick the
+ * variant by mesh size. */
 bvh_status bvh_tuning_export(const bvh_ctx* ctx, char* json_out, size_t json_cap);
 bvh_status bvh_tuning_import(bvh_ctx* ctx, const char* json);
 
