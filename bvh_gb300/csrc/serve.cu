@@ -347,6 +347,7 @@ static cudaError_t launch_batch(bvh_server* sv, Slot& s) {
   MeshPtrs mp;
   for (int k = 0; k < 9; ++k) mp.v[k] = s.mesh + s.tri_cap * k;
   StageEvents none;
+  s.ws.sort_variant = default_sort_variant(n);
   if ((e = batched_build(s.ws, mp, n, s.d_meta + ML.offsets, count,
                          reinterpret_cast<const SegItem*>(s.d_meta + ML.items), n_items, s.mbox, s.indices, s.stream,
                          &none)) != cudaSuccess)
